@@ -1,0 +1,343 @@
+"""Benchmark of the Flockers continuous-space step (boid-updates/s).
+
+Workload (default): 1,048,576 boids, f32, density 0.025 boids per unit^2
+(torus side 6476.34), radius 10, discretization 10/1.5, all weights 1.0,
+jump 0.7, uniform positions and unit headings, seed 7.  A "step" is one
+Schedule::step of the whole flock: the agent pass (every Bird::step) and the
+field's lazy_update, on inputs resident in HBM.  L2 is flushed (a 512 MiB
+write) before every timed step; the JSON line says so.
+
+  python bench.py [--steps K] [--warmup W] [--workload c2|c1|c3] [--impl ours|reference]
+
+--impl reference times the reference-equivalent CPU path (the oracle's
+priority-queue schedule, one host core: the reference's sequential path is
+single-threaded) on the same workload, a bounded number of steps.
+Under torchrun each rank runs an independent replica on its own GPU (the
+step does not shard: replicas only) and rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+D_C = float(np.float32(10.0) / np.float32(1.5))
+WORKLOADS = {
+    # name: (n, side, seed, generator, sim steps of the workload)
+    "c1": dict(n=1000, side=200.0, seed=42, gen="uniform", steps=200,
+               desc="Flockers 1,000 boids, torus 200x200"),
+    "c2": dict(n=1 << 20, side=float(np.float32(np.sqrt((1 << 20) / 0.025))), seed=7,
+               gen="uniform", steps=1000,
+               desc="Flockers 1,048,576 boids, density 0.025 (torus side 6476.34)"),
+    "c3": dict(n=1 << 22, side=12952.0, seed=11, gen="clustered", steps=500,
+               desc="Flockers 4,194,304 boids in 256 Gaussian clusters (sigma 40), torus 12952"),
+}
+METRIC = "boid-updates/s (1M boids, 1 GB300)"
+UNIT = "boid-updates/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gen(wl):
+    import krabmaga_gb300 as kg
+
+    if wl["gen"] == "uniform":
+        return kg.gen_uniform(wl["n"], wl["side"], wl["side"], wl["seed"], 1.0)
+    return kg.gen_clustered(wl["n"], wl["side"], wl["side"], 256, 40.0, 0.3, wl["seed"])
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference(wl, steps):
+    """The oracle's reference-equivalent run: returns (boid-updates/s, sample text)."""
+    import oracle
+
+    ids, xy, dxy = gen(wl)
+    p = oracle.params(seed=wl["seed"], query_mode=0)
+    secs, _ = oracle.simulate_timed(wl["side"], wl["side"], D_C, p, ids, xy, dxy, steps)
+    return wl["n"] * steps / secs, (f"{wl['desc']}, {steps} steps through the priority-queue "
+                                    f"schedule (oracle restatement of the reference, 1 core)")
+
+
+def run_reference(args, wl):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    steps = max(1, min(args.steps, args.ref_steps))
+    value, sample = cpu_reference(wl, steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": steps, "warmup": 0, "ms_per_step": 1e3 * wl["n"] / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Philox uniform flock)",
+        "config": {"workload": wl["desc"], "global_batch": wl["n"], "parallelism": "cpu",
+                   "host": platform.machine()},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl):
+    import torch
+
+    import krabmaga_gb300 as kg
+    from krabmaga_gb300 import _lib as L
+
+    ws, rank, local = dist_setup()
+    dev = local
+    torch.cuda.set_device(dev)
+    n, side = wl["n"], wl["side"]
+    ids, xy, dxy = gen(wl)
+    params = kg.FlockParams(seed=wl["seed"], query_mode=kg.KB_QUERY_RELAX,
+                            arith=kg.KB_ARITH_FAST if args.arith == "fast" else kg.KB_ARITH_STRICT)
+    pc = params.to_c()
+
+    f = kg.Field2D(side, side, D_C, True, device=dev, capacity_hint=n)
+    f.set_locations(ids, xy, dxy)
+    f.lazy_update()
+    stream = torch.cuda.ExternalStream(f.cuda_stream(), device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def one_step(t):
+        L.call("kb_flock_compute", f.handle, C.byref(pc), C.c_uint64(t))
+        L.call("kb_field_lazy_update", f.handle)
+
+    step_no = 0
+    for _ in range(args.warmup):
+        one_step(step_no)
+        step_no += 1
+    f.synchronize()
+
+    K = args.steps
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.fill_(k & 0xFF)  # evict L2 between timed steps
+                ev[k][0].record(stream)
+                L.call("kb_flock_compute", f.handle, C.byref(pc), C.c_uint64(step_no))
+                ev[k][1].record(stream)
+                L.call("kb_field_lazy_update", f.handle)
+                ev[k][2].record(stream)
+                step_no += 1
+        torch.cuda.synchronize(dev)
+    f.synchronize()  # raises if a kernel set the device error word
+    barrier(ws)
+    step_ms = [ev[k][0].elapsed_time(ev[k][2]) for k in range(K)]
+    force_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
+    total_s = allmax(ws, sum(step_ms) / 1e3)
+    value = ws * n * K / total_s
+
+    # warm-L2 throughput (no flush, graph-replayed steps), informational
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    warm_steps = min(200, max(10, K))
+    with torch.cuda.stream(stream):
+        L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(step_no), C.c_uint32(warm_steps))
+        step_no += warm_steps
+        e0.record(stream)
+        L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(step_no), C.c_uint32(warm_steps))
+        step_no += warm_steps
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    warm_value = n * warm_steps / (e0.elapsed_time(e1) / 1e3)
+
+    # e2e: the public API from host arrays to host arrays, one whole simulation
+    e2e_steps = wl["steps"] if not args.e2e_steps else args.e2e_steps
+    pinned = [torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).pin_memory()
+              for a in (ids, xy, dxy)]
+    out_ids = torch.empty(n, dtype=torch.int32).pin_memory()
+    out_st = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    e2e_times = []
+    for _ in range(args.e2e_reps):
+        barrier(ws)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        g = kg.Field2D(side, side, D_C, True, device=dev, capacity_hint=n)
+        L.call("kb_field_set_locations", g.handle, C.c_size_t(n),
+               C.cast(pinned[0].data_ptr(), L._U32), C.cast(pinned[1].data_ptr(), L._F),
+               C.cast(pinned[2].data_ptr(), L._F))
+        L.call("kb_field_lazy_update", g.handle)
+        L.call("kb_flock_step", g.handle, C.byref(pc), C.c_uint64(0), C.c_uint32(e2e_steps))
+        cnt = C.c_size_t()
+        L.call("kb_field_get_state", g.handle, C.cast(out_ids.data_ptr(), L._U32),
+               C.cast(out_st.data_ptr(), L._F), C.c_size_t(n), C.byref(cnt))
+        t1 = time.perf_counter()
+        g.close()
+        e2e_times.append(allmax(ws, t1 - t0))
+    e2e_t = min(e2e_times)
+    e2e_value = ws * n * e2e_steps / e2e_t
+    h2d = n * (4 + 8 + 8)
+    d2h = n * (4 + 16)
+
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    ncells = (int(np.ceil(np.float32(side) / np.float32(D_C))) + 1) ** 2
+    force_bytes = n * 32 + ncells * 4  # state read+write per boid, bag offsets read
+    force_s = statistics.mean(force_ms) / 1e3
+    achieved = force_bytes / force_s / 1e9
+    clocks = clk.summary()
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        cval, sample = cpu_reference(wl, args.cpu_steps)
+        cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
+        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Philox uniform flock)",
+        "config": {"workload": wl["desc"], "global_batch": n * ws, "seq_len": None,
+                   "parallelism": f"replicas{ws}", "arith": args.arith, "query": "relax",
+                   "l2": "flushed (512 MiB write) before every timed step",
+                   "warm_l2_value": warm_value},
+        "roofline": {"bound": "hbm", "kernel": "k_flock_force", "achieved": achieved,
+                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "algorithmic_bytes_per_launch": force_bytes,
+                     "force_ms_mean": statistics.mean(force_ms),
+                     "step_ms_mean": statistics.mean(step_ms)},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
+                "d2h_bytes_per_step": d2h / e2e_steps, "h2d_bytes_per_call": h2d,
+                "d2h_bytes_per_call": d2h,
+                "call": f"Field2D create + set_locations + lazy_update + {e2e_steps} steps + "
+                        f"get_state, host arrays in and out"},
+        "gpu_launches": 3 * K,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "strict"])
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--ref-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--e2e-reps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/*
+ * krabgpu.h -- C ABI of the GB300 continuous-space agent step.
+ *
+ * The drop-in boundary for krABMaga's Field2D + Flockers path.  Every entry
+ * point below names the reference item it replaces (file:line within the
+ * krABMaga 0.6.1 tree).  Conventions:
+ *   - opaque handles; the library owns all device memory, host arrays are
+ *     caller-owned and copied;
+ *   - every call returns kb_status (KB_OK = 0); no exception, abort or panic
+ *     crosses the ABI; kb_last_error() gives a message for the calling thread;
+ *   - one handle per host thread (the reference Field2D is !Sync: RefCell);
+ *     calls are ordered on the handle's own CUDA stream and the calls that
+ *     return host data synchronise that stream;
+ *   - positions are f32 (Real2D, src/engine/location.rs:17-22), ids u32
+ *     (Bird::id, tests/model/flockers/bird.rs:21).
+ */
+#ifndef KRABGPU_H
+#define KRABGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t kb_status;
+#define KB_OK 0
+#define KB_ERR_ARG 1         /* bad argument (null pointer, size, non-finite geometry) */
+#define KB_ERR_OOM 2         /* device or pinned allocation failed */
+#define KB_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define KB_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+#define KB_ERR_DEVICE_FLAG 5 /* a kernel raised its error word (see kb_field_device_flags) */
+#define KB_ERR_STATE 6       /* call not valid in the handle's current state */
+#define KB_ERR_RANGE 7       /* a location maps outside the bag matrix: the reference panics */
+#define KB_ERR_NO_DEVICE 8   /* no CUDA device / the library cannot run here */
+#define KB_ERR_BUSY 9        /* admission refused (serving budget or slot table full) */
+
+/* Device error-word bits (kb_field_device_flags). */
+#define KB_FLAG_KEY_RANGE 0x1u     /* a position discretised outside the bag matrix */
+#define KB_FLAG_REBIN_MISS 0x2u    /* a boid moved more than one cell in one step */
+#define KB_FLAG_SPIN_TIMEOUT 0x4u  /* a bounded spin-wait expired */
+#define KB_FLAG_NONFINITE 0x8u     /* a non-finite position was produced */
+
+/* Query kinds: which Field2D neighbour query the flock step uses. */
+#define KB_QUERY_RELAX 0 /* get_neighbors_within_relax_distance, field_2d.rs:472-516 */
+#define KB_QUERY_EXACT 1 /* get_neighbors_within_distance, field_2d.rs:386-440 (in-tree Bird) */
+
+/* Arithmetic of the flock step. */
+#define KB_ARITH_STRICT 0 /* IEEE f32 with the reference's rounding points: bit-exact */
+#define KB_ARITH_FAST 1   /* approximate division/sqrt; within 1e-5 of domain vs FP64 */
+
+typedef struct kb_field kb_field;
+
+/* Field2D::new(w, h, d, toroidal), field_2d.rs:304-322. */
+typedef struct {
+    float width;
+    float height;
+    float discretization;
+    int32_t toroidal;
+    int32_t device;         /* CUDA ordinal */
+    uint32_t capacity_hint; /* expected object count (storage grows as needed) */
+} kb_field_desc;
+
+/* The Flockers constants (bird.rs:12-17) and query radius (bird.rs:41) as a
+ * parameter block; seed keys the Philox jitter stream that replaces
+ * rand::rng() (bird.rs:113-117). */
+typedef struct {
+    float cohesion;
+    float avoidance;
+    float consistency;
+    float randomness;
+    float momentum;
+    float jump;
+    float neighbor_radius;
+    int32_t query_mode; /* KB_QUERY_* */
+    int32_t arith;      /* KB_ARITH_* */
+    uint32_t _pad;
+    uint64_t seed;
+} kb_flock_params;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* kb_last_error(void);
+/* Library version string. */
+const char* kb_version(void);
+/* Number of visible CUDA devices (0 if none); never fails. */
+int32_t kb_device_count(void);
+
+/* ------------------------------------------------------------------ Field2D */
+
+/* Field2D::new -- field_2d.rs:304-322 */
+kb_status kb_field_create(const kb_field_desc* desc, kb_field** out);
+kb_status kb_field_destroy(kb_field* f);
+/* dw, dh, max_x = ceil(w/d), max_y = ceil(h/d) -- field_2d.rs:316-317, 396-397 */
+kb_status kb_field_dims(const kb_field* f, int32_t out4[4]);
+
+/* set_object_location(object, loc) -- field_2d.rs:838-846.  The object is
+ * {id, pos, last_d}; loc picks its bag.  Goes to the write buffer. */
+kb_status kb_field_set_object_location(kb_field* f, uint32_t id, const float pos[2],
+                                       const float last_d[2], const float loc[2]);
+/* Bulk form: n objects, each placed at its own position (what Flocker::init,
+ * state.rs:41-56, and Bird::step, bird.rs:151-153, do). xy and dxy are n*2. */
+kb_status kb_field_set_locations(kb_field* f, size_t n, const uint32_t* ids, const float* xy,
+                                 const float* dxy);
+/* remove_object_location(object, loc) -- field_2d.rs:885-898 (write buffer). */
+kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float loc[2]);
+/* Field::lazy_update -- field_2d.rs:905-921: the write buffer becomes the
+ * read buffer and a new empty write buffer starts. */
+kb_status kb_field_lazy_update(kb_field* f);
+/* *nagents (field_2d.rs:276, counted by set_object_location until the first
+ * lazy_update). */
+kb_status kb_field_num_agents(kb_field* f, size_t* out);
+/* Objects in the read buffer. */
+kb_status kb_field_num_objects(kb_field* f, size_t* out);
+
+/* Neighbour queries against the read buffer.  ids (and, if non-NULL,
+ * states = {x, y, dx, dy} per object) receive up to cap objects in the
+ * reference's visiting order; *n receives the full count.
+ * get_neighbors_within_relax_distance -- field_2d.rs:472-516 */
+kb_status kb_field_get_neighbors_within_relax_distance(kb_field* f, const float loc[2], float dist,
+                                                       uint32_t* ids, float* states, size_t cap,
+                                                       size_t* n);
+/* get_neighbors_within_distance -- field_2d.rs:386-440 */
+kb_status kb_field_get_neighbors_within_distance(kb_field* f, const float loc[2], float dist,
+                                                 uint32_t* ids, float* states, size_t cap,
+                                                 size_t* n);
+/* get_objects -- field_2d.rs:544-549 (read buffer bag at loc) */
+kb_status kb_field_get_objects(kb_field* f, const float loc[2], uint32_t* ids, float* states,
+                               size_t cap, size_t* n);
+/* get_objects_unbuffered -- field_2d.rs:577-582 (write buffer bag at loc) */
+kb_status kb_field_get_objects_unbuffered(kb_field* f, const float loc[2], uint32_t* ids,
+                                          float* states, size_t cap, size_t* n);
+/* num_objects_at_location -- field_2d.rs:803-808 */
+kb_status kb_field_num_objects_at_location(kb_field* f, const float loc[2], size_t* n);
+/* get_empty_bags -- field_2d.rs:727-739: (i*d, j*d) of every empty read bag,
+ * i (x) outer. xy holds cap pairs. */
+kb_status kb_field_get_empty_bags(kb_field* f, float* xy, size_t cap, size_t* n);
+/* get_random_empty_bag -- field_2d.rs:764-772; the reference's unseeded rng
+ * becomes Philox(seed).  *found = 0 when no bag is empty (None). */
+kb_status kb_field_get_random_empty_bag(kb_field* f, uint64_t seed, float xy[2], int32_t* found);
+/* iter_objects / iter_objects_unbuffered -- field_2d.rs:619-640 / 677-698:
+ * every object with its bag's real position, bags i-outer, j-inner, each bag
+ * in insertion order.  buffered = 1 for the read buffer, 0 for the write one.
+ * cell_xy (2 per object), ids, states (4 per object) may be NULL. */
+kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, uint32_t* ids,
+                                float* states, size_t cap, size_t* n);
+
+/* --------------------------------------------------------------- Flockers */
+
+/* One Schedule::step agent pass for the Flockers model (schedule.rs:395-408
+ * running Bird::step, bird.rs:39-154, for every bird): reads the read
+ * buffer, writes every bird's next state into the (empty) write buffer.
+ * `step` keys the jitter stream. */
+kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step);
+/* nsteps full steps: compute + lazy_update each (schedule.rs:395-412), with
+ * step numbers first_step ... first_step+nsteps-1.  The read buffer must
+ * hold the flock and the write buffer must be empty (call lazy_update after
+ * initialisation, as Schedule::step does at step 0, schedule.rs:349-351). */
+kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                        uint32_t nsteps);
+/* Read buffer in its stored order (bags ascending, insertion order inside a
+ * bag): ids and {x, y, dx, dy} states; either may be NULL. */
+kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n);
+/* Error word raised by this handle's kernels since the last clear (KB_FLAG_*). */
+kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear);
+/* Wait for the handle's stream; returns KB_ERR_DEVICE_FLAG if a kernel
+ * raised the error word. */
+kb_status kb_field_synchronize(kb_field* f);
+/* The handle's CUDA stream (a cudaStream_t), for recording events or
+ * ordering other work against the handle's kernels. */
+kb_status kb_field_cuda_stream(kb_field* f, void** stream);
+
+/* Parity support.  For nq query points (qxy, 2 per point) against the read
+ * buffer: counts[q] = candidate count of the query kind (KB_QUERY_*), and if
+ * ids != NULL the candidate ids packed in visiting order (cap entries max;
+ * *total = sum of counts). */
+kb_status kb_field_neighbor_lists(kb_field* f, int32_t kind, float dist, size_t nq,
+                                  const float* qxy, uint32_t* counts, uint32_t* ids, size_t cap,
+                                  size_t* total);
+/* Per query point: candidate count and an order-independent 32-bit digest of
+ * the candidate ids (sum of a 32-bit mix of each id). */
+kb_status kb_field_neighbor_digest(kb_field* f, int32_t kind, float dist, size_t nq,
+                                   const float* qxy, uint32_t* counts, uint32_t* digest);
+
+/* ------------------------------------------------------------ workloads */
+
+/* Uniform flock: ids 0..n-1, pos = (w*u1, h*u2), heading a uniform unit
+ * vector scaled by heading_scale (0 gives the reference's last_d = (0,0),
+ * state.rs:47), all drawn from Philox(seed).  Host-only; needs no GPU. */
+kb_status kb_gen_uniform(size_t n, float w, float h, uint64_t seed, float heading_scale,
+                         uint32_t* ids, float* xy, float* dxy);
+/* Clustered flock: nclusters isotropic Gaussian clusters (sigma) with
+ * uniform centres on a w x h torus, positions wrapped; headings share the
+ * cluster's angle plus N(0, angle_sigma) noise.  Host-only. */
+kb_status kb_gen_clustered(size_t n, float w, float h, uint32_t nclusters, float sigma,
+                           float angle_sigma, uint64_t seed, uint32_t* ids, float* xy, float* dxy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KRABGPU_H */

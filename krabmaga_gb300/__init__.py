@@ -1,0 +1,21 @@
+"""krabmaga_gb300 -- GB300-native continuous-space agent step for krABMaga.
+
+The compute runs in ``libkrabgpu.so`` (hand-written sm_103a kernels behind the
+C ABI of include/krabgpu.h); this package is its Python host binding with the
+reference's API names (Field2D, State, Schedule, simulate, Flocker).
+"""
+from . import _lib
+from ._lib import KbError, lib, LIB_PATH, KB_QUERY_RELAX, KB_QUERY_EXACT, KB_ARITH_STRICT, KB_ARITH_FAST
+from .field import Bird, Field2D, Real2D
+from .model import (FlockParams, Flocker, Schedule, State, gen_clustered, gen_uniform, simulate,
+                    simulate_old)
+
+__all__ = [
+    "Bird", "Field2D", "Real2D", "FlockParams", "Flocker", "Schedule", "State", "simulate",
+    "simulate_old", "gen_uniform", "gen_clustered", "KbError", "lib", "LIB_PATH",
+    "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
+]
+
+
+def device_count() -> int:
+    return int(lib.kb_device_count())

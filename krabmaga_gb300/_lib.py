@@ -1,0 +1,147 @@
+"""ctypes binding of libkrabgpu.so (the C ABI declared in include/krabgpu.h).
+
+The shared library is built in place by ``__graft_entry__.build()`` (or
+``make -C krabmaga_gb300``).  There is no fallback: if the library is missing
+or cannot load, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libkrabgpu.so")
+
+KB_OK = 0
+KB_ERR_ARG = 1
+KB_ERR_OOM = 2
+KB_ERR_CUDA = 3
+KB_ERR_TIMEOUT = 4
+KB_ERR_DEVICE_FLAG = 5
+KB_ERR_STATE = 6
+KB_ERR_RANGE = 7
+KB_ERR_NO_DEVICE = 8
+KB_ERR_BUSY = 9
+
+KB_QUERY_RELAX = 0
+KB_QUERY_EXACT = 1
+KB_ARITH_STRICT = 0
+KB_ARITH_FAST = 1
+
+STATUS_NAMES = {
+    0: "KB_OK", 1: "KB_ERR_ARG", 2: "KB_ERR_OOM", 3: "KB_ERR_CUDA", 4: "KB_ERR_TIMEOUT",
+    5: "KB_ERR_DEVICE_FLAG", 6: "KB_ERR_STATE", 7: "KB_ERR_RANGE", 8: "KB_ERR_NO_DEVICE",
+    9: "KB_ERR_BUSY",
+}
+
+
+class KbError(RuntimeError):
+    """A libkrabgpu call returned a non-zero kb_status."""
+
+    def __init__(self, status: int, func: str, msg: str):
+        self.status = status
+        super().__init__(f"{func}: {STATUS_NAMES.get(status, status)}: {msg}")
+
+
+class FieldDesc(C.Structure):
+    _fields_ = [
+        ("width", C.c_float),
+        ("height", C.c_float),
+        ("discretization", C.c_float),
+        ("toroidal", C.c_int32),
+        ("device", C.c_int32),
+        ("capacity_hint", C.c_uint32),
+    ]
+
+
+class FlockParamsC(C.Structure):
+    _fields_ = [
+        ("cohesion", C.c_float),
+        ("avoidance", C.c_float),
+        ("consistency", C.c_float),
+        ("randomness", C.c_float),
+        ("momentum", C.c_float),
+        ("jump", C.c_float),
+        ("neighbor_radius", C.c_float),
+        ("query_mode", C.c_int32),
+        ("arith", C.c_int32),
+        ("_pad", C.c_uint32),
+        ("seed", C.c_uint64),
+    ]
+
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+    )
+lib = C.CDLL(LIB_PATH)
+
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_U32 = C.POINTER(C.c_uint32)
+_SZ = C.POINTER(C.c_size_t)
+
+_SIGS = {
+    "kb_last_error": (C.c_char_p, []),
+    "kb_version": (C.c_char_p, []),
+    "kb_device_count": (C.c_int32, []),
+    "kb_field_create": (C.c_int32, [C.POINTER(FieldDesc), C.POINTER(_P)]),
+    "kb_field_destroy": (C.c_int32, [_P]),
+    "kb_field_dims": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
+    "kb_field_cuda_stream": (C.c_int32, [_P, C.POINTER(_P)]),
+    "kb_field_set_object_location": (C.c_int32, [_P, C.c_uint32, _F, _F, _F]),
+    "kb_field_set_locations": (C.c_int32, [_P, C.c_size_t, _U32, _F, _F]),
+    "kb_field_remove_object_location": (C.c_int32, [_P, C.c_uint32, _F]),
+    "kb_field_lazy_update": (C.c_int32, [_P]),
+    "kb_field_num_agents": (C.c_int32, [_P, _SZ]),
+    "kb_field_num_objects": (C.c_int32, [_P, _SZ]),
+    "kb_field_get_neighbors_within_relax_distance": (
+        C.c_int32, [_P, _F, C.c_float, _U32, _F, C.c_size_t, _SZ]),
+    "kb_field_get_neighbors_within_distance": (
+        C.c_int32, [_P, _F, C.c_float, _U32, _F, C.c_size_t, _SZ]),
+    "kb_field_get_objects": (C.c_int32, [_P, _F, _U32, _F, C.c_size_t, _SZ]),
+    "kb_field_get_objects_unbuffered": (C.c_int32, [_P, _F, _U32, _F, C.c_size_t, _SZ]),
+    "kb_field_num_objects_at_location": (C.c_int32, [_P, _F, _SZ]),
+    "kb_field_get_empty_bags": (C.c_int32, [_P, _F, C.c_size_t, _SZ]),
+    "kb_field_get_random_empty_bag": (C.c_int32, [_P, C.c_uint64, _F, C.POINTER(C.c_int32)]),
+    "kb_field_iter_objects": (C.c_int32, [_P, C.c_int32, _F, _U32, _F, C.c_size_t, _SZ]),
+    "kb_flock_compute": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64]),
+    "kb_flock_step": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_uint32]),
+    "kb_field_get_state": (C.c_int32, [_P, _U32, _F, C.c_size_t, _SZ]),
+    "kb_field_device_flags": (C.c_int32, [_P, _U32, C.c_int32]),
+    "kb_field_synchronize": (C.c_int32, [_P]),
+    "kb_field_neighbor_lists": (
+        C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32, C.c_size_t, _SZ]),
+    "kb_field_neighbor_digest": (
+        C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
+    "kb_gen_uniform": (C.c_int32, [C.c_size_t, C.c_float, C.c_float, C.c_uint64, C.c_float,
+                                   _U32, _F, _F]),
+    "kb_gen_clustered": (C.c_int32, [C.c_size_t, C.c_float, C.c_float, C.c_uint32, C.c_float,
+                                     C.c_float, C.c_uint64, _U32, _F, _F]),
+}
+
+for _name, (_res, _args) in _SIGS.items():
+    _fn = getattr(lib, _name)
+    _fn.restype = _res
+    _fn.argtypes = _args
+
+
+def last_error() -> str:
+    return (lib.kb_last_error() or b"").decode()
+
+
+def check(status: int, func: str) -> None:
+    if status != KB_OK:
+        raise KbError(status, func, last_error())
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib, name)(*args), name)
+
+
+def fptr(a):
+    return a.ctypes.data_as(_F) if a is not None else None
+
+
+def uptr(a):
+    return a.ctypes.data_as(_U32) if a is not None else None

@@ -1,0 +1,930 @@
+// kb_api.cpp -- host runtime behind include/krabgpu.h: field handles, the
+// write-buffer bookkeeping of Field2D, step orchestration with CUDA-graph
+// replay, and the Field2D query entry points.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/krabgpu.h"
+#include "kb_common.h"
+#include "kb_launch.h"
+#include "kb_runtime.h"
+
+namespace kb {
+
+thread_local std::string g_last_error;
+
+kb_status fail(kb_status code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+kb_status cuda_fail(cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(KB_ERR_OOM, m);
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return fail(KB_ERR_NO_DEVICE, m);
+    return fail(KB_ERR_CUDA, m);
+}
+
+// Host copy of discretize + bag index (field_2d.rs:328-339, 840-841) for
+// argument checks on API writes; the same IEEE f32 operations as the device.
+int64_t host_bag_index(const Rep& R, float x, float y) {
+    int32_t cx = as_i32(std::floor(x / R.d));
+    int32_t cy = as_i32(std::floor(y / R.d));
+    int32_t idx = (int32_t)((uint32_t)cx * (uint32_t)R.dh + (uint32_t)cy);
+    if (idx < 0 || (uint32_t)idx >= R.ncells) return -1;
+    return idx;
+}
+
+bool make_rep_geometry(float w, float h, float d, int toroidal, Rep* R, std::string* why) {
+    if (!(std::isfinite(w) && std::isfinite(h) && std::isfinite(d)) || w <= 0.f || h <= 0.f ||
+        d <= 0.f) {
+        *why = "width, height and discretization must be finite and positive";
+        return false;
+    }
+    std::memset(R, 0, sizeof(*R));
+    R->w = w;
+    R->h = h;
+    R->d = d;
+    R->toroidal = toroidal ? 1 : 0;
+    const float cw = std::ceil(w / d), ch = std::ceil(h / d);
+    if (cw > 1.0e8f || ch > 1.0e8f || (double)(cw + 1.0f) * (double)(ch + 1.0f) > 2.0e9) {
+        *why = "bag matrix too large (more than 2e9 bags)";
+        return false;
+    }
+    R->max_x = as_i32(cw);
+    R->max_y = as_i32(ch);
+    R->dw = R->max_x + 1;
+    R->dh = R->max_y + 1;
+    R->ncells = (uint32_t)R->dw * (uint32_t)R->dh;
+    return true;
+}
+
+void set_rep_params(Rep* R, const kb_flock_params* p) {
+    R->coh = p->cohesion;
+    R->avo = p->avoidance;
+    R->con = p->consistency;
+    R->rnd = p->randomness;
+    R->mom = p->momentum;
+    R->jump = p->jump;
+    R->radius = p->neighbor_radius;
+    R->dd = (p->neighbor_radius <= 0.0f) ? -1 : as_i32(std::floor(p->neighbor_radius / R->d));
+    R->qmode = p->query_mode;
+    R->seed_lo = (uint32_t)p->seed;
+    R->seed_hi = (uint32_t)(p->seed >> 32);
+}
+
+bool params_ok(const kb_flock_params* p, std::string* why) {
+    const float v[7] = {p->cohesion, p->avoidance, p->consistency, p->randomness,
+                        p->momentum, p->jump,      p->neighbor_radius};
+    for (float x : v)
+        if (!std::isfinite(x)) {
+            *why = "flock parameters must be finite";
+            return false;
+        }
+    if (p->query_mode != KB_QUERY_RELAX && p->query_mode != KB_QUERY_EXACT) {
+        *why = "query_mode must be KB_QUERY_RELAX or KB_QUERY_EXACT";
+        return false;
+    }
+    if (p->arith != KB_ARITH_STRICT && p->arith != KB_ARITH_FAST) {
+        *why = "arith must be KB_ARITH_STRICT or KB_ARITH_FAST";
+        return false;
+    }
+    return true;
+}
+
+// The stencil-gather rebin needs every boid to land within one bag of where
+// it was (or across the seam): a move shorter than a bag, and y wrapped by
+// the same length as x (bird.rs:147 wraps y with the width).
+bool fast_rebin_ok(const Rep& R) {
+    return R.w == R.h && R.max_x == R.max_y && std::fabs(R.jump) * 1.001f < R.d && R.max_x >= 3;
+}
+
+}  // namespace kb
+
+using namespace kb;
+
+// ========================================================================
+struct kb_field {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Rep rep{};                  // geometry + last parameters
+    DevBuf<Rep> d_rep;
+    // read buffer
+    uint32_t cap = 0;
+    DevBuf<float4> rst;
+    DevBuf<uint32_t> rid;
+    DevBuf<uint32_t> start[2];
+    int cur = 0;
+    uint32_t rn = 0;
+    // write list
+    DevBuf<float4> wst;
+    DevBuf<uint32_t> wid, wkey;
+    DevBuf<uint8_t> wdead;
+    uint32_t wn = 0;
+    bool w_from_compute = false;   // write list == one flock pass over the read buffer
+    bool w_has_dead = false;
+    bool layout_is_positions = true;  // every stored bag == discretize(own pos)
+    std::vector<float4> p_st;
+    std::vector<uint32_t> p_id, p_key;
+    bool p_loc_differs = false;
+    // step temporaries
+    DevBuf<uint32_t> hist, cursor, tid, tsrc;
+    DevBuf<float4> tst;
+    DevBuf<ScanCtl> scan_ctl, aux_ctl;
+    DevBuf<unsigned long long> tstate, aux_tstate;
+    uint32_t aux_tiles = 0;
+    DevBuf<uint32_t> err;
+    DevBuf<unsigned long long> dstep;
+    DevBuf<uint32_t> small;  // 16 words of scratch for counts
+    // Field2D bookkeeping (field_2d.rs:276, 284-287)
+    size_t nagents = 0;
+    bool density_check = false;
+    // graphs: (steps per graph, start parity, params) -> exec
+    struct GraphKey {
+        uint32_t steps;
+        int parity;
+        std::vector<uint8_t> params;
+        bool operator<(const GraphKey& o) const {
+            if (steps != o.steps) return steps < o.steps;
+            if (parity != o.parity) return parity < o.parity;
+            return params < o.params;
+        }
+    };
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    uint64_t buffers_version = 0;
+    uint64_t graphs_version = 0;
+
+    ~kb_field() {
+        drop_graphs();
+        if (stream) cudaStreamDestroy(stream);
+    }
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        cudaGetDevice(&now);
+        if (prev >= 0 && now != prev) cudaSetDevice(prev);
+    }
+};
+
+#define KB_CUDA(call)                                   \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+kb_status grow(kb_field* f, uint32_t need) {
+    if (need <= f->cap) return KB_OK;
+    uint64_t nc = std::max<uint64_t>(need, (uint64_t)f->cap * 2);
+    if (nc < 1024) nc = 1024;
+    if (nc > 0xFFFFFFF0ull) nc = 0xFFFFFFF0ull;
+    if (need > nc) return fail(KB_ERR_ARG, "object count exceeds 2^32-16");
+    const uint32_t c = (uint32_t)nc;
+    DevBuf<float4> rst, wst, tst;
+    DevBuf<uint32_t> rid, wid, wkey, tid, tsrc;
+    DevBuf<uint8_t> wdead;
+    cudaError_t e;
+    if ((e = rst.alloc(c)) || (e = wst.alloc(c)) || (e = tst.alloc(c)) || (e = rid.alloc(c)) ||
+        (e = wid.alloc(c)) || (e = wkey.alloc(c)) || (e = tid.alloc(c)) || (e = tsrc.alloc(c)) ||
+        (e = wdead.alloc(c)))
+        return cuda_fail(e, "growing object storage");
+    if (f->rn) {
+        KB_CUDA(cudaMemcpyAsync(rst.p, f->rst.p, sizeof(float4) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(rid.p, f->rid.p, sizeof(uint32_t) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
+    }
+    if (f->wn) {
+        KB_CUDA(cudaMemcpyAsync(wst.p, f->wst.p, sizeof(float4) * f->wn, cudaMemcpyDeviceToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(wid.p, f->wid.p, sizeof(uint32_t) * f->wn, cudaMemcpyDeviceToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(wkey.p, f->wkey.p, sizeof(uint32_t) * f->wn, cudaMemcpyDeviceToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(wdead.p, f->wdead.p, f->wn, cudaMemcpyDeviceToDevice, f->stream));
+    }
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    f->rst.swap(rst); f->wst.swap(wst); f->tst.swap(tst);
+    f->rid.swap(rid); f->wid.swap(wid); f->wkey.swap(wkey);
+    f->tid.swap(tid); f->tsrc.swap(tsrc); f->wdead.swap(wdead);
+    f->cap = c;
+    f->drop_graphs();
+    return KB_OK;
+}
+
+kb_status upload_rep(kb_field* f) {
+    KB_CUDA(launch_set_rep(f->d_rep.p, f->rep, f->stream));
+    return KB_OK;
+}
+
+// Append the host-side pending writes to the device write list.
+kb_status flush_pending(kb_field* f) {
+    const size_t np = f->p_id.size();
+    if (np == 0) return KB_OK;
+    if ((uint64_t)f->wn + np > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many objects");
+    kb_status st = grow(f, f->wn + (uint32_t)np);
+    if (st) return st;
+    KB_CUDA(cudaMemcpyAsync(f->wst.p + f->wn, f->p_st.data(), sizeof(float4) * np, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemcpyAsync(f->wid.p + f->wn, f->p_id.data(), sizeof(uint32_t) * np, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemcpyAsync(f->wkey.p + f->wn, f->p_key.data(), sizeof(uint32_t) * np, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemsetAsync(f->wdead.p + f->wn, 0, np, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));  // the pending vectors are reused
+    f->wn += (uint32_t)np;
+    if (f->p_loc_differs) f->layout_is_positions = false;
+    f->p_st.clear(); f->p_id.clear(); f->p_key.clear();
+    f->p_loc_differs = false;
+    f->w_from_compute = false;
+    return KB_OK;
+}
+
+kb_status read_u32(kb_field* f, const uint32_t* dptr, uint32_t* out) {
+    KB_CUDA(cudaMemcpyAsync(out, dptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return KB_OK;
+}
+
+kb_status check_flags(kb_field* f) {
+    uint32_t flags = 0;
+    kb_status st = read_u32(f, f->err.p, &flags);
+    if (st) return st;
+    if (flags) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf,
+                      "device error word 0x%x (1 key out of range, 2 rebin miss, 4 spin "
+                      "timeout, 8 non-finite)",
+                      flags);
+        return fail(KB_ERR_DEVICE_FLAG, buf);
+    }
+    return KB_OK;
+}
+
+kb_status ensure_aux_scan(kb_field* f, uint32_t n) {
+    const uint32_t t = scan_tiles(n) + 1;
+    if (t <= f->aux_tiles) return KB_OK;
+    DevBuf<unsigned long long> ts;
+    cudaError_t e = ts.alloc(t);
+    if (e) return cuda_fail(e, "scan workspace");
+    KB_CUDA(cudaMemsetAsync(ts.p, 0, sizeof(unsigned long long) * t, f->stream));
+    f->aux_tstate.swap(ts);
+    f->aux_tiles = t;
+    return KB_OK;
+}
+
+// The general stable sort: write list -> read buffer.  hist already holds
+// the key counts when counted == true.
+kb_status general_rebuild(kb_field* f, bool counted) {
+    cudaStream_t s = f->stream;
+    const int nxt = 1 - f->cur;
+    if (!counted) KB_CUDA(launch_hist_list(f->wkey.p, f->wdead.p, f->wn, f->hist.p, s));
+    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->rep.ncells, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    KB_CUDA(launch_scatter_list(f->wkey.p, f->wdead.p, f->wst.p, f->wid.p, f->wn, f->start[nxt].p, f->cursor.p, f->tst.p, f->tid.p, f->tsrc.p, s));
+    KB_CUDA(launch_canon(f->start[nxt].p, f->rep.ncells, f->tst.p, f->tid.p, f->tsrc.p, f->cursor.p, f->rst.p, f->rid.p, s));
+    f->cur = nxt;
+    return KB_OK;
+}
+
+kb_status fast_rebuild(kb_field* f, bool bump_step) {
+    cudaStream_t s = f->stream;
+    const int nxt = 1 - f->cur;
+    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->rep.ncells, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    RebinArgs a;
+    a.reps = f->d_rep.p;
+    a.nrep = 1;
+    a.start_cur = f->start[f->cur].p;
+    a.start_next = f->start[nxt].p;
+    a.key = f->wkey.p;
+    a.a_st = f->wst.p;
+    a.a_ids = f->wid.p;
+    a.ncells = f->rep.ncells;
+    a.s_st = f->rst.p;
+    a.s_ids = f->rid.p;
+    a.step = bump_step ? f->dstep.p : nullptr;
+    a.err = f->err.p;
+    KB_CUDA(launch_rebin(a, s));
+    f->cur = nxt;
+    return KB_OK;
+}
+
+kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
+    ForceArgs a;
+    a.reps = f->d_rep.p;
+    a.nrep = 1;
+    a.st = f->rst.p;
+    a.ids = f->rid.p;
+    a.start = f->start[f->cur].p;
+    a.n = f->rn;
+    a.step = f->dstep.p;
+    a.out_st = f->wst.p;
+    a.out_ids = f->wid.p;
+    a.out_key = f->wkey.p;
+    a.hist = f->hist.p;
+    a.err = f->err.p;
+    KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
+    return KB_OK;
+}
+
+kb_status field_lazy_update(kb_field* f) {
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    // field_2d.rs:905-921: the first swap fixes nagents' density estimate.
+    if (!f->density_check) f->density_check = true;
+    if (f->w_from_compute && !f->w_has_dead) {
+        Rep R = f->rep;
+        if (fast_rebin_ok(R) && f->layout_is_positions) st = fast_rebuild(f, false);
+        else st = general_rebuild(f, true);
+        if (st) return st;
+        f->rn = f->wn;
+        f->layout_is_positions = true;
+    } else {
+        st = general_rebuild(f, false);
+        if (st) return st;
+        uint32_t total = 0;
+        st = read_u32(f, f->start[f->cur].p + f->rep.ncells, &total);
+        if (st) return st;
+        f->rn = total;
+    }
+    f->wn = 0;
+    f->w_from_compute = false;
+    f->w_has_dead = false;
+    return KB_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* kb_last_error(void) { return g_last_error.c_str(); }
+const char* kb_version(void) { return "krabgpu 0.1.0 (sm_103a)"; }
+
+int32_t kb_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
+    if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
+    *out = nullptr;
+    Rep R;
+    std::string why;
+    if (!make_rep_geometry(desc->width, desc->height, desc->discretization, desc->toroidal, &R, &why))
+        return fail(KB_ERR_ARG, why);
+    int ndev = kb_device_count();
+    if (ndev <= 0) return fail(KB_ERR_NO_DEVICE, "no CUDA device visible");
+    if (desc->device < 0 || desc->device >= ndev) return fail(KB_ERR_ARG, "bad device ordinal");
+    DeviceGuard g(desc->device);
+    kb_field* f = new kb_field();
+    f->device = desc->device;
+    f->rep = R;
+    cudaError_t e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking);
+    const uint32_t nt = scan_tiles(R.ncells) + 1;
+    if (!e) e = f->d_rep.alloc(1);
+    if (!e) e = f->start[0].alloc((size_t)R.ncells + 1);
+    if (!e) e = f->start[1].alloc((size_t)R.ncells + 1);
+    if (!e) e = f->hist.alloc(R.ncells);
+    if (!e) e = f->cursor.alloc(R.ncells);
+    if (!e) e = f->scan_ctl.alloc(1);
+    if (!e) e = f->aux_ctl.alloc(1);
+    if (!e) e = f->tstate.alloc(nt);
+    if (!e) e = f->err.alloc(1);
+    if (!e) e = f->dstep.alloc(1);
+    if (!e) e = f->small.alloc(16);
+    if (!e) e = cudaMemsetAsync(f->start[0].p, 0, sizeof(uint32_t) * ((size_t)R.ncells + 1), f->stream);
+    if (!e) e = cudaMemsetAsync(f->start[1].p, 0, sizeof(uint32_t) * ((size_t)R.ncells + 1), f->stream);
+    if (!e) e = cudaMemsetAsync(f->hist.p, 0, sizeof(uint32_t) * R.ncells, f->stream);
+    if (!e) e = cudaMemsetAsync(f->cursor.p, 0, sizeof(uint32_t) * R.ncells, f->stream);
+    if (!e) e = cudaMemsetAsync(f->scan_ctl.p, 0, sizeof(ScanCtl), f->stream);
+    if (!e) e = cudaMemsetAsync(f->aux_ctl.p, 0, sizeof(ScanCtl), f->stream);
+    if (!e) e = cudaMemsetAsync(f->tstate.p, 0, sizeof(unsigned long long) * nt, f->stream);
+    if (!e) e = cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream);
+    if (!e) e = cudaMemsetAsync(f->dstep.p, 0, sizeof(unsigned long long), f->stream);
+    if (!e) e = launch_set_rep(f->d_rep.p, f->rep, f->stream);
+    if (!e) e = cudaStreamSynchronize(f->stream);
+    if (e) {
+        delete f;
+        return cuda_fail(e, "creating field");
+    }
+    if (desc->capacity_hint) {
+        kb_status st = grow(f, desc->capacity_hint);
+        if (st) {
+            delete f;
+            return st;
+        }
+    }
+    *out = f;
+    return KB_OK;
+}
+
+kb_status kb_field_destroy(kb_field* f) {
+    if (!f) return KB_OK;
+    DeviceGuard g(f->device);
+    cudaStreamSynchronize(f->stream);
+    delete f;
+    return KB_OK;
+}
+
+kb_status kb_field_dims(const kb_field* f, int32_t out4[4]) {
+    if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
+    out4[0] = f->rep.dw;
+    out4[1] = f->rep.dh;
+    out4[2] = f->rep.max_x;
+    out4[3] = f->rep.max_y;
+    return KB_OK;
+}
+
+kb_status kb_field_cuda_stream(kb_field* f, void** stream) {
+    if (!f || !stream) return fail(KB_ERR_ARG, "null argument");
+    *stream = (void*)f->stream;
+    return KB_OK;
+}
+
+kb_status kb_field_set_object_location(kb_field* f, uint32_t id, const float pos[2],
+                                       const float last_d[2], const float loc[2]) {
+    if (!f || !pos || !last_d || !loc) return fail(KB_ERR_ARG, "null argument");
+    if (!(std::isfinite(pos[0]) && std::isfinite(pos[1]) && std::isfinite(last_d[0]) &&
+          std::isfinite(last_d[1]) && std::isfinite(loc[0]) && std::isfinite(loc[1])))
+        return fail(KB_ERR_ARG, "non-finite position or heading");
+    int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
+    if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
+    f->p_st.push_back(make_float4(pos[0], pos[1], last_d[0], last_d[1]));
+    f->p_id.push_back(id);
+    f->p_key.push_back((uint32_t)idx);
+    if (host_bag_index(f->rep, pos[0], pos[1]) != idx) f->p_loc_differs = true;
+    if (!f->density_check) f->nagents += 1;
+    f->w_from_compute = false;
+    return KB_OK;
+}
+
+kb_status kb_field_set_locations(kb_field* f, size_t n, const uint32_t* ids, const float* xy,
+                                 const float* dxy) {
+    if (!f || (n && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
+    const size_t old = f->p_id.size();
+    f->p_st.reserve(old + n);
+    f->p_id.reserve(old + n);
+    f->p_key.reserve(old + n);
+    for (size_t i = 0; i < n; ++i) {
+        if (!(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) &&
+              std::isfinite(dxy[2 * i]) && std::isfinite(dxy[2 * i + 1]))) {
+            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
+            return fail(KB_ERR_ARG, "non-finite position or heading");
+        }
+        int64_t idx = host_bag_index(f->rep, xy[2 * i], xy[2 * i + 1]);
+        if (idx < 0) {
+            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
+            char buf[128];
+            std::snprintf(buf, sizeof buf, "object %zu: location outside the bag matrix (the reference panics)", i);
+            return fail(KB_ERR_RANGE, buf);
+        }
+        f->p_st.push_back(make_float4(xy[2 * i], xy[2 * i + 1], dxy[2 * i], dxy[2 * i + 1]));
+        f->p_id.push_back(ids[i]);
+        f->p_key.push_back((uint32_t)idx);
+    }
+    if (!f->density_check) f->nagents += n;
+    if (n) f->w_from_compute = false;
+    return KB_OK;
+}
+
+kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float loc[2]) {
+    if (!f || !loc) return fail(KB_ERR_ARG, "null argument");
+    int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
+    if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
+    DeviceGuard g(f->device);
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    KB_CUDA(cudaMemsetAsync(f->small.p, 0, sizeof(uint32_t), f->stream));
+    KB_CUDA(launch_remove(f->wkey.p, f->wdead.p, f->wid.p, f->wn, (uint32_t)idx, id, f->small.p, f->stream));
+    uint32_t removed = 0;
+    st = read_u32(f, f->small.p, &removed);
+    if (st) return st;
+    if (removed) {
+        f->w_has_dead = true;
+        if (!f->density_check) f->nagents -= removed;
+    }
+    return KB_OK;
+}
+
+kb_status kb_field_lazy_update(kb_field* f) {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    return field_lazy_update(f);
+}
+
+kb_status kb_field_num_agents(kb_field* f, size_t* out) {
+    if (!f || !out) return fail(KB_ERR_ARG, "null argument");
+    *out = f->nagents;
+    return KB_OK;
+}
+
+kb_status kb_field_num_objects(kb_field* f, size_t* out) {
+    if (!f || !out) return fail(KB_ERR_ARG, "null argument");
+    *out = f->rn;
+    return KB_OK;
+}
+
+static kb_status query_points(kb_field* f, int kind, float dist, size_t nq, const float* qxy,
+                              uint32_t* counts, uint32_t* digest, uint32_t* ids, float* states,
+                              size_t cap, size_t* total) {
+    if (nq > 0x7FFFFFFFull) return fail(KB_ERR_ARG, "too many query points");
+    DeviceGuard g(f->device);
+    if (nq == 0) {
+        if (total) *total = 0;
+        return KB_OK;
+    }
+    const uint32_t n = (uint32_t)nq;
+    DevBuf<float2> dq;
+    DevBuf<uint32_t> dcounts, ddig, doff, dids;
+    DevBuf<float4> dst;
+    cudaError_t e = dq.alloc(n);
+    if (!e) e = dcounts.alloc(n);
+    if (!e && digest) e = ddig.alloc(n);
+    if (e) return cuda_fail(e, "query buffers");
+    KB_CUDA(cudaMemcpyAsync(dq.p, qxy, sizeof(float2) * n, cudaMemcpyHostToDevice, f->stream));
+    QueryArgs a;
+    a.rep = f->rep;
+    a.kind = kind;
+    a.dist = dist;
+    a.start = f->start[f->cur].p;
+    a.st = f->rst.p;
+    a.ids = f->rid.p;
+    a.nq = n;
+    a.q = dq.p;
+    a.counts = dcounts.p;
+    a.digest = digest ? ddig.p : nullptr;
+    a.offsets = nullptr;
+    a.out_ids = nullptr;
+    a.out_st = nullptr;
+    a.cap = 0;
+    KB_CUDA(launch_query(a, f->stream));
+    if (ids || states || total) {
+        kb_status st = ensure_aux_scan(f, n);
+        if (st) return st;
+        e = doff.alloc((size_t)n + 1);
+        if (e) return cuda_fail(e, "query offsets");
+        KB_CUDA(launch_scan(dcounts.p, doff.p, n, f->aux_ctl.p, f->aux_tstate.p, f->err.p, false, f->stream));
+        uint32_t tot = 0;
+        st = read_u32(f, doff.p + n, &tot);
+        if (st) return st;
+        if (total) *total = tot;
+        const uint64_t take = std::min<uint64_t>(tot, cap);
+        if ((ids || states) && take > 0) {
+            if (!e) e = dids.alloc(take);
+            if (!e && states) e = dst.alloc(take);
+            if (e) return cuda_fail(e, "query output");
+            a.offsets = doff.p;
+            a.out_ids = dids.p;
+            a.out_st = states ? dst.p : nullptr;
+            a.cap = take;
+            KB_CUDA(launch_query(a, f->stream));
+            if (ids) KB_CUDA(cudaMemcpyAsync(ids, dids.p, sizeof(uint32_t) * take, cudaMemcpyDeviceToHost, f->stream));
+            if (states) KB_CUDA(cudaMemcpyAsync(states, dst.p, sizeof(float4) * take, cudaMemcpyDeviceToHost, f->stream));
+        }
+    }
+    if (counts) KB_CUDA(cudaMemcpyAsync(counts, dcounts.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, f->stream));
+    if (digest) KB_CUDA(cudaMemcpyAsync(digest, ddig.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return KB_OK;
+}
+
+kb_status kb_field_get_neighbors_within_relax_distance(kb_field* f, const float loc[2], float dist,
+                                                       uint32_t* ids, float* states, size_t cap,
+                                                       size_t* n) {
+    if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
+    return query_points(f, KB_QUERY_RELAX, dist, 1, loc, nullptr, nullptr, ids, states, cap, n);
+}
+
+kb_status kb_field_get_neighbors_within_distance(kb_field* f, const float loc[2], float dist,
+                                                 uint32_t* ids, float* states, size_t cap,
+                                                 size_t* n) {
+    if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
+    return query_points(f, KB_QUERY_EXACT, dist, 1, loc, nullptr, nullptr, ids, states, cap, n);
+}
+
+kb_status kb_field_neighbor_lists(kb_field* f, int32_t kind, float dist, size_t nq,
+                                  const float* qxy, uint32_t* counts, uint32_t* ids, size_t cap,
+                                  size_t* total) {
+    if (!f || (nq && (!qxy || !counts))) return fail(KB_ERR_ARG, "null argument");
+    if (kind != KB_QUERY_RELAX && kind != KB_QUERY_EXACT) return fail(KB_ERR_ARG, "bad query kind");
+    size_t t = 0;
+    kb_status st = query_points(f, kind, dist, nq, qxy, counts, nullptr, ids, nullptr, cap, &t);
+    if (total) *total = t;
+    return st;
+}
+
+kb_status kb_field_neighbor_digest(kb_field* f, int32_t kind, float dist, size_t nq,
+                                   const float* qxy, uint32_t* counts, uint32_t* digest) {
+    if (!f || (nq && (!qxy || !counts || !digest))) return fail(KB_ERR_ARG, "null argument");
+    if (kind != KB_QUERY_RELAX && kind != KB_QUERY_EXACT) return fail(KB_ERR_ARG, "bad query kind");
+    return query_points(f, kind, dist, nq, qxy, counts, digest, nullptr, nullptr, 0, nullptr);
+}
+
+kb_status kb_field_get_objects(kb_field* f, const float loc[2], uint32_t* ids, float* states,
+                               size_t cap, size_t* n) {
+    if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
+    int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
+    if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
+    DeviceGuard g(f->device);
+    uint32_t se[2];
+    KB_CUDA(cudaMemcpyAsync(se, f->start[f->cur].p + idx, sizeof(se), cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    const uint32_t cnt = se[1] - se[0];
+    *n = cnt;
+    const size_t take = std::min<size_t>(cnt, cap);
+    if (take) {
+        if (ids) KB_CUDA(cudaMemcpyAsync(ids, f->rid.p + se[0], sizeof(uint32_t) * take, cudaMemcpyDeviceToHost, f->stream));
+        if (states) KB_CUDA(cudaMemcpyAsync(states, f->rst.p + se[0], sizeof(float4) * take, cudaMemcpyDeviceToHost, f->stream));
+        KB_CUDA(cudaStreamSynchronize(f->stream));
+    }
+    return KB_OK;
+}
+
+kb_status kb_field_get_objects_unbuffered(kb_field* f, const float loc[2], uint32_t* ids,
+                                          float* states, size_t cap, size_t* n) {
+    if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
+    int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
+    if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
+    DeviceGuard g(f->device);
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    DevBuf<uint32_t> dids;
+    DevBuf<float4> dst;
+    const uint64_t take = std::min<uint64_t>(cap, f->wn);
+    cudaError_t e = cudaSuccess;
+    if (take && ids) e = dids.alloc(take);
+    if (!e && take && states) e = dst.alloc(take);
+    if (e) return cuda_fail(e, "query output");
+    KB_CUDA(launch_filter_key(f->wkey.p, f->wdead.p, f->wst.p, f->wid.p, f->wn, (uint32_t)idx, dids.p, dst.p, take, f->small.p, f->stream));
+    uint32_t cnt = 0;
+    st = read_u32(f, f->small.p, &cnt);
+    if (st) return st;
+    *n = cnt;
+    const uint64_t got = std::min<uint64_t>(cnt, take);
+    if (got) {
+        if (ids) KB_CUDA(cudaMemcpyAsync(ids, dids.p, sizeof(uint32_t) * got, cudaMemcpyDeviceToHost, f->stream));
+        if (states) KB_CUDA(cudaMemcpyAsync(states, dst.p, sizeof(float4) * got, cudaMemcpyDeviceToHost, f->stream));
+        KB_CUDA(cudaStreamSynchronize(f->stream));
+    }
+    return KB_OK;
+}
+
+kb_status kb_field_num_objects_at_location(kb_field* f, const float loc[2], size_t* n) {
+    return kb_field_get_objects(f, loc, nullptr, nullptr, 0, n);
+}
+
+kb_status kb_field_get_empty_bags(kb_field* f, float* xy, size_t cap, size_t* n) {
+    if (!f || !n || (cap && !xy)) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    DevBuf<float2> dxy;
+    const uint64_t take = std::min<uint64_t>(cap, f->rep.ncells);
+    if (take) {
+        cudaError_t e = dxy.alloc(take);
+        if (e) return cuda_fail(e, "empty bag output");
+    }
+    KB_CUDA(launch_empty_bags(f->rep, f->start[f->cur].p, dxy.p, take, f->small.p, f->stream));
+    uint32_t cnt = 0;
+    kb_status st = read_u32(f, f->small.p, &cnt);
+    if (st) return st;
+    *n = cnt;
+    const uint64_t got = std::min<uint64_t>(cnt, take);
+    if (got) {
+        KB_CUDA(cudaMemcpyAsync(xy, dxy.p, sizeof(float2) * got, cudaMemcpyDeviceToHost, f->stream));
+        KB_CUDA(cudaStreamSynchronize(f->stream));
+    }
+    return KB_OK;
+}
+
+kb_status kb_field_get_random_empty_bag(kb_field* f, uint64_t seed, float xy[2], int32_t* found) {
+    if (!f || !xy || !found) return fail(KB_ERR_ARG, "null argument");
+    size_t n = 0;
+    kb_status st = kb_field_get_empty_bags(f, nullptr, 0, &n);
+    if (st) return st;
+    if (n == 0) {
+        *found = 0;
+        return KB_OK;
+    }
+    std::vector<float> all(2 * n);
+    st = kb_field_get_empty_bags(f, all.data(), n, &n);
+    if (st) return st;
+    U4 o = philox4x32_10(U4{0u, 0u, 0u, 2u}, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint64_t pick = (((uint64_t)o.y << 32) | o.x) % n;
+    xy[0] = all[2 * pick];
+    xy[1] = all[2 * pick + 1];
+    *found = 1;
+    return KB_OK;
+}
+
+kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, uint32_t* ids,
+                                float* states, size_t cap, size_t* n) {
+    if (!f || !n) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    const float4* src_st;
+    const uint32_t* src_id;
+    const uint32_t* src_start;
+    uint32_t cnt;
+    DevBuf<uint32_t> tmp_start, tmp_id, tmp_src, cursor;
+    DevBuf<float4> tmp_st, tmp_sorted;
+    DevBuf<uint32_t> tmp_sorted_id;
+    if (buffered) {
+        src_st = f->rst.p;
+        src_id = f->rid.p;
+        src_start = f->start[f->cur].p;
+        cnt = f->rn;
+    } else {
+        // stable sort of the live write list into scratch (write buffer order)
+        kb_status st = flush_pending(f);
+        if (st) return st;
+        const uint32_t nc = f->rep.ncells, w = f->wn > 0 ? f->wn : 1;
+        cudaError_t e = tmp_start.alloc((size_t)nc + 1);
+        if (!e) e = cursor.alloc(nc);
+        if (!e) e = tmp_st.alloc(w);
+        if (!e) e = tmp_id.alloc(w);
+        if (!e) e = tmp_src.alloc(w);
+        if (!e) e = tmp_sorted.alloc(w);
+        if (!e) e = tmp_sorted_id.alloc(w);
+        if (e) return cuda_fail(e, "iteration scratch");
+        KB_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(uint32_t) * nc, f->stream));
+        KB_CUDA(launch_hist_list(f->wkey.p, f->wdead.p, f->wn, cursor.p, f->stream));
+        st = ensure_aux_scan(f, nc);
+        if (st) return st;
+        KB_CUDA(launch_scan(cursor.p, tmp_start.p, nc, f->aux_ctl.p, f->aux_tstate.p, f->err.p, true, f->stream));
+        KB_CUDA(launch_scatter_list(f->wkey.p, f->wdead.p, f->wst.p, f->wid.p, f->wn, tmp_start.p, cursor.p, tmp_st.p, tmp_id.p, tmp_src.p, f->stream));
+        KB_CUDA(launch_canon(tmp_start.p, nc, tmp_st.p, tmp_id.p, tmp_src.p, cursor.p, tmp_sorted.p, tmp_sorted_id.p, f->stream));
+        st = read_u32(f, tmp_start.p + nc, &cnt);
+        if (st) return st;
+        src_st = tmp_sorted.p;
+        src_id = tmp_sorted_id.p;
+        src_start = tmp_start.p;
+    }
+    *n = cnt;
+    const size_t take = std::min<size_t>(cnt, cap);
+    if (take) {
+        if (cell_xy) {
+            DevBuf<uint32_t> cell_of;
+            DevBuf<float2> dxy;
+            cudaError_t e = cell_of.alloc(cnt);
+            if (!e) e = dxy.alloc(cnt);
+            if (e) return cuda_fail(e, "iteration output");
+            KB_CUDA(launch_cell_of(src_start, f->rep.ncells, cell_of.p, f->stream));
+            KB_CUDA(launch_cell_xy(f->rep, cell_of.p, cnt, dxy.p, f->stream));
+            KB_CUDA(cudaMemcpyAsync(cell_xy, dxy.p, sizeof(float2) * take, cudaMemcpyDeviceToHost, f->stream));
+            KB_CUDA(cudaStreamSynchronize(f->stream));
+        }
+        if (ids) KB_CUDA(cudaMemcpyAsync(ids, src_id, sizeof(uint32_t) * take, cudaMemcpyDeviceToHost, f->stream));
+        if (states) KB_CUDA(cudaMemcpyAsync(states, src_st, sizeof(float4) * take, cudaMemcpyDeviceToHost, f->stream));
+    }
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return KB_OK;
+}
+
+kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n) {
+    if (!f || !n) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    *n = f->rn;
+    const size_t take = std::min<size_t>(f->rn, cap);
+    if (take) {
+        if (ids) KB_CUDA(cudaMemcpyAsync(ids, f->rid.p, sizeof(uint32_t) * take, cudaMemcpyDeviceToHost, f->stream));
+        if (states) KB_CUDA(cudaMemcpyAsync(states, f->rst.p, sizeof(float4) * take, cudaMemcpyDeviceToHost, f->stream));
+    }
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return check_flags(f);
+}
+
+kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear) {
+    if (!f || !flags) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    kb_status st = read_u32(f, f->err.p, flags);
+    if (st) return st;
+    if (clear) {
+        KB_CUDA(cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream));
+        KB_CUDA(cudaStreamSynchronize(f->stream));
+    }
+    return KB_OK;
+}
+
+kb_status kb_field_synchronize(kb_field* f) {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return check_flags(f);
+}
+
+kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step) {
+    if (!f || !p) return fail(KB_ERR_ARG, "null argument");
+    std::string why;
+    if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
+    if (f->wn || !f->p_id.empty())
+        return fail(KB_ERR_STATE, "write buffer not empty: call lazy_update first");
+    DeviceGuard g(f->device);
+    kb_status st = grow(f, f->rn);
+    if (st) return st;
+    set_rep_params(&f->rep, p);
+    if ((st = upload_rep(f))) return st;
+    KB_CUDA(launch_set_u64(f->dstep.p, step, f->stream));
+    if ((st = enqueue_force(f, p))) return st;
+    f->wn = f->rn;
+    f->w_from_compute = true;
+    f->w_has_dead = false;
+    return KB_OK;
+}
+
+// Enqueue nsteps steps (force + rebuild) directly on the stream.
+static kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps, bool fast) {
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        kb_status st = enqueue_force(f, p);
+        if (st) return st;
+        f->wn = f->rn;
+        st = fast ? fast_rebuild(f, true) : general_rebuild(f, true);
+        if (st) return st;
+        if (!fast) KB_CUDA(launch_add_u64(f->dstep.p, 1ull, f->stream));
+        f->wn = 0;
+    }
+    return KB_OK;
+}
+
+kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                        uint32_t nsteps) {
+    if (!f || !p) return fail(KB_ERR_ARG, "null argument");
+    std::string why;
+    if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
+    if (f->wn || !f->p_id.empty())
+        return fail(KB_ERR_STATE, "write buffer not empty: call lazy_update first");
+    if (nsteps == 0) return KB_OK;
+    DeviceGuard g(f->device);
+    kb_status st = grow(f, f->rn);
+    if (st) return st;
+    set_rep_params(&f->rep, p);
+    if ((st = upload_rep(f))) return st;
+    KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
+    const bool fast = fast_rebin_ok(f->rep) && f->layout_is_positions;
+    uint32_t done = 0;
+    if (!f->layout_is_positions) {
+        // the first step after arbitrary set_object_location calls re-sorts generally
+        if ((st = enqueue_steps(f, p, 1, false))) return st;
+        f->layout_is_positions = true;
+        done = 1;
+    }
+    const bool use_fast = fast_rebin_ok(f->rep);
+    // CUDA-graph replay of chunks of up to 100 steps (one graph per chunk
+    // length and start parity; the graph reads the step number from device
+    // memory, so one capture serves every step range).
+    const uint32_t CHUNK = 100;
+    while (done < nsteps) {
+        const uint32_t k = std::min(CHUNK, nsteps - done);
+        if (k < 4) {
+            if ((st = enqueue_steps(f, p, k, use_fast))) return st;
+            done += k;
+            continue;
+        }
+        kb_field::GraphKey key;
+        key.steps = k;
+        key.parity = f->cur;
+        key.params.assign((const uint8_t*)&f->rep, (const uint8_t*)&f->rep + sizeof(Rep));
+        key.params.push_back((uint8_t)p->arith);
+        key.params.push_back((uint8_t)(f->rn & 0xff));
+        key.params.push_back((uint8_t)((f->rn >> 8) & 0xff));
+        key.params.push_back((uint8_t)((f->rn >> 16) & 0xff));
+        key.params.push_back((uint8_t)((f->rn >> 24) & 0xff));
+        auto it = f->graphs.find(key);
+        const int cur0 = f->cur;
+        if (it == f->graphs.end()) {
+            cudaGraph_t graph = nullptr;
+            KB_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
+            st = enqueue_steps(f, p, k, use_fast);
+            cudaError_t ce = cudaStreamEndCapture(f->stream, &graph);
+            if (st) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (ce) return cuda_fail(ce, "cudaStreamEndCapture");
+            cudaGraphExec_t exec = nullptr;
+            ce = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce) return cuda_fail(ce, "cudaGraphInstantiate");
+            if (f->graphs.size() > 16) f->drop_graphs();
+            it = f->graphs.emplace(key, exec).first;
+            f->cur = cur0;  // capture recorded the swaps; replay performs them
+        }
+        KB_CUDA(cudaGraphLaunch(it->second, f->stream));
+        f->cur = (k & 1u) ? 1 - cur0 : cur0;
+        done += k;
+    }
+    return KB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,805 @@
+// kb_kernels.cu -- sm_103a kernels of the continuous-space agent step.
+//
+// Data layout in HBM (one field, or many replicas packed back to back):
+//   read buffer  st[n] float4 {x, y, last_dx, last_dy}, ids[n] u32, sorted by
+//                bag index (cell_off + x*dh + y, field_2d.rs:508), each bag in
+//                insertion order; start[ncells+1] u32 bag offsets.
+//   write list   the same records in arbitrary order plus a u32 bag key each
+//                (the write buffer of field_2d.rs:838-846).
+// A flock step is: force pass (read buffer -> write list, key histogram),
+// scan of the histogram, stencil-gather rebin (write list -> read buffer).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kb_common.h"
+#include "kb_launch.h"
+#include "kb_runtime.h"
+
+namespace kb {
+namespace {
+
+// ---------------------------------------------------------- f32 arithmetic
+// STRICT: every operation rounds once, as the reference's Rust f32 code does
+// (no fused multiply-add, IEEE division and square root).  FAST: the
+// compiler may fuse, and divisions use the approximate reciprocal.
+template <bool STRICT>
+struct F;
+template <>
+struct F<true> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+};
+template <>
+struct F<false> {
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
+};
+
+// field_2d.rs:1004-1014
+__device__ __forceinline__ float toroidal_transform(float v, float dim) {
+    if (v >= 0.0f && v < dim) return v;
+    float r = fmodf(v, dim);
+    if (r < 0.0f) r = __fadd_rn(r, dim);
+    return r;
+}
+
+// field_2d.rs:988-1002
+__device__ __forceinline__ float toroidal_distance(float a, float b, float dim) {
+    float d0 = __fsub_rn(a, b);
+    if (fabsf(d0) <= __fdiv_rn(dim, 2.0f)) return d0;
+    float d = __fsub_rn(toroidal_transform(a, dim), toroidal_transform(b, dim));
+    float d2 = __fmul_rn(d, 2.0f);
+    if (d2 > dim) return __fsub_rn(d, dim);
+    if (d2 < -dim) return __fadd_rn(d, dim);
+    return d;
+}
+
+// field_2d.rs:974-986
+__device__ __forceinline__ float distance(float x1, float y1, float x2, float y2, float w, float h,
+                                          bool tor) {
+    float dx, dy;
+    if (tor) {
+        dx = toroidal_distance(x1, x2, w);
+        dy = toroidal_distance(y1, y2, h);
+    } else {
+        dx = __fsub_rn(x1, x2);
+        dy = __fsub_rn(y1, y2);
+    }
+    return __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+}
+
+// field_2d.rs:934-972: 1 = whole bag inside, -1 = bag skipped, 0 = filter.
+__device__ __forceinline__ int check_circle(int bx, int by, const Rep& R, float lx, float ly,
+                                            float dis) {
+    float nw_x = __fmul_rn((float)bx, R.d), nw_y = __fmul_rn((float)by, R.d);
+    float ne_y = fminf(__fadd_rn(nw_y, R.d), R.h);
+    float sw_x = fminf(__fadd_rn(nw_x, R.d), R.w);
+    bool tor = R.toroidal != 0;
+    float a = distance(nw_x, nw_y, lx, ly, R.w, R.h, tor);
+    float b = distance(nw_x, ne_y, lx, ly, R.w, R.h, tor);
+    float c = distance(sw_x, nw_y, lx, ly, R.w, R.h, tor);
+    float e = distance(sw_x, ne_y, lx, ly, R.w, R.h, tor);
+    if (a <= dis && b <= dis && c <= dis && e <= dis) return 1;
+    if (a > dis && b > dis && c > dis && e > dis) return -1;
+    return 0;
+}
+
+// discretize (field_2d.rs:328-339), always IEEE (bag choice is index work).
+__device__ __forceinline__ int32_t disc(float v, float d) { return as_i32(floorf(__fdiv_rn(v, d))); }
+
+// The query's cell range (field_2d.rs:398-418 / 484-500).  False: dist <= 0.
+__device__ __forceinline__ bool cell_range(const Rep& R, float x, float y, int32_t dd, int* mi,
+                                           int* Mi, int* mj, int* Mj) {
+    if (dd < 0) return false;
+    int cx = disc(x, R.d), cy = disc(y, R.d);
+    int a = cx - dd, b = cx + dd, c = cy - dd, e = cy + dd;
+    if (R.toroidal) {
+        a = max(0, a);
+        b = min(b, R.max_x - 1);
+        c = max(0, c);
+        e = min(e, R.max_y - 1);
+    }
+    *mi = a; *Mi = b; *mj = c; *Mj = e;
+    return true;
+}
+
+// Reference bag index ((x*dh)+y) with i32 wrapping; -1 outside the matrix.
+__device__ __forceinline__ int64_t bag_index(const Rep& R, int32_t cx, int32_t cy) {
+    int32_t idx = (int32_t)((uint32_t)cx * (uint32_t)R.dh + (uint32_t)cy);
+    if (idx < 0 || (uint32_t)idx >= R.ncells) return -1;
+    return idx;
+}
+
+__device__ __forceinline__ uint32_t id_mix(uint32_t id) {
+    uint32_t z = id * 0x9E3779B1u;
+    z ^= z >> 15;
+    z *= 0x85EBCA77u;
+    z ^= z >> 13;
+    return z;
+}
+
+// Replica owning boid slot i / cell c (tables sorted by offset).
+__device__ __forceinline__ int rep_of_boid(const Rep* reps, int nrep, uint32_t i) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&reps[mid].boid_off) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int rep_of_cell(const Rep* reps, int nrep, uint32_t c) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&reps[mid].cell_off) <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------- force pass
+// One thread per boid of the read buffer: Bird::step (bird.rs:39-154)
+// against the read buffer, next state into the write list at the same slot.
+template <bool STRICT>
+struct Acc {
+    float xa = 0.f, ya = 0.f, xc = 0.f, yc = 0.f, xs = 0.f, ys = 0.f;
+    int count = 0;
+    uint32_t vec = 0;  // candidates including self (the reference's vec.len())
+
+    __device__ __forceinline__ void add(const Rep& R, float sx, float sy, float4 o) {
+        using M = F<STRICT>;
+        float dx = toroidal_distance(sx, o.x, R.w);
+        float dy = toroidal_distance(sy, o.y, R.h);
+        count += 1;
+        float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
+        float q = M::add(M::mul(sq, sq), 1.0f);
+        if (STRICT) {
+            xa = M::add(xa, M::div(dx, q));
+            ya = M::add(ya, M::div(dy, q));
+        } else {
+            float inv = __fdividef(1.0f, q);
+            xa = xa + dx * inv;
+            ya = ya + dy * inv;
+        }
+        xc = M::add(xc, dx);
+        yc = M::add(yc, dy);
+        xs = M::add(xs, o.z);
+        ys = M::add(ys, o.w);
+    }
+};
+
+template <bool STRICT, int QMODE, bool MULTI>
+__global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
+    using M = F<STRICT>;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int r = MULTI ? rep_of_boid(a.reps, a.nrep, i) : 0;
+    const Rep R = a.reps[r];
+    const unsigned long long step = *a.step;
+    const float4 me = a.st[i];
+    const uint32_t my_id = a.ids[i];
+
+    Acc<STRICT> acc;
+    int mi, Mi, mj, Mj;
+    if (cell_range(R, me.x, me.y, R.dd, &mi, &Mi, &mj, &Mj)) {
+        for (int ci = mi; ci <= Mi; ++ci) {
+            const int bx = t_transform(ci, R.max_x);
+            const uint32_t colbase = R.cell_off + (uint32_t)bx * (uint32_t)R.dh;
+            if (QMODE == 0 && R.toroidal) {
+                // clamped range: the column's bags mj..Mj are one contiguous run
+                if (mj > Mj) continue;
+                const uint32_t s = a.start[colbase + mj], e = a.start[colbase + Mj + 1];
+                for (uint32_t k = s; k < e; ++k) {
+                    acc.vec += 1;
+                    if (a.ids[k] != my_id) acc.add(R, me.x, me.y, a.st[k]);
+                }
+            } else {
+                for (int cj = mj; cj <= Mj; ++cj) {
+                    const int by = t_transform(cj, R.max_y);
+                    const uint32_t c = colbase + (uint32_t)by;
+                    const uint32_t s = a.start[c], e = a.start[c + 1];
+                    if (s == e) continue;
+                    int check = 1;
+                    if (QMODE == 1) {
+                        check = check_circle(bx, by, R, me.x, me.y, R.radius);
+                        if (check == -1) continue;
+                    }
+                    for (uint32_t k = s; k < e; ++k) {
+                        const float4 o = a.st[k];
+                        if (QMODE == 1 && check == 0 &&
+                            !(distance(me.x, me.y, o.x, o.y, R.w, R.h, R.toroidal != 0) <=
+                              R.radius))
+                            continue;
+                        acc.vec += 1;
+                        if (a.ids[k] != my_id) acc.add(R, me.x, me.y, o);
+                    }
+                }
+            }
+        }
+    }
+
+    float avx = 0.f, avy = 0.f, cox = 0.f, coy = 0.f, rax = 0.f, ray = 0.f, csx = 0.f, csy = 0.f;
+    if (acc.vec > 0) {
+        float xa = acc.xa, ya = acc.ya, xc = acc.xc, yc = acc.yc, xs = acc.xs, ys = acc.ys;
+        if (acc.count > 0) {
+            const float c = (float)acc.count;
+            xa = M::div(xa, c); ya = M::div(ya, c);
+            xc = M::div(xc, c); yc = M::div(yc, c);
+            xs = M::div(xs, c); ys = M::div(ys, c);
+            csx = M::div(xs, c);  // bird.rs:91-94: a second division by count
+            csy = M::div(ys, c);
+        } else {
+            csx = xs;
+            csy = ys;
+        }
+        avx = M::mul(400.0f, xa);
+        avy = M::mul(400.0f, ya);
+        cox = M::div(-xc, 10.0f);
+        coy = M::div(-yc, 10.0f);
+        const U4 o = philox4x32_10(U4{my_id, (uint32_t)step, (uint32_t)(step >> 32), STREAM_JITTER},
+                                   R.seed_lo, R.seed_hi);
+        const float xr = M::sub(M::mul(unit_f32(o.x), 2.0f), 1.0f);
+        const float yr = M::sub(M::mul(unit_f32(o.y), 2.0f), 1.0f);
+        const float sq = M::sqrt(M::add(M::mul(xr, xr), M::mul(yr, yr)));
+        rax = M::div(M::mul(0.05f, xr), sq);
+        ray = M::div(M::mul(0.05f, yr), sq);
+    }
+    float dx = M::add(M::add(M::add(M::add(M::mul(R.coh, cox), M::mul(R.avo, avx)),
+                                    M::mul(R.con, csx)),
+                             M::mul(R.rnd, rax)),
+                      M::mul(R.mom, me.z));
+    float dy = M::add(M::add(M::add(M::add(M::mul(R.coh, coy), M::mul(R.avo, avy)),
+                                    M::mul(R.con, csy)),
+                             M::mul(R.rnd, ray)),
+                      M::mul(R.mom, me.w));
+    const float dis = M::sqrt(M::add(M::mul(dx, dx), M::mul(dy, dy)));
+    if (dis > 0.0f) {
+        dx = M::mul(M::div(dx, dis), R.jump);
+        dy = M::mul(M::div(dy, dis), R.jump);
+    }
+    const float nx = toroidal_transform(__fadd_rn(me.x, dx), R.w);
+    const float ny = toroidal_transform(__fadd_rn(me.y, dy), R.w);  // bird.rs:147: y wraps with w
+
+    a.out_st[i] = make_float4(nx, ny, dx, dy);
+    a.out_ids[i] = my_id;
+    const int32_t ncx = disc(nx, R.d), ncy = disc(ny, R.d);
+    int64_t idx = bag_index(R, ncx, ncy);
+    uint32_t flags = 0;
+    if (idx < 0) {
+        flags |= ERR_KEY_RANGE;
+        idx = 0;
+    }
+    if (!isfinite(nx) || !isfinite(ny)) flags |= ERR_NONFINITE;
+    // the rebin gathers a bag's arrivals from the 3x3 old bags around it
+    // (plus the seam columns/rows); anything else must take the general sort
+    const int32_t ocx = disc(me.x, R.d), ocy = disc(me.y, R.d);
+    const bool okx = abs(ncx - ocx) <= 1 || (ncx <= 1 && ocx >= R.max_x - 1) ||
+                     (ncx >= R.max_x - 1 && ocx <= 1);
+    const bool oky = abs(ncy - ocy) <= 1 || (ncy <= 1 && ocy >= R.max_y - 1) ||
+                     (ncy >= R.max_y - 1 && ocy <= 1);
+    if (!(okx && oky)) flags |= ERR_REBIN_MISS;
+    if (flags) atomicOr(a.err, flags);
+    const uint32_t key = R.cell_off + (uint32_t)idx;
+    a.out_key[i] = key;
+    atomicAdd(&a.hist[key], 1u);
+}
+
+// ---------------------------------------------------------- scan
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr unsigned long long FLAG_AGG = 1ull, FLAG_INC = 2ull;
+constexpr uint32_t SPIN_LIMIT = 1u << 20;
+
+__device__ __forceinline__ unsigned long long pack_tile(uint32_t epoch, unsigned long long flag,
+                                                        uint32_t v) {
+    return ((unsigned long long)(epoch & 0x3FFFFFFFu) << 34) | (flag << 32) | v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n, ScanCtl* ctl,
+           unsigned long long* tstate, uint32_t* err, int zero_in, uint32_t ntiles) {
+    __shared__ uint32_t s_tile, s_epoch, s_prefix;
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        s_tile = atomicAdd(&ctl->tile_counter, 1u);
+        s_epoch = *((volatile uint32_t*)&ctl->epoch);
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile, epoch = s_epoch;
+    const uint64_t base = (uint64_t)tile * SCAN_TILE + (uint64_t)tid * SCAN_ITEMS;
+
+    uint32_t v[SCAN_ITEMS];
+    if (base + SCAN_ITEMS <= n) {
+        const uint4* p = reinterpret_cast<const uint4*>(in + base);
+        uint4 a = p[0], b = p[1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        if (zero_in) {
+            uint4* q = reinterpret_cast<uint4*>(const_cast<uint32_t*>(in + base));
+            q[0] = make_uint4(0, 0, 0, 0);
+            q[1] = make_uint4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            v[k] = (base + k < n) ? in[base + k] : 0u;
+            if (zero_in && base + k < n) const_cast<uint32_t*>(in)[base + k] = 0u;
+        }
+    }
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) tsum += v[k];
+    // block exclusive scan of the per-thread sums
+    uint32_t x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = (lane < SCAN_THREADS / 32) ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) s_warp[lane] = w;  // inclusive warp prefixes
+    }
+    __syncthreads();
+    const uint32_t agg = s_warp[SCAN_THREADS / 32 - 1];
+    const uint32_t texcl = x - tsum + (warp > 0 ? s_warp[warp - 1] : 0u);
+
+    // decoupled look-back across tiles
+    if (warp == 0) {
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) {
+                atomicExch(&tstate[0], pack_tile(epoch, FLAG_INC, agg));
+            }
+        } else {
+            if (lane == 0) atomicExch(&tstate[tile], pack_tile(epoch, FLAG_AGG, agg));
+            int64_t pred = (int64_t)tile - 1;
+            bool done = false;
+            while (!done) {
+                const int64_t j = pred - lane;
+                unsigned long long word = pack_tile(epoch, FLAG_INC, 0u);  // lanes past tile 0
+                if (j >= 0) {
+                    uint32_t spins = 0;
+                    while (true) {
+                        word = *((volatile unsigned long long*)&tstate[j]);
+                        const bool ready = (uint32_t)(word >> 34) == (epoch & 0x3FFFFFFFu) &&
+                                           ((word >> 32) & 3ull) != 0ull;
+                        if (ready) break;
+                        if (++spins > SPIN_LIMIT) {
+                            atomicOr(err, ERR_SPIN_TIMEOUT);
+                            word = pack_tile(epoch, FLAG_INC, 0u);
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                }
+                const bool inc = ((word >> 32) & 3ull) == FLAG_INC;
+                const uint32_t incmask = __ballot_sync(0xffffffffu, inc);
+                uint32_t val = (uint32_t)word;
+                int stop = incmask ? (__ffs(incmask) - 1) : 32;  // nearest inclusive predecessor
+                if (lane > stop) val = 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                prefix += val;
+                if (incmask) done = true;
+                else pred -= 32;
+            }
+            if (lane == 0) atomicExch(&tstate[tile], pack_tile(epoch, FLAG_INC, prefix + agg));
+        }
+        if (lane == 0) s_prefix = prefix;
+    }
+    __syncthreads();
+    const uint32_t prefix = s_prefix;
+    uint32_t run = prefix + texcl;
+    if (base + SCAN_ITEMS <= n) {
+        uint32_t o[SCAN_ITEMS];
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            o[k] = run;
+            run += v[k];
+        }
+        uint4* p = reinterpret_cast<uint4*>(out + base);
+        p[0] = make_uint4(o[0], o[1], o[2], o[3]);
+        p[1] = make_uint4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            if (base + k < n) out[base + k] = run;
+            run += v[k];
+        }
+    }
+    if (tile == ntiles - 1 && tid == 0) out[n] = prefix + agg;
+    // the last CTA to finish re-arms the control block for the next launch
+    if (tid == 0) {
+        __threadfence();
+        const uint32_t d = atomicAdd(&ctl->done_counter, 1u);
+        if (d == ntiles - 1) {
+            ctl->tile_counter = 0u;
+            ctl->done_counter = 0u;
+            __threadfence();
+            atomicAdd(&ctl->epoch, 1u);
+        }
+    }
+}
+
+// ---------------------------------------------------------- rebin
+// Source lines of the bags that can receive boids landing in line X: X-1..X+1
+// and, across the seam, the first two / last two lines.  Ascending, unique.
+__device__ __forceinline__ int source_lines(int X, int maxv, int* out) {
+    int tmp[7];
+    int n = 0;
+    if (X >= maxv - 1) { tmp[n++] = 0; tmp[n++] = 1; }
+    if (X - 1 >= 0) tmp[n++] = X - 1;
+    tmp[n++] = X;
+    if (X + 1 <= maxv) tmp[n++] = X + 1;
+    if (X <= 1) { tmp[n++] = maxv - 1; tmp[n++] = maxv; }
+    // insertion sort + unique, clipped to [0, maxv]
+    for (int a = 1; a < n; ++a) {
+        int v = tmp[a], b = a - 1;
+        while (b >= 0 && tmp[b] > v) { tmp[b + 1] = tmp[b]; --b; }
+        tmp[b + 1] = v;
+    }
+    int m = 0;
+    for (int a = 0; a < n; ++a) {
+        int v = tmp[a];
+        if (v < 0 || v > maxv) continue;
+        if (m > 0 && out[m - 1] == v) continue;
+        out[m++] = v;
+    }
+    return m;
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c == 0 && a.step != nullptr) *a.step += 1ull;
+    if (c >= a.ncells) return;
+    uint32_t dst = a.start_next[c];
+    const uint32_t end = a.start_next[c + 1];
+    if (dst == end) return;
+    const int r = MULTI ? rep_of_cell(a.reps, a.nrep, c) : 0;
+    const Rep R = a.reps[r];
+    const uint32_t local = c - R.cell_off;
+    const int X = (int)(local / (uint32_t)R.dh), Y = (int)(local % (uint32_t)R.dh);
+    int cols[7], rows[7];
+    const int nc = source_lines(X, R.max_x, cols);
+    const int nr = source_lines(Y, R.max_y, rows);
+    for (int ia = 0; ia < nc; ++ia) {
+        const uint32_t colbase = R.cell_off + (uint32_t)cols[ia] * (uint32_t)R.dh;
+        int ib = 0;
+        while (ib < nr) {
+            int jb = ib;  // merge consecutive rows into one contiguous run
+            while (jb + 1 < nr && rows[jb + 1] == rows[jb] + 1) ++jb;
+            const uint32_t s = a.start_cur[colbase + rows[ib]];
+            const uint32_t e = a.start_cur[colbase + rows[jb] + 1];
+            for (uint32_t p = s; p < e; ++p) {
+                if (a.key[p] == c) {
+                    if (dst < end) {
+                        a.s_st[dst] = a.a_st[p];
+                        a.s_ids[dst] = a.a_ids[p];
+                    }
+                    ++dst;
+                }
+            }
+            ib = jb + 1;
+        }
+    }
+    if (dst != end) atomicOr(a.err, ERR_REBIN_MISS);
+}
+
+// ---------------------------------------------------------- general sort
+__global__ void k_hist_list(const uint32_t* __restrict__ key, const uint8_t* __restrict__ dead,
+                            uint32_t n, uint32_t* __restrict__ hist) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (dead && dead[i])) return;
+    atomicAdd(&hist[key[i]], 1u);
+}
+
+__global__ void k_scatter_list(const uint32_t* __restrict__ key, const uint8_t* __restrict__ dead,
+                               const float4* __restrict__ st, const uint32_t* __restrict__ ids,
+                               uint32_t n, const uint32_t* __restrict__ start,
+                               uint32_t* __restrict__ cursor, float4* __restrict__ t_st,
+                               uint32_t* __restrict__ t_ids, uint32_t* __restrict__ t_src) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (dead && dead[i])) return;
+    const uint32_t k = key[i];
+    const uint32_t slot = start[k] + atomicAdd(&cursor[k], 1u);
+    t_st[slot] = st[i];
+    t_ids[slot] = ids[i];
+    t_src[slot] = i;
+}
+
+// One thread per bag: order the bag's members by their write-list index
+// (the reference's insertion order), then reset the bag's cursor.
+__global__ void k_canon(const uint32_t* __restrict__ start, uint32_t ncells,
+                        const float4* __restrict__ t_st, const uint32_t* __restrict__ t_ids,
+                        const uint32_t* __restrict__ t_src, uint32_t* __restrict__ cursor,
+                        float4* __restrict__ s_st, uint32_t* __restrict__ s_ids) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const uint32_t s = start[c], e = start[c + 1];
+    if (s == e) return;
+    cursor[c] = 0u;
+    for (uint32_t m = s; m < e; ++m) {
+        const uint32_t src = t_src[m];
+        uint32_t rank = 0;
+        for (uint32_t m2 = s; m2 < e; ++m2) rank += (t_src[m2] < src) ? 1u : 0u;
+        s_st[s + rank] = t_st[m];
+        s_ids[s + rank] = t_ids[m];
+    }
+}
+
+// ---------------------------------------------------------- queries
+template <int KIND>
+__global__ void k_query(QueryArgs a) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.nq) return;
+    const Rep& R = a.rep;
+    const float2 p = a.q[q];
+    const bool fill = a.offsets != nullptr;
+    const uint64_t off = fill ? a.offsets[q] : 0;
+    uint32_t cnt = 0, dig = 0;
+    int mi, Mi, mj, Mj;
+    const int32_t dd = (a.dist <= 0.0f) ? -1 : disc(a.dist, R.d);
+    if (cell_range(R, p.x, p.y, dd, &mi, &Mi, &mj, &Mj)) {
+        for (int ci = mi; ci <= Mi; ++ci) {
+            const int bx = t_transform(ci, R.max_x);
+            for (int cj = mj; cj <= Mj; ++cj) {
+                const int by = t_transform(cj, R.max_y);
+                const uint32_t c = R.cell_off + (uint32_t)bx * (uint32_t)R.dh + (uint32_t)by;
+                const uint32_t s = a.start[c], e = a.start[c + 1];
+                if (s == e) continue;
+                int check = 1;
+                if (KIND == 1) {
+                    check = check_circle(bx, by, R, p.x, p.y, a.dist);
+                    if (check == -1) continue;
+                }
+                for (uint32_t k = s; k < e; ++k) {
+                    if (KIND == 1 && check == 0) {
+                        const float4 o = a.st[k];
+                        if (!(distance(p.x, p.y, o.x, o.y, R.w, R.h, R.toroidal != 0) <= a.dist))
+                            continue;
+                    }
+                    const uint32_t id = a.ids[k];
+                    if (fill && off + cnt < a.cap) {
+                        a.out_ids[off + cnt] = id;
+                        if (a.out_st) a.out_st[off + cnt] = a.st[k];
+                    }
+                    dig += id_mix(id);
+                    ++cnt;
+                }
+            }
+        }
+    }
+    if (!fill) {
+        a.counts[q] = cnt;
+        if (a.digest) a.digest[q] = dig;
+    }
+}
+
+// ---------------------------------------------------------- ordered filters
+// One block walks the list in chunks, keeping list order (write-buffer
+// lookups are API calls, not the per-step path).
+constexpr int FILTER_THREADS = 1024;
+
+template <typename Pred, typename Emit>
+__device__ void ordered_filter(uint32_t n, Pred pred, Emit emit, uint32_t* out_count) {
+    __shared__ uint32_t s_warp[FILTER_THREADS / 32];
+    __shared__ uint32_t s_base;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_base = 0;
+    __syncthreads();
+    for (uint32_t c0 = 0; c0 < n; c0 += FILTER_THREADS) {
+        const uint32_t i = c0 + tid;
+        const bool f = i < n && pred(i);
+        const uint32_t bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int w = 0; w < FILTER_THREADS / 32; ++w) {
+            const uint32_t cw = s_warp[w];
+            if (w < warp) before += cw;
+            total += cw;
+        }
+        const uint32_t pos = s_base + before + __popc(bal & ((1u << lane) - 1u));
+        if (f) emit(i, pos);
+        __syncthreads();
+        if (tid == 0) s_base += total;
+        __syncthreads();
+    }
+    if (tid == 0) *out_count = s_base;
+}
+
+__global__ void __launch_bounds__(FILTER_THREADS)
+    k_filter_key(const uint32_t* key, const uint8_t* dead, const float4* st, const uint32_t* ids,
+                 uint32_t n, uint32_t target, uint32_t* out_ids, float4* out_st, uint64_t cap,
+                 uint32_t* out_count) {
+    ordered_filter(
+        n, [&](uint32_t i) { return key[i] == target && !(dead && dead[i]); },
+        [&](uint32_t i, uint32_t pos) {
+            if (pos < cap) {
+                if (out_ids) out_ids[pos] = ids[i];
+                if (out_st) out_st[pos] = st[i];
+            }
+        },
+        out_count);
+}
+
+__global__ void __launch_bounds__(FILTER_THREADS)
+    k_empty_bags(Rep R, const uint32_t* start, float2* out, uint64_t cap, uint32_t* out_count) {
+    ordered_filter(
+        R.ncells, [&](uint32_t c) { return start[c + 1] == start[c]; },
+        [&](uint32_t c, uint32_t pos) {
+            if (pos < cap) {
+                const uint32_t i = c / (uint32_t)R.dh, j = c % (uint32_t)R.dh;
+                out[pos] = make_float2(__fmul_rn((float)i, R.d), __fmul_rn((float)j, R.d));
+            }
+        },
+        out_count);
+}
+
+__global__ void k_remove(const uint32_t* key, uint8_t* dead, const uint32_t* ids, uint32_t n,
+                         uint32_t target, uint32_t id, uint32_t* removed) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (key[i] == target && ids[i] == id && !dead[i]) {
+        dead[i] = 1;
+        atomicAdd(removed, 1u);
+    }
+}
+
+__global__ void k_cell_of(const uint32_t* start, uint32_t ncells, uint32_t* cell_of) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    for (uint32_t k = start[c]; k < start[c + 1]; ++k) cell_of[k] = c;
+}
+
+__global__ void k_cell_xy(Rep R, const uint32_t* cell_of, uint32_t n, float2* out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t c = cell_of[k] - R.cell_off;
+    const uint32_t i = c / (uint32_t)R.dh, j = c % (uint32_t)R.dh;
+    out[k] = make_float2(__fmul_rn((float)i, R.d), __fmul_rn((float)j, R.d));
+}
+
+__global__ void k_set_rep(Rep* dst, Rep v) { *dst = v; }
+__global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
+__global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst += v; }
+
+inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+cudaError_t launch_set_rep(Rep* dst, const Rep& v, cudaStream_t s) {
+    k_set_rep<<<1, 1, 0, s>>>(dst, v);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_u64(unsigned long long* dst, unsigned long long v, cudaStream_t s) {
+    k_set_u64<<<1, 1, 0, s>>>(dst, v);
+    return cudaGetLastError();
+}
+cudaError_t launch_add_u64(unsigned long long* dst, unsigned long long v, cudaStream_t s) {
+    k_add_u64<<<1, 1, 0, s>>>(dst, v);
+    return cudaGetLastError();
+}
+
+// ====================================================================== launchers
+cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* ctl,
+                        unsigned long long* tile_state, uint32_t* err, bool zero_in,
+                        cudaStream_t s) {
+    const uint32_t nt = scan_tiles(n);
+    if (nt == 0) {
+        return cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
+    }
+    k_scan<<<nt, SCAN_THREADS, 0, s>>>(in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s) {
+    if (a.n == 0) return cudaSuccess;
+    const unsigned g = grid_for(a.n, 256);
+    const bool multi = a.nrep > 1;
+#define KB_FORCE(S, Q, MU) k_flock_force<S, Q, MU><<<g, 256, 0, s>>>(a)
+    if (strict) {
+        if (qmode == 0) { if (multi) KB_FORCE(true, 0, true); else KB_FORCE(true, 0, false); }
+        else { if (multi) KB_FORCE(true, 1, true); else KB_FORCE(true, 1, false); }
+    } else {
+        if (qmode == 0) { if (multi) KB_FORCE(false, 0, true); else KB_FORCE(false, 0, false); }
+        else { if (multi) KB_FORCE(false, 1, true); else KB_FORCE(false, 1, false); }
+    }
+#undef KB_FORCE
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s) {
+    const unsigned g = grid_for(a.ncells > 0 ? a.ncells : 1, 256);
+    if (a.nrep > 1) k_rebin<true><<<g, 256, 0, s>>>(a);
+    else k_rebin<false><<<g, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hist_list(const uint32_t* key, const uint8_t* dead, uint32_t n, uint32_t* hist,
+                             cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_hist_list<<<grid_for(n, 256), 256, 0, s>>>(key, dead, n, hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_list(const uint32_t* key, const uint8_t* dead, const float4* st,
+                                const uint32_t* ids, uint32_t n, const uint32_t* start,
+                                uint32_t* cursor, float4* t_st, uint32_t* t_ids, uint32_t* t_src,
+                                cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_scatter_list<<<grid_for(n, 256), 256, 0, s>>>(key, dead, st, ids, n, start, cursor, t_st,
+                                                     t_ids, t_src);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_canon(const uint32_t* start, uint32_t ncells, const float4* t_st,
+                         const uint32_t* t_ids, const uint32_t* t_src, uint32_t* cursor,
+                         float4* s_st, uint32_t* s_ids, cudaStream_t s) {
+    if (ncells == 0) return cudaSuccess;
+    k_canon<<<grid_for(ncells, 256), 256, 0, s>>>(start, ncells, t_st, t_ids, t_src, cursor, s_st,
+                                                  s_ids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_query(const QueryArgs& a, cudaStream_t s) {
+    if (a.nq == 0) return cudaSuccess;
+    const unsigned g = grid_for(a.nq, 128);
+    if (a.kind == 1) k_query<1><<<g, 128, 0, s>>>(a);
+    else k_query<0><<<g, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_filter_key(const uint32_t* key, const uint8_t* dead, const float4* st,
+                              const uint32_t* ids, uint32_t n, uint32_t target, uint32_t* out_ids,
+                              float4* out_st, uint64_t cap, uint32_t* out_count, cudaStream_t s) {
+    k_filter_key<<<1, FILTER_THREADS, 0, s>>>(key, dead, st, ids, n, target, out_ids, out_st, cap,
+                                              out_count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_remove(const uint32_t* key, uint8_t* dead, const uint32_t* ids, uint32_t n,
+                          uint32_t target, uint32_t id, uint32_t* removed, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_remove<<<grid_for(n, 256), 256, 0, s>>>(key, dead, ids, n, target, id, removed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_empty_bags(const Rep& rep, const uint32_t* start, float2* out, uint64_t cap,
+                              uint32_t* out_count, cudaStream_t s) {
+    k_empty_bags<<<1, FILTER_THREADS, 0, s>>>(rep, start, out, cap, out_count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_of(const uint32_t* start, uint32_t ncells, uint32_t* cell_of,
+                           cudaStream_t s) {
+    if (ncells == 0) return cudaSuccess;
+    k_cell_of<<<grid_for(ncells, 256), 256, 0, s>>>(start, ncells, cell_of);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_xy(const Rep& rep, const uint32_t* cell_of, uint32_t n, float2* out,
+                           cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_cell_xy<<<grid_for(n, 256), 256, 0, s>>>(rep, cell_of, n, out);
+    return cudaGetLastError();
+}
+
+}  // namespace kb

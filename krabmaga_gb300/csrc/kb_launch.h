@@ -1,0 +1,120 @@
+// kb_launch.h -- host-side launchers of the kernels in kb_kernels.cu.  Every
+// launcher enqueues on the given stream and returns the launch error.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kb_common.h"
+
+namespace kb {
+
+// Scan workspace: a tile counter, a finish counter and an epoch that tags
+// the per-tile look-back words, so the scan needs no reset between launches
+// (and replays correctly inside a CUDA graph).
+struct ScanCtl {
+    uint32_t tile_counter;
+    uint32_t done_counter;
+    uint32_t epoch;
+    uint32_t _pad;
+};
+constexpr uint32_t SCAN_TILE = 2048;  // items per CTA (256 threads x 8)
+inline uint32_t scan_tiles(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+// Exclusive scan of in[0..n) into out[0..n]; out[n] = total.  When zero_in,
+// in[] is cleared as it is read (the histogram is ready for the next step).
+cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* ctl,
+                        unsigned long long* tile_state, uint32_t* err, bool zero_in,
+                        cudaStream_t s);
+
+// Flock step agent pass: reads the canonical read buffer (st, ids, start),
+// writes next states into the write list in the same order plus each one's
+// new bag key, and counts keys into hist.
+struct ForceArgs {
+    const Rep* reps;
+    int32_t nrep;
+    const float4* st;
+    const uint32_t* ids;
+    const uint32_t* start;
+    uint32_t n;
+    const unsigned long long* step;
+    float4* out_st;
+    uint32_t* out_ids;
+    uint32_t* out_key;
+    uint32_t* hist;
+    uint32_t* err;
+};
+cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
+
+// Stencil-gather rebin: builds the canonical read buffer of the next step
+// from the write list (in the previous canonical order) and the scanned
+// histogram.  Bumps *step when step != nullptr.
+struct RebinArgs {
+    const Rep* reps;
+    int32_t nrep;
+    const uint32_t* start_cur;
+    const uint32_t* start_next;
+    const uint32_t* key;
+    const float4* a_st;
+    const uint32_t* a_ids;
+    uint32_t ncells;
+    float4* s_st;
+    uint32_t* s_ids;
+    unsigned long long* step;
+    uint32_t* err;
+};
+cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s);
+
+// General stable counting sort of the write list by key (insertion order
+// kept inside each bag): histogram, scatter, per-bag canonicalisation.
+cudaError_t launch_hist_list(const uint32_t* key, const uint8_t* dead, uint32_t n, uint32_t* hist,
+                             cudaStream_t s);
+cudaError_t launch_scatter_list(const uint32_t* key, const uint8_t* dead, const float4* st,
+                                const uint32_t* ids, uint32_t n, const uint32_t* start,
+                                uint32_t* cursor, float4* t_st, uint32_t* t_ids, uint32_t* t_src,
+                                cudaStream_t s);
+cudaError_t launch_canon(const uint32_t* start, uint32_t ncells, const float4* t_st,
+                         const uint32_t* t_ids, const uint32_t* t_src, uint32_t* cursor,
+                         float4* s_st, uint32_t* s_ids, cudaStream_t s);
+
+// Field2D queries over the read buffer of a single replica.
+//   mode 0: counts only (+ digest when digest != nullptr)
+//   mode 1: fill ids/states at offsets[q]
+struct QueryArgs {
+    Rep rep;
+    int32_t kind;  // 0 relax, 1 exact
+    float dist;
+    const uint32_t* start;
+    const float4* st;
+    const uint32_t* ids;
+    uint32_t nq;
+    const float2* q;
+    uint32_t* counts;
+    uint32_t* digest;
+    const uint32_t* offsets;
+    uint32_t* out_ids;
+    float4* out_st;
+    uint64_t cap;
+};
+cudaError_t launch_query(const QueryArgs& a, cudaStream_t s);
+
+// Ordered filter of the write list: entries with key == target and not dead,
+// in list order; writes ids/states (up to cap) and the count.
+cudaError_t launch_filter_key(const uint32_t* key, const uint8_t* dead, const float4* st,
+                              const uint32_t* ids, uint32_t n, uint32_t target, uint32_t* out_ids,
+                              float4* out_st, uint64_t cap, uint32_t* out_count, cudaStream_t s);
+// Mark write-list entries (key == target, id == id, live) dead; adds the
+// number marked to *removed.
+cudaError_t launch_remove(const uint32_t* key, uint8_t* dead, const uint32_t* ids, uint32_t n,
+                          uint32_t target, uint32_t id, uint32_t* removed, cudaStream_t s);
+// Empty bags of the read buffer in index order, as (i*d, j*d).
+cudaError_t launch_empty_bags(const Rep& rep, const uint32_t* start, float2* out, uint64_t cap,
+                              uint32_t* out_count, cudaStream_t s);
+// Bag index of every stored object (read buffer), for iteration.
+cudaError_t launch_cell_of(const uint32_t* start, uint32_t ncells, uint32_t* cell_of,
+                           cudaStream_t s);
+// (i*d, j*d) of the bag of each object.
+cudaError_t launch_cell_xy(const Rep& rep, const uint32_t* cell_of, uint32_t n, float2* out,
+                           cudaStream_t s);
+
+}  // namespace kb

@@ -1,0 +1,57 @@
+// kb_runtime.h -- host-side helpers shared by the runtime translation units:
+// an owning device buffer and the small state-setting launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <string>
+#include <utility>
+
+#include "../../include/krabgpu.h"
+#include "kb_common.h"
+
+namespace kb {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    cudaError_t alloc(size_t count) {
+        release();
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return e;
+        }
+        n = count;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void swap(DevBuf& o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+    }
+};
+
+// Record a failure message for kb_last_error() and return the code.
+kb_status fail(kb_status code, const std::string& msg);
+kb_status cuda_fail(cudaError_t e, const char* what);
+
+// Stream-ordered writes of small device state (values travel as kernel
+// arguments, so no host staging buffer has to outlive the call).
+cudaError_t launch_set_rep(Rep* dst, const Rep& v, cudaStream_t s);
+cudaError_t launch_set_u64(unsigned long long* dst, unsigned long long v, cudaStream_t s);
+cudaError_t launch_add_u64(unsigned long long* dst, unsigned long long v, cudaStream_t s);
+
+}  // namespace kb

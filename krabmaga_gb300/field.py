@@ -1,0 +1,256 @@
+"""Field2D over the GPU C ABI, with the reference's method names.
+
+Mirrors ``engine::fields::field_2d::Field2D`` (src/engine/fields/field_2d.rs,
+sequential build, lines 267-1014) for objects of the Flockers ``Bird`` shape
+``{id, pos, last_d}`` (tests/model/flockers/bird.rs:20-25).  Reads of the read
+buffer, writes to the write buffer and the ``lazy_update`` swap keep the
+reference's double-buffer semantics; every query runs as a kernel on the
+field's device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Callable, List, Optional, Tuple
+
+import numpy as np
+
+from . import _lib as L
+
+
+@dataclass(frozen=True)
+class Real2D:
+    """src/engine/location.rs:17-22 (2 x f32)."""
+
+    x: float
+    y: float
+
+    def as_f32(self) -> np.ndarray:
+        return np.array([self.x, self.y], dtype=np.float32)
+
+
+@dataclass(frozen=True)
+class Bird:
+    """tests/model/flockers/bird.rs:20-25; equality and hashing by id only
+    (bird.rs:157-174)."""
+
+    id: int
+    pos: Real2D
+    last_d: Real2D = Real2D(0.0, 0.0)
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, Bird) and other.id == self.id
+
+    def __hash__(self) -> int:
+        return hash(self.id)
+
+
+def _birds(ids: np.ndarray, st: np.ndarray) -> List[Bird]:
+    return [
+        Bird(int(i), Real2D(float(s[0]), float(s[1])), Real2D(float(s[2]), float(s[3])))
+        for i, s in zip(ids, st)
+    ]
+
+
+class Field2D:
+    """Field2D::new(w, h, d, toroidal) -- field_2d.rs:304-322."""
+
+    def __init__(self, w: float, h: float, d: float, toroidal: bool, device: int = 0,
+                 capacity_hint: int = 0):
+        desc = L.FieldDesc(w, h, d, 1 if toroidal else 0, device, capacity_hint)
+        h_ = C.c_void_p()
+        L.call("kb_field_create", C.byref(desc), C.byref(h_))
+        self._h = h_
+        self.width = float(np.float32(w))
+        self.height = float(np.float32(h))
+        self.discretization = float(np.float32(d))
+        self.toroidal = bool(toroidal)
+        dims = (C.c_int32 * 4)()
+        L.call("kb_field_dims", self._h, dims)
+        self.dw, self.dh, self.max_x, self.max_y = (int(v) for v in dims)
+
+    # -- lifetime ------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            L.lib.kb_field_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def cuda_stream(self) -> int:
+        s = C.c_void_p()
+        L.call("kb_field_cuda_stream", self._h, C.byref(s))
+        return s.value or 0
+
+    # -- writes (write buffer) -----------------------------------------
+    def set_object_location(self, obj: Bird, loc: Real2D) -> None:
+        """field_2d.rs:838-846"""
+        pos = obj.pos.as_f32()
+        ld = obj.last_d.as_f32()
+        lc = loc.as_f32()
+        L.call("kb_field_set_object_location", self._h, C.c_uint32(obj.id), L.fptr(pos),
+               L.fptr(ld), L.fptr(lc))
+
+    def set_locations(self, ids: np.ndarray, xy: np.ndarray, dxy: np.ndarray) -> None:
+        """Bulk set_object_location, each object at its own position."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        xy = np.ascontiguousarray(xy, dtype=np.float32).reshape(-1, 2)
+        dxy = np.ascontiguousarray(dxy, dtype=np.float32).reshape(-1, 2)
+        assert len(ids) == len(xy) == len(dxy)
+        L.call("kb_field_set_locations", self._h, C.c_size_t(len(ids)), L.uptr(ids),
+               L.fptr(xy), L.fptr(dxy))
+
+    def remove_object_location(self, obj: Bird, loc: Real2D) -> None:
+        """field_2d.rs:885-898"""
+        L.call("kb_field_remove_object_location", self._h, C.c_uint32(obj.id),
+               L.fptr(loc.as_f32()))
+
+    def lazy_update(self) -> None:
+        """Field::lazy_update -- field_2d.rs:905-921"""
+        L.call("kb_field_lazy_update", self._h)
+
+    @property
+    def nagents(self) -> int:
+        """field_2d.rs:276 (counted until the first lazy_update)."""
+        n = C.c_size_t()
+        L.call("kb_field_num_agents", self._h, C.byref(n))
+        return n.value
+
+    def num_objects(self) -> int:
+        n = C.c_size_t()
+        L.call("kb_field_num_objects", self._h, C.byref(n))
+        return n.value
+
+    # -- reads ----------------------------------------------------------
+    def _query(self, fn: str, loc: Real2D, dist: float) -> List[Bird]:
+        lc = loc.as_f32()
+        n = C.c_size_t()
+        L.call(fn, self._h, L.fptr(lc), C.c_float(dist), None, None, C.c_size_t(0), C.byref(n))
+        cnt = n.value
+        ids = np.zeros(max(cnt, 1), np.uint32)
+        st = np.zeros((max(cnt, 1), 4), np.float32)
+        L.call(fn, self._h, L.fptr(lc), C.c_float(dist), L.uptr(ids), L.fptr(st),
+               C.c_size_t(cnt), C.byref(n))
+        return _birds(ids[:cnt], st[:cnt])
+
+    def get_neighbors_within_relax_distance(self, loc: Real2D, dist: float) -> List[Bird]:
+        """field_2d.rs:472-516"""
+        return self._query("kb_field_get_neighbors_within_relax_distance", loc, dist)
+
+    def get_neighbors_within_distance(self, loc: Real2D, dist: float) -> List[Bird]:
+        """field_2d.rs:386-440"""
+        return self._query("kb_field_get_neighbors_within_distance", loc, dist)
+
+    def _bag(self, fn: str, loc: Real2D) -> List[Bird]:
+        lc = loc.as_f32()
+        n = C.c_size_t()
+        L.call(fn, self._h, L.fptr(lc), None, None, C.c_size_t(0), C.byref(n))
+        cnt = n.value
+        ids = np.zeros(max(cnt, 1), np.uint32)
+        st = np.zeros((max(cnt, 1), 4), np.float32)
+        L.call(fn, self._h, L.fptr(lc), L.uptr(ids), L.fptr(st), C.c_size_t(cnt), C.byref(n))
+        return _birds(ids[:cnt], st[:cnt])
+
+    def get_objects(self, loc: Real2D) -> List[Bird]:
+        """field_2d.rs:544-549"""
+        return self._bag("kb_field_get_objects", loc)
+
+    def get_objects_unbuffered(self, loc: Real2D) -> List[Bird]:
+        """field_2d.rs:577-582"""
+        return self._bag("kb_field_get_objects_unbuffered", loc)
+
+    def num_objects_at_location(self, loc: Real2D) -> int:
+        """field_2d.rs:803-808"""
+        n = C.c_size_t()
+        L.call("kb_field_num_objects_at_location", self._h, L.fptr(loc.as_f32()), C.byref(n))
+        return n.value
+
+    def get_empty_bags(self) -> List[Real2D]:
+        """field_2d.rs:727-739"""
+        n = C.c_size_t()
+        L.call("kb_field_get_empty_bags", self._h, None, C.c_size_t(0), C.byref(n))
+        xy = np.zeros((max(n.value, 1), 2), np.float32)
+        L.call("kb_field_get_empty_bags", self._h, L.fptr(xy), C.c_size_t(n.value), C.byref(n))
+        return [Real2D(float(a), float(b)) for a, b in xy[: n.value]]
+
+    def get_random_empty_bag(self, seed: int = 0) -> Optional[Real2D]:
+        """field_2d.rs:764-772 (Philox(seed) instead of an unseeded rng)."""
+        xy = np.zeros(2, np.float32)
+        found = C.c_int32()
+        L.call("kb_field_get_random_empty_bag", self._h, C.c_uint64(seed), L.fptr(xy),
+               C.byref(found))
+        return Real2D(float(xy[0]), float(xy[1])) if found.value else None
+
+    def _iter(self, buffered: int) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = C.c_size_t()
+        L.call("kb_field_iter_objects", self._h, C.c_int32(buffered), None, None, None,
+               C.c_size_t(0), C.byref(n))
+        cnt = n.value
+        cxy = np.zeros((max(cnt, 1), 2), np.float32)
+        ids = np.zeros(max(cnt, 1), np.uint32)
+        st = np.zeros((max(cnt, 1), 4), np.float32)
+        L.call("kb_field_iter_objects", self._h, C.c_int32(buffered), L.fptr(cxy), L.uptr(ids),
+               L.fptr(st), C.c_size_t(cnt), C.byref(n))
+        return cxy[:cnt], ids[:cnt], st[:cnt]
+
+    def iter_objects(self, closure: Callable[[Real2D, Bird], None]) -> None:
+        """field_2d.rs:619-640"""
+        cxy, ids, st = self._iter(1)
+        for c, b in zip(cxy, _birds(ids, st)):
+            closure(Real2D(float(c[0]), float(c[1])), b)
+
+    def iter_objects_unbuffered(self, closure: Callable[[Real2D, Bird], None]) -> None:
+        """field_2d.rs:677-698"""
+        cxy, ids, st = self._iter(0)
+        for c, b in zip(cxy, _birds(ids, st)):
+            closure(Real2D(float(c[0]), float(c[1])), b)
+
+    # -- bulk state / parity support ---------------------------------
+    def get_state(self) -> Tuple[np.ndarray, np.ndarray]:
+        """Read buffer in stored order: (ids u32[n], states f32[n,4])."""
+        n = C.c_size_t()
+        L.call("kb_field_get_state", self._h, None, None, C.c_size_t(0), C.byref(n))
+        cnt = n.value
+        ids = np.zeros(max(cnt, 1), np.uint32)
+        st = np.zeros((max(cnt, 1), 4), np.float32)
+        L.call("kb_field_get_state", self._h, L.uptr(ids), L.fptr(st), C.c_size_t(cnt),
+               C.byref(n))
+        return ids[:cnt], st[:cnt]
+
+    def neighbor_lists(self, kind: int, dist: float, qxy: np.ndarray):
+        """Candidate id lists of many query points: (counts, packed ids)."""
+        q = np.ascontiguousarray(qxy, dtype=np.float32).reshape(-1, 2)
+        counts = np.zeros(max(len(q), 1), np.uint32)
+        total = C.c_size_t()
+        L.call("kb_field_neighbor_lists", self._h, C.c_int32(kind), C.c_float(dist),
+               C.c_size_t(len(q)), L.fptr(q), L.uptr(counts), None, C.c_size_t(0),
+               C.byref(total))
+        ids = np.zeros(max(total.value, 1), np.uint32)
+        L.call("kb_field_neighbor_lists", self._h, C.c_int32(kind), C.c_float(dist),
+               C.c_size_t(len(q)), L.fptr(q), L.uptr(counts), L.uptr(ids),
+               C.c_size_t(total.value), C.byref(total))
+        return counts[: len(q)], ids[: total.value]
+
+    def neighbor_digest(self, kind: int, dist: float, qxy: np.ndarray):
+        q = np.ascontiguousarray(qxy, dtype=np.float32).reshape(-1, 2)
+        counts = np.zeros(max(len(q), 1), np.uint32)
+        dig = np.zeros(max(len(q), 1), np.uint32)
+        L.call("kb_field_neighbor_digest", self._h, C.c_int32(kind), C.c_float(dist),
+               C.c_size_t(len(q)), L.fptr(q), L.uptr(counts), L.uptr(dig))
+        return counts[: len(q)], dig[: len(q)]
+
+    def device_flags(self, clear: bool = False) -> int:
+        v = C.c_uint32()
+        L.call("kb_field_device_flags", self._h, C.byref(v), C.c_int32(1 if clear else 0))
+        return v.value
+
+    def synchronize(self) -> None:
+        L.call("kb_field_synchronize", self._h)

@@ -1,0 +1,248 @@
+"""The Flockers step on the GPU against the oracle.
+
+Bars (all through the C ABI):
+  * neighbour sets: bit-exact (ids, in the reference's visiting order) at
+    every step;
+  * KB_ARITH_STRICT trajectories: bit-exact against the oracle and the
+    committed golden fixtures (the oracle is f32-faithful, so this is stronger
+    than the FP64 tolerance below);
+  * one step, either arithmetic: positions and headings within 1e-5 of the
+    domain size of the FP64 oracle;
+  * long runs of KB_ARITH_FAST: flock order parameter and mean neighbour count
+    within 1% of the strict run.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import krabmaga_gb300 as kg
+import oracle
+from conftest import C1_D, C1_SIDE
+from krabmaga_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL_REL_DOMAIN = 1e-5  # spec tolerance for one step vs FP64
+
+
+def gpu_field(side, d, ids, xy, dxy, tor=True):
+    f = kg.Field2D(side, side, d, tor, capacity_hint=len(ids))
+    f.set_locations(ids, xy, dxy)
+    f.lazy_update()
+    return f
+
+
+def oracle_field(side, d, ids, xy, dxy, tor=True):
+    o = oracle.OracleField(side, side, d, tor)
+    o.set_many(ids, xy, dxy)
+    o.lazy_update()
+    return o
+
+
+def step(f, p, first, n):
+    L.call("kb_flock_step", f.handle, C.byref(p.to_c()), C.c_uint64(first), C.c_uint32(n))
+
+
+def same_bits(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["c1_relax_strict.npz", "c1_exact_strict.npz"])
+def test_c1_matches_golden_fixtures(gpu, name):
+    g = np.load(os.path.join(GOLDEN, name))
+    f = gpu_field(C1_SIDE, C1_D, g["ids0"], g["xy0"], g["dxy0"])
+    p = kg.FlockParams(seed=int(g["seed"]), query_mode=int(g["kind"]), arith=kg.KB_ARITH_STRICT)
+    ids, st = f.get_state()
+    counts, lists = f.neighbor_lists(int(g["kind"]), 10.0, st[:, :2])
+    assert np.array_equal(counts, g["nb_counts0"]) and np.array_equal(lists, g["nb_ids0"])
+    done = 0
+    for c in g["checkpoints"]:
+        step(f, p, done, int(c) - done)
+        done = int(c)
+        ids, st = f.get_state()
+        assert np.array_equal(ids, g[f"ids_{c}"]), f"ids differ at step {c}"
+        assert same_bits(st, g[f"st_{c}"]), f"state differs at step {c}"
+
+
+@pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
+def test_c1_neighbour_sets_bit_exact_every_step(gpu, kind):
+    ids0, xy0, dxy0 = kg.gen_uniform(1000, C1_SIDE, C1_SIDE, 42, 1.0)
+    f = gpu_field(C1_SIDE, C1_D, ids0, xy0, dxy0)
+    o = oracle_field(C1_SIDE, C1_D, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=42, query_mode=kind, arith=kg.KB_ARITH_STRICT)
+    op = oracle.params_from(p)
+    for t in range(200):
+        ids, st = f.get_state()
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"state differs at step {t}"
+        gc, gl = f.neighbor_lists(kind, 10.0, st[:, :2])
+        oc, ol = o.neighbor_lists(kind, 10.0, ost[:, :2])
+        assert np.array_equal(gc, oc) and np.array_equal(gl, ol), f"neighbour sets differ at {t}"
+        step(f, p, t, 1)
+        o.flock_run(op, t, 1)
+
+
+def test_compute_plus_lazy_update_equals_fused_steps(gpu):
+    ids0, xy0, dxy0 = kg.gen_uniform(3000, 300.0, 300.0, 3, 1.0)
+    p = kg.FlockParams(seed=9)
+    a = gpu_field(300.0, C1_D, ids0, xy0, dxy0)
+    b = gpu_field(300.0, C1_D, ids0, xy0, dxy0)
+    state = kg.Flocker((300.0, 300.0), 3000, C1_D, params=p)
+    state.field1.close()
+    state.field1 = a  # already initialised and past its step-0 update
+    sched = kg.Schedule()
+    for t in range(30):  # the reference's per-step path: agents, then update
+        state.before_step(sched)
+        sched.step += 1
+        state.update(sched.step)
+    step(b, p, 0, 30)  # graph-replayed steps
+    ia, sa = a.get_state()
+    ib, sb = b.get_state()
+    assert np.array_equal(ia, ib) and same_bits(sa, sb)
+
+
+def test_general_rebuild_path_matches_oracle(gpu):
+    # A jump longer than a bag (1.2 > d = 1.0) can carry a boid past the
+    # neighbouring bag, so every step takes the general stable sort instead of
+    # the stencil gather; the result must still equal the oracle bit for bit.
+    ids0, xy0, dxy0 = kg.gen_uniform(2000, 120.0, 120.0, 4, 1.0)
+    p = kg.FlockParams(seed=1, jump=1.2, neighbor_radius=2.0)
+    d = 1.0  # jump > d: general path
+    f = gpu_field(120.0, d, ids0, xy0, dxy0)
+    o = oracle_field(120.0, d, ids0, xy0, dxy0)
+    step(f, p, 0, 25)
+    o.flock_run(oracle.params_from(p), 0, 25)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+
+
+def test_steps_are_deterministic(gpu):
+    ids0, xy0, dxy0 = kg.gen_uniform(20000, 900.0, 900.0, 5, 1.0)
+    outs = []
+    for _ in range(2):
+        f = gpu_field(900.0, C1_D, ids0, xy0, dxy0)
+        step(f, kg.FlockParams(seed=3, arith=kg.KB_ARITH_FAST), 0, 50)
+        outs.append(f.get_state())
+    assert np.array_equal(outs[0][0], outs[1][0]) and same_bits(outs[0][1], outs[1][1])
+
+
+def _fp64_one_step(side, d, ids0, xy0, dxy0, kind, arith):
+    f = gpu_field(side, d, ids0, xy0, dxy0)
+    o = oracle_field(side, d, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=77, query_mode=kind, arith=arith)
+    oid, ref = o.flock_step_fp64(oracle.params_from(p), 0)
+    step(f, p, 0, 1)
+    ids, st = f.get_state()
+    order = np.argsort(ids)
+    oorder = np.argsort(oid)
+    got = st[order].astype(np.float64)
+    want = ref[oorder]
+    dpos = np.abs(got[:, :2] - want[:, :2])
+    dpos = np.minimum(dpos, side - dpos)  # across the seam
+    dhead = np.abs(got[:, 2:] - want[:, 2:])
+    return max(dpos.max(), dhead.max()) / side
+
+
+@pytest.mark.parametrize("arith", [kg.KB_ARITH_STRICT, kg.KB_ARITH_FAST])
+@pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
+def test_one_step_within_fp64_tolerance(gpu, arith, kind):
+    ids0, xy0, dxy0 = kg.gen_uniform(1000, C1_SIDE, C1_SIDE, 42, 1.0)
+    err = _fp64_one_step(C1_SIDE, C1_D, ids0, xy0, dxy0, kind, arith)
+    assert err <= TOL_REL_DOMAIN, err
+
+
+def _order_and_neighbours(f, jump):
+    """Local order parameter (mean over boids of the norm of the mean unit
+    heading of its candidate neighbours) and mean candidate count."""
+    ids, st = f.get_state()
+    counts, lists = f.neighbor_lists(kg.KB_QUERY_RELAX, 10.0, st[:, :2])
+    pos = np.empty(int(ids.max()) + 1, np.int64)
+    pos[ids] = np.arange(len(ids))
+    h = st[:, 2:].astype(np.float64) / jump
+    owner = np.repeat(np.arange(len(ids)), counts)
+    sums = np.zeros((len(ids), 2))
+    np.add.at(sums, owner, h[pos[lists]])
+    local = np.linalg.norm(sums, axis=1) / np.maximum(counts, 1)
+    return local.mean(), counts.mean()
+
+
+def test_long_run_statistics_fast_vs_strict(gpu):
+    # C1-density flocks (0.025 boids per unit^2), 200 steps, 12 seeds of
+    # 10,000 boids: the ensemble means of both statistics agree within 1%.
+    res = {kg.KB_ARITH_STRICT: [], kg.KB_ARITH_FAST: []}
+    side = float(np.sqrt(10000 / 0.025))
+    for seed in range(12):
+        ids0, xy0, dxy0 = kg.gen_uniform(10000, side, side, 100 + seed, 1.0)
+        for arith in res:
+            f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+            step(f, kg.FlockParams(seed=seed, arith=arith), 0, 200)
+            res[arith].append(_order_and_neighbours(f, 0.7))
+    s = np.array(res[kg.KB_ARITH_STRICT]).mean(0)
+    q = np.array(res[kg.KB_ARITH_FAST]).mean(0)
+    print("strict (order, neighbours):", s, "fast:", q)
+    assert abs(q[0] - s[0]) / s[0] < 0.01, (q, s)
+    assert abs(q[1] - s[1]) / s[1] < 0.01, (q, s)
+
+
+def test_c2_full_size_one_step(gpu):
+    """1,048,576 boids at density 0.025: neighbour digests of every boid and
+    the one-step state (strict) equal the oracle's."""
+    n = 1 << 20
+    side = float(np.float32(np.sqrt(n / 0.025)))
+    ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 7, 1.0)
+    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+    gc, gd = f.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, st[:, :2])
+    oc, od = o.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, st[:, :2])
+    assert np.array_equal(gc, oc) and np.array_equal(gd, od)
+    p = kg.FlockParams(seed=7)
+    step(f, p, 0, 1)
+    o.flock_run(oracle.params_from(p), 0, 1)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+    assert f.device_flags() == 0
+
+
+def test_c3_clustered_digests(gpu):
+    """Clustered stress (256 Gaussian clusters, sigma 40) at a quarter of the
+    4,194,304-boid size: after 3 strict steps the state equals the oracle's
+    and so do the neighbour digests of a sample of boids."""
+    n = 1 << 20
+    side = 12952.0 / 2
+    ids0, xy0, dxy0 = kg.gen_clustered(n, side, side, 256, 40.0, 0.3, 11)
+    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=11)
+    step(f, p, 0, 3)
+    o.flock_run(oracle.params_from(p), 0, 3)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+    q = st[:: 97, :2]
+    gc, gd = f.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, q)
+    oc, od = o.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, q)
+    assert np.array_equal(gc, oc) and np.array_equal(gd, od)
+    assert gc.max() > 100  # dense cluster cores are exercised
+
+
+def test_device_jitter_matches_oracle_philox(gpu):
+    # a lone bird (no neighbours but itself) moves by momentum + jitter only:
+    # its heading reveals the device's Philox draws for (seed, id, step)
+    side = 100.0
+    ids = np.array([12345], np.uint32)
+    xy = np.array([[50.0, 50.0]], np.float32)
+    dxy = np.array([[0.0, 0.0]], np.float32)
+    f = gpu_field(side, C1_D, ids, xy, dxy)
+    o = oracle_field(side, C1_D, ids, xy, dxy)
+    p = kg.FlockParams(seed=(7 << 32) | 99, momentum=0.0)
+    for t in range(5):
+        step(f, p, t, 1)
+        o.flock_run(oracle.params_from(p), t, 1)
+        assert same_bits(f.get_state()[1], o.iter(1)[1])
