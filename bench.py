@@ -198,23 +198,42 @@ def run_ours(args, wl):
     pc = params.to_c()
 
     f = kg.Field2D(side, side, D_C, True, device=dev, capacity_hint=n)
+    tx, ty = (int(v) for v in args.tile.split("x"))
+    f.set_step_options(not args.unfused, tx, ty)
     f.set_locations(ids, xy, dxy)
     f.lazy_update()
     stream = torch.cuda.ExternalStream(f.cuda_stream(), device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
 
     def one_step(t):
-        L.call("kb_flock_compute", f.handle, C.byref(pc), C.c_uint64(t))
-        L.call("kb_field_lazy_update", f.handle)
+        L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(t), C.c_uint32(1))
 
     step_no = 0
     for _ in range(args.warmup):
         one_step(step_no)
         step_no += 1
     f.synchronize()
+    if args.profile:  # a short plain run for a profiler: warm-up, then `steps` launches
+        if args.phase_clocks:
+            L.call("kb_field_phase_clocks", f.handle, C.c_int32(1), None)
+        for _ in range(args.steps):
+            one_step(step_no)
+            step_no += 1
+        f.synchronize()
+        out = {"profile_run": True, "steps": args.steps, "stats": f.step_stats()}
+        if args.phase_clocks:
+            clk = (C.c_uint64 * 16)()
+            L.call("kb_field_phase_clocks", f.handle, C.c_int32(0), clk)
+            names = ["tile_setup", "segments_offsets", "serial_prefix", "stage_wait", "keys",
+                     "gather", "force", "hist_flush", "tile_fetch", "barrier1", "scan", "barrier2"]
+            ctas = out["stats"]["ctas"]
+            out["phase_us_per_step"] = {nm: clk[i] / ctas / args.steps / 2070.0
+                                        for i, nm in enumerate(names)}
+        print(json.dumps(out))
+        return
 
     K = args.steps
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
     barrier(ws)
     torch.cuda.synchronize(dev)
     with ClockSampler(dev) as clk:
@@ -222,18 +241,17 @@ def run_ours(args, wl):
             for k in range(K):
                 flush.fill_(k & 0xFF)  # evict L2 between timed steps
                 ev[k][0].record(stream)
-                L.call("kb_flock_compute", f.handle, C.byref(pc), C.c_uint64(step_no))
+                one_step(step_no)  # one persistent launch: the whole step
                 ev[k][1].record(stream)
-                L.call("kb_field_lazy_update", f.handle)
-                ev[k][2].record(stream)
                 step_no += 1
         torch.cuda.synchronize(dev)
     f.synchronize()  # raises if a kernel set the device error word
     barrier(ws)
-    step_ms = [ev[k][0].elapsed_time(ev[k][2]) for k in range(K)]
-    force_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
+    step_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
+    force_ms = step_ms
     total_s = allmax(ws, sum(step_ms) / 1e3)
     value = ws * n * K / total_s
+    stats = f.step_stats()
 
     # warm-L2 throughput (no flush, graph-replayed steps), informational
     torch.cuda.synchronize(dev)
@@ -281,9 +299,9 @@ def run_ours(args, wl):
         return
     hbm, peak_kind = peaks()
     ncells = (int(np.ceil(np.float32(side) / np.float32(D_C))) + 1) ** 2
-    force_bytes = n * 32 + ncells * 4  # state read+write per boid, bag offsets read
+    step_bytes = n * 32 + ncells * 8  # state read+write per boid, bag offsets write+read
     force_s = statistics.mean(force_ms) / 1e3
-    achieved = force_bytes / force_s / 1e9
+    achieved = step_bytes / force_s / 1e9
     clocks = clk.summary()
 
     cpu = None
@@ -300,12 +318,13 @@ def run_ours(args, wl):
                    "parallelism": f"replicas{ws}", "arith": args.arith, "query": "relax",
                    "l2": "flushed (512 MiB write) before every timed step",
                    "warm_l2_value": warm_value},
-        "roofline": {"bound": "hbm", "kernel": "k_flock_force", "achieved": achieved,
-                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_fused (whole step, one launch)",
+                     "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None,
-                     "algorithmic_bytes_per_launch": force_bytes,
-                     "force_ms_mean": statistics.mean(force_ms),
-                     "step_ms_mean": statistics.mean(step_ms)},
+                     "algorithmic_bytes_per_launch": step_bytes,
+                     "launch_ms_mean": statistics.mean(step_ms),
+                     "launch_ms_median": statistics.median(step_ms),
+                     "fused": stats},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
@@ -313,7 +332,7 @@ def run_ours(args, wl):
                 "d2h_bytes_per_call": d2h,
                 "call": f"Field2D create + set_locations + lazy_update + {e2e_steps} steps + "
                         f"get_state, host arrays in and out"},
-        "gpu_launches": 3 * K,
+        "gpu_launches": K,
     }
     print(json.dumps(line), flush=True)
 
@@ -331,6 +350,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--e2e-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile", default="0x0", help="fused tile shape TXxTY in bags (0x0: automatic)")
+    ap.add_argument("--unfused", action="store_true", help="separate force/scan/rebin kernels")
+    ap.add_argument("--profile", action="store_true", help="short plain run for ncu, no timing")
+    ap.add_argument("--phase-clocks", action="store_true", help="with --profile: per-phase cycles")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -158,6 +158,18 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
  * initialisation, as Schedule::step does at step 0, schedule.rs:349-351). */
 kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                         uint32_t nsteps);
+/* Step implementation options (no reference counterpart; tuning only):
+ * fused = 1 runs eligible fields (toroidal, square, jump < discretization)
+ * through the persistent fused step, 0 through the separate force / scan /
+ * rebin kernels; tile_tx x tile_ty bags per tile (0 = automatic). */
+kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty);
+/* Counters of the fused step: out4 = {tiles that ran through the global
+ * scratch path (cumulative), tiles per step, CTAs, tx << 16 | ty}. */
+kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]);
+/* Tuning aid (no reference counterpart): enable = 1 makes the fused step
+ * accumulate per-phase cycle counts; out16 (may be NULL) receives the sums
+ * over CTAs of the 16 phase counters. */
+kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long* out16);
 /* Read buffer in its stored order (bags ascending, insertion order inside a
  * bag): ids and {x, y, dx, dy} states; either may be NULL. */
 kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n);

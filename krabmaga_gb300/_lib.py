@@ -106,6 +106,9 @@ _SIGS = {
     "kb_field_get_random_empty_bag": (C.c_int32, [_P, C.c_uint64, _F, C.POINTER(C.c_int32)]),
     "kb_field_iter_objects": (C.c_int32, [_P, C.c_int32, _F, _U32, _F, C.c_size_t, _SZ]),
     "kb_flock_compute": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64]),
+    "kb_field_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "kb_field_step_stats": (C.c_int32, [_P, _U32]),
+    "kb_field_phase_clocks": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_uint64)]),
     "kb_flock_step": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_uint32]),
     "kb_field_get_state": (C.c_int32, [_P, _U32, _F, C.c_size_t, _SZ]),
     "kb_field_device_flags": (C.c_int32, [_P, _U32, C.c_int32]),

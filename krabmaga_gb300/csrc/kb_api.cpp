@@ -13,6 +13,7 @@
 
 #include "../../include/krabgpu.h"
 #include "kb_common.h"
+#include "kb_fused.h"
 #include "kb_launch.h"
 #include "kb_runtime.h"
 
@@ -77,6 +78,11 @@ void set_rep_params(Rep* R, const kb_flock_params* p) {
     R->qmode = p->query_mode;
     R->seed_lo = (uint32_t)p->seed;
     R->seed_hi = (uint32_t)(p->seed >> 32);
+    // With the clamped (toroidal) cell range every candidate lies within
+    // (dd+1)*d of the boid, so toroidal_distance's |a-b| <= dim/2 test holds
+    // whenever (dd+1)*d stays clear of half the side.
+    const double reach = ((double)std::max(R->dd, 0) + 1.0) * (double)R->d;
+    R->nowrap = (R->toroidal && reach * 1.01 + 1e-3 < 0.5 * (double)std::min(R->w, R->h)) ? 1 : 0;
 }
 
 bool params_ok(const kb_flock_params* p, std::string* why) {
@@ -157,8 +163,29 @@ struct kb_field {
         }
     };
     std::map<GraphKey, cudaGraphExec_t> graphs;
-    uint64_t buffers_version = 0;
-    uint64_t graphs_version = 0;
+    // persistent fused step (kb_fused.cu)
+    struct Fused {
+        bool ready = false;
+        uint32_t n = 0;
+        int strict = -1, qmode = -1, dd = -1;
+        FusedCfg cfg{};
+        uint32_t nctas = 0;
+        uint32_t ntiles = 0;
+        DevBuf<Tile> tiles;
+        DevBuf<float4> g_st;
+        DevBuf<uint32_t> g_ids;
+        DevBuf<unsigned long long> scan_state;
+        DevBuf<uint32_t> ctl;  // [0] tile counter, [1..2] barrier, [3] scan epoch, [4] overflow tiles
+        DevBuf<unsigned long long> phase_cycles;  // per-CTA phase clocks when profiling
+        bool profile = false;
+    } fused;
+    int fused_mode = 1;  // 0 off, 1 on when eligible
+    // After fused steps the read buffer can stay virtual: the last write list
+    // (in buffer a_last: 0 rst, 1 wst, 2 tst) plus start[1-cur] (its bag
+    // offsets) and start[cur] (the read buffer's bag offsets).
+    bool virt = false;
+    int a_last = 0;
+    int32_t tile_tx = 0, tile_ty = 0;  // 0: automatic
 
     ~kb_field() {
         drop_graphs();
@@ -191,8 +218,14 @@ struct DeviceGuard {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
+kb_status materialize(kb_field* f);
+
 kb_status grow(kb_field* f, uint32_t need) {
     if (need <= f->cap) return KB_OK;
+    if (f->virt) {
+        kb_status st = materialize(f);
+        if (st) return st;
+    }
     uint64_t nc = std::max<uint64_t>(need, (uint64_t)f->cap * 2);
     if (nc < 1024) nc = 1024;
     if (nc > 0xFFFFFFF0ull) nc = 0xFFFFFFF0ull;
@@ -332,13 +365,178 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     a.out_key = f->wkey.p;
     a.hist = f->hist.p;
     a.err = f->err.p;
+    a.check_moves = fast_rebin_ok(f->rep) ? 1 : 0;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
+    return KB_OK;
+}
+
+float4* buf_st(kb_field* f, int i) { return i == 0 ? f->rst.p : (i == 1 ? f->wst.p : f->tst.p); }
+uint32_t* buf_ids(kb_field* f, int i) { return i == 0 ? f->rid.p : (i == 1 ? f->wid.p : f->tid.p); }
+
+// Rebuild the read buffer from a virtual state (the stencil gather of the
+// last write list into canonical order).
+kb_status materialize(kb_field* f) {
+    if (!f->virt) return KB_OK;
+    int dst = 0;
+    if (f->a_last == 0) dst = 1;  // the write list sits in rst: gather into wst, then swap roles
+    RebinArgs r;
+    r.reps = f->d_rep.p;
+    r.nrep = 1;
+    r.start_cur = f->start[1 - f->cur].p;
+    r.start_next = f->start[f->cur].p;
+    r.key = nullptr;
+    r.a_st = buf_st(f, f->a_last);
+    r.a_ids = buf_ids(f, f->a_last);
+    r.ncells = f->rep.ncells;
+    r.s_st = buf_st(f, dst);
+    r.s_ids = buf_ids(f, dst);
+    r.step = nullptr;
+    r.err = f->err.p;
+    KB_CUDA(launch_rebin(r, f->stream));
+    if (dst == 1) {
+        f->rst.swap(f->wst);
+        f->rid.swap(f->wid);
+        f->drop_graphs();
+    }
+    f->virt = false;
+    return KB_OK;
+}
+
+// Tile shape and shared-memory capacities for a field of n boids: tiles of
+// tx x ty bags; capacities sized from the mean occupancy with room for
+// Poisson fluctuations (over-full tiles take the global scratch path).
+FusedCfg fused_config(const kb_field* f, int dd) {
+    FusedCfg c{};
+    c.tx = f->tile_tx > 0 ? f->tile_tx : 16;
+    c.ty = f->tile_ty > 0 ? f->tile_ty : 32;
+    c.dd = dd;
+    const double rho = (double)f->rn / (double)f->rep.ncells;
+    const double staged_cells = (double)(c.tx + 2 * dd + 2) * (c.ty + 2 * dd + 2);
+    const double sord_cells = (double)(c.tx + 2 * dd) * (c.ty + 2 * dd);
+    auto cap = [](double mean) {
+        double v = mean * 1.5 + 6.0 * std::sqrt(mean + 1.0) + 64.0;
+        if (v > 6144.0) v = 6144.0;
+        return (uint32_t)((uint32_t)v + 31u) / 32u * 32u;
+    };
+    c.stage_cap = cap(rho * staged_cells);
+    c.sord_cap = cap(rho * sord_cells);
+    return c;
+}
+
+bool fused_eligible(const kb_field* f, const kb_flock_params* p) {
+    return f->fused_mode != 0 && f->rep.toroidal && fast_rebin_ok(f->rep) &&
+           f->layout_is_positions && f->rn > 0 && f->rep.dd <= FUSED_DD_MAX &&
+           (p->query_mode == KB_QUERY_RELAX || p->query_mode == KB_QUERY_EXACT);
+}
+
+kb_status fused_prepare(kb_field* f, const kb_flock_params* p) {
+    auto& F = f->fused;
+    const int strict = p->arith == KB_ARITH_STRICT ? 1 : 0;
+    const int dd = std::max(f->rep.dd, 0);
+    if (F.ready && F.n == f->rn && F.strict == strict && F.qmode == p->query_mode && F.dd == dd)
+        return KB_OK;
+    F.ready = false;
+    FusedCfg cfg = fused_config(f, dd);
+    int maxc = fused_max_ctas(cfg, strict != 0, p->query_mode, f->device);
+    while (maxc <= 0 && (cfg.stage_cap > 256 || cfg.sord_cap > 256)) {
+        cfg.stage_cap = std::max(256u, cfg.stage_cap / 2);
+        cfg.sord_cap = std::max(256u, cfg.sord_cap / 2);
+        maxc = fused_max_ctas(cfg, strict != 0, p->query_mode, f->device);
+    }
+    if (maxc <= 0) return fail(KB_ERR_CUDA, "fused step: no co-resident CTA fits");
+    std::vector<Tile> tiles;
+    for (int x = 0; x < f->rep.dw; x += cfg.tx)
+        for (int y = 0; y < f->rep.dh; y += cfg.ty)
+            tiles.push_back(Tile{0u, (uint16_t)x, (uint16_t)y});
+    if (f->rep.dw > 65535 || f->rep.dh > 65535) return fail(KB_ERR_ARG, "bag matrix side above 65535");
+    cudaError_t e = F.tiles.alloc(tiles.size());
+    if (!e) e = F.g_st.alloc(f->rn);
+    if (!e) e = F.g_ids.alloc(f->rn);
+    if (!e) e = F.scan_state.alloc((size_t)maxc);
+    if (!e) e = F.ctl.alloc(8);
+    if (e) return cuda_fail(e, "fused step buffers");
+    KB_CUDA(cudaMemcpyAsync(F.tiles.p, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemsetAsync(F.scan_state.p, 0, sizeof(unsigned long long) * maxc, f->stream));
+    KB_CUDA(cudaMemsetAsync(F.ctl.p, 0, sizeof(uint32_t) * 8, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    F.cfg = cfg;
+    F.nctas = (uint32_t)maxc;
+    F.ntiles = (uint32_t)tiles.size();
+    F.n = f->rn;
+    F.strict = strict;
+    F.qmode = p->query_mode;
+    F.dd = dd;
+    F.ready = true;
+    f->drop_graphs();
+    return KB_OK;
+}
+
+// nsteps steps of the persistent kernel.  From a materialised read buffer
+// the first step's rebin is the identity (previous offsets := current ones);
+// from a virtual state the kernel continues from the last write list.  The
+// read buffer is left virtual.
+kb_status fused_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
+    auto& F = f->fused;
+    cudaStream_t s = f->stream;
+    const int cur0 = f->cur;
+    int in = 0;
+    if (!f->virt) {
+        const size_t sb = sizeof(uint32_t) * ((size_t)f->rep.ncells + 1);
+        KB_CUDA(cudaMemcpyAsync(f->start[1 - cur0].p, f->start[cur0].p, sb, cudaMemcpyDeviceToDevice, s));
+        in = 0;
+    } else {
+        in = f->a_last;
+    }
+    const int o0 = in == 0 ? 1 : 0, o1 = in == 2 ? 1 : 2;  // the two buffers that are not the input
+    FusedArgs a{};
+    a.reps = f->d_rep.p;
+    a.nrep = 1;
+    a.tiles = F.tiles.p;
+    a.ntiles = F.ntiles;
+    a.cfg = F.cfg;
+    a.ncells = f->rep.ncells;
+    a.n = f->rn;
+    a.a_in_st = buf_st(f, in);
+    a.a_in_ids = buf_ids(f, in);
+    a.a_st[0] = buf_st(f, o0);
+    a.a_st[1] = buf_st(f, o1);
+    a.a_ids[0] = buf_ids(f, o0);
+    a.a_ids[1] = buf_ids(f, o1);
+    a.start_b[0] = f->start[1 - cur0].p;
+    a.start_b[1] = f->start[cur0].p;
+    a.hist = f->hist.p;
+    a.g_sord_st = F.g_st.p;
+    a.g_sord_ids = F.g_ids.p;
+    a.step = f->dstep.p;
+    a.nsteps = nsteps;
+    a.tile_counter = F.ctl.p;
+    a.bar = F.ctl.p + 1;
+    a.scan_state = F.scan_state.p;
+    a.scan_epoch = F.ctl.p + 3;
+    a.err = f->err.p;
+    a.stats = F.ctl.p + 4;
+    a.phase_cycles = nullptr;
+    if (F.profile) {
+        if (F.phase_cycles.n < (size_t)F.nctas * 16) {
+            cudaError_t e = F.phase_cycles.alloc((size_t)F.nctas * 16);
+            if (e) return cuda_fail(e, "phase clocks");
+            KB_CUDA(cudaMemsetAsync(F.phase_cycles.p, 0, sizeof(unsigned long long) * F.nctas * 16, s));
+        }
+        a.phase_cycles = F.phase_cycles.p;
+    }
+    KB_CUDA(launch_fused(a, F.strict != 0, F.qmode, F.nctas, s));
+    const int last = (int)((nsteps - 1) & 1u);
+    f->a_last = last == 0 ? o0 : o1;
+    // the newest offsets are in start_b[last]; the previous ones in the other
+    f->cur = (last == 0) ? 1 - cur0 : cur0;
+    f->virt = true;
     return KB_OK;
 }
 
 kb_status field_lazy_update(kb_field* f) {
     kb_status st = flush_pending(f);
     if (st) return st;
+    f->virt = false;  // the write buffer replaces the read buffer
     // field_2d.rs:905-921: the first swap fixes nagents' density estimate.
     if (!f->density_check) f->density_check = true;
     if (f->w_from_compute && !f->w_has_dead) {
@@ -543,6 +741,7 @@ static kb_status query_points(kb_field* f, int kind, float dist, size_t nq, cons
                               size_t cap, size_t* total) {
     if (nq > 0x7FFFFFFFull) return fail(KB_ERR_ARG, "too many query points");
     DeviceGuard g(f->device);
+    if (kb_status st0 = materialize(f)) return st0;
     if (nq == 0) {
         if (total) *total = 0;
         return KB_OK;
@@ -640,6 +839,9 @@ kb_status kb_field_get_objects(kb_field* f, const float loc[2], uint32_t* ids, f
     int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
     if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
     DeviceGuard g(f->device);
+    if (cap && (ids || states)) {
+        if (kb_status st0 = materialize(f)) return st0;
+    }
     uint32_t se[2];
     KB_CUDA(cudaMemcpyAsync(se, f->start[f->cur].p + idx, sizeof(se), cudaMemcpyDeviceToHost, f->stream));
     KB_CUDA(cudaStreamSynchronize(f->stream));
@@ -741,6 +943,7 @@ kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, u
     DevBuf<float4> tmp_st, tmp_sorted;
     DevBuf<uint32_t> tmp_sorted_id;
     if (buffered) {
+        if (kb_status st0 = materialize(f)) return st0;
         src_st = f->rst.p;
         src_id = f->rid.p;
         src_start = f->start[f->cur].p;
@@ -795,6 +998,7 @@ kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, u
 kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n) {
     if (!f || !n) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
+    if (kb_status st0 = materialize(f)) return st0;
     *n = f->rn;
     const size_t take = std::min<size_t>(f->rn, cap);
     if (take) {
@@ -824,6 +1028,48 @@ kb_status kb_field_synchronize(kb_field* f) {
     return check_flags(f);
 }
 
+kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty) {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    if (tile_tx < 0 || tile_ty < 0 || tile_tx > 64 || tile_ty > 128)
+        return fail(KB_ERR_ARG, "tile shape out of range (tx <= 64, ty <= 128)");
+    f->fused_mode = fused ? 1 : 0;
+    f->tile_tx = tile_tx;
+    f->tile_ty = tile_ty;
+    f->fused.ready = false;
+    return KB_OK;
+}
+
+kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long* out16) {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    f->fused.profile = enable != 0;
+    if (out16) {
+        for (int k = 0; k < 16; ++k) out16[k] = 0;
+        const size_t n = f->fused.phase_cycles.n;
+        if (n) {
+            std::vector<unsigned long long> h(n);
+            KB_CUDA(cudaMemcpyAsync(h.data(), f->fused.phase_cycles.p, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, f->stream));
+            KB_CUDA(cudaStreamSynchronize(f->stream));
+            for (size_t i = 0; i < n; ++i) out16[i % 16] += h[i];
+        }
+    }
+    return KB_OK;
+}
+
+kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]) {
+    if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    out4[0] = out4[1] = out4[2] = out4[3] = 0;
+    if (f->fused.ready) {
+        KB_CUDA(cudaMemcpyAsync(out4, f->fused.ctl.p + 4, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
+        KB_CUDA(cudaStreamSynchronize(f->stream));
+        out4[1] = f->fused.ntiles;
+        out4[2] = f->fused.nctas;
+        out4[3] = (uint32_t)f->fused.cfg.tx << 16 | (uint32_t)f->fused.cfg.ty;
+    }
+    return KB_OK;
+}
+
 kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step) {
     if (!f || !p) return fail(KB_ERR_ARG, "null argument");
     std::string why;
@@ -831,8 +1077,9 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
     if (f->wn || !f->p_id.empty())
         return fail(KB_ERR_STATE, "write buffer not empty: call lazy_update first");
     DeviceGuard g(f->device);
-    kb_status st = grow(f, f->rn);
+    kb_status st = materialize(f);
     if (st) return st;
+    if ((st = grow(f, f->rn))) return st;
     set_rep_params(&f->rep, p);
     if ((st = upload_rep(f))) return st;
     KB_CUDA(launch_set_u64(f->dstep.p, step, f->stream));
@@ -866,12 +1113,12 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         return fail(KB_ERR_STATE, "write buffer not empty: call lazy_update first");
     if (nsteps == 0) return KB_OK;
     DeviceGuard g(f->device);
-    kb_status st = grow(f, f->rn);
-    if (st) return st;
     set_rep_params(&f->rep, p);
+    kb_status st;
+    if (f->virt && !fused_eligible(f, p) && (st = materialize(f))) return st;
+    if (!f->virt && (st = grow(f, f->rn))) return st;
     if ((st = upload_rep(f))) return st;
     KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
-    const bool fast = fast_rebin_ok(f->rep) && f->layout_is_positions;
     uint32_t done = 0;
     if (!f->layout_is_positions) {
         // the first step after arbitrary set_object_location calls re-sorts generally
@@ -879,6 +1126,12 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         f->layout_is_positions = true;
         done = 1;
     }
+    if (done < nsteps && fused_eligible(f, p)) {
+        if ((st = fused_prepare(f, p))) return st;
+        if ((st = fused_steps(f, p, nsteps - done))) return st;
+        return KB_OK;
+    }
+    if (f->virt && (st = materialize(f))) return st;
     const bool use_fast = fast_rebin_ok(f->rep);
     // CUDA-graph replay of chunks of up to 100 steps (one graph per chunk
     // length and start parity; the graph reads the step number from device

@@ -39,7 +39,7 @@ struct Rep {
     int32_t dd;             // floor(radius/d) (field_2d.rs:488), -1 when radius <= 0
     int32_t qmode;          // 0 relax, 1 exact
     uint32_t seed_lo, seed_hi;
-    uint32_t _pad;
+    int32_t nowrap;         // 1: no candidate pair can straddle the seam ((dd+1)*d < min(w,h)/2)
 };
 
 // ------------------------------------------------------------------ Philox

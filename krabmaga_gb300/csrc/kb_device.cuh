@@ -1,0 +1,241 @@
+// kb_device.cuh -- device helpers shared by the kernels: the reference's
+// f32 helper functions with its rounding points, the query cell range, bag
+// indexing, replica lookup and the per-boid force accumulator.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kb_common.h"
+
+namespace kb {
+
+// ---------------------------------------------------------- f32 arithmetic
+// STRICT: every operation rounds once, as the reference's Rust f32 code does
+// (no fused multiply-add, IEEE division and square root).  FAST: the
+// compiler may fuse, and divisions use the approximate reciprocal.
+template <bool STRICT>
+struct F;
+template <>
+struct F<true> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+};
+template <>
+struct F<false> {
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
+};
+
+// field_2d.rs:1004-1014
+__device__ __forceinline__ float toroidal_transform(float v, float dim) {
+    if (v >= 0.0f && v < dim) return v;
+    float r = fmodf(v, dim);
+    if (r < 0.0f) r = __fadd_rn(r, dim);
+    return r;
+}
+
+// field_2d.rs:988-1002
+__device__ __forceinline__ float toroidal_distance(float a, float b, float dim) {
+    float d0 = __fsub_rn(a, b);
+    // dim / 2.0 is exact, so it equals dim * 0.5 bit for bit
+    if (fabsf(d0) <= __fmul_rn(dim, 0.5f)) return d0;
+    float d = __fsub_rn(toroidal_transform(a, dim), toroidal_transform(b, dim));
+    float d2 = __fmul_rn(d, 2.0f);
+    if (d2 > dim) return __fsub_rn(d, dim);
+    if (d2 < -dim) return __fadd_rn(d, dim);
+    return d;
+}
+
+// field_2d.rs:974-986
+__device__ __forceinline__ float distance(float x1, float y1, float x2, float y2, float w, float h,
+                                          bool tor) {
+    float dx, dy;
+    if (tor) {
+        dx = toroidal_distance(x1, x2, w);
+        dy = toroidal_distance(y1, y2, h);
+    } else {
+        dx = __fsub_rn(x1, x2);
+        dy = __fsub_rn(y1, y2);
+    }
+    return __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+}
+
+// field_2d.rs:934-972: 1 = whole bag inside, -1 = bag skipped, 0 = filter.
+__device__ __forceinline__ int check_circle(int bx, int by, const Rep& R, float lx, float ly,
+                                            float dis) {
+    float nw_x = __fmul_rn((float)bx, R.d), nw_y = __fmul_rn((float)by, R.d);
+    float ne_y = fminf(__fadd_rn(nw_y, R.d), R.h);
+    float sw_x = fminf(__fadd_rn(nw_x, R.d), R.w);
+    bool tor = R.toroidal != 0;
+    float a = distance(nw_x, nw_y, lx, ly, R.w, R.h, tor);
+    float b = distance(nw_x, ne_y, lx, ly, R.w, R.h, tor);
+    float c = distance(sw_x, nw_y, lx, ly, R.w, R.h, tor);
+    float e = distance(sw_x, ne_y, lx, ly, R.w, R.h, tor);
+    if (a <= dis && b <= dis && c <= dis && e <= dis) return 1;
+    if (a > dis && b > dis && c > dis && e > dis) return -1;
+    return 0;
+}
+
+// discretize (field_2d.rs:328-339), always IEEE (bag choice is index work).
+__device__ __forceinline__ int32_t disc(float v, float d) { return as_i32(floorf(__fdiv_rn(v, d))); }
+
+// The query's cell range (field_2d.rs:398-418 / 484-500).  False: dist <= 0.
+__device__ __forceinline__ bool cell_range(const Rep& R, float x, float y, int32_t dd, int* mi,
+                                           int* Mi, int* mj, int* Mj) {
+    if (dd < 0) return false;
+    int cx = disc(x, R.d), cy = disc(y, R.d);
+    int a = cx - dd, b = cx + dd, c = cy - dd, e = cy + dd;
+    if (R.toroidal) {
+        a = max(0, a);
+        b = min(b, R.max_x - 1);
+        c = max(0, c);
+        e = min(e, R.max_y - 1);
+    }
+    *mi = a; *Mi = b; *mj = c; *Mj = e;
+    return true;
+}
+
+// Reference bag index ((x*dh)+y) with i32 wrapping; -1 outside the matrix.
+__device__ __forceinline__ int64_t bag_index(const Rep& R, int32_t cx, int32_t cy) {
+    int32_t idx = (int32_t)((uint32_t)cx * (uint32_t)R.dh + (uint32_t)cy);
+    if (idx < 0 || (uint32_t)idx >= R.ncells) return -1;
+    return idx;
+}
+
+__device__ __forceinline__ uint32_t id_mix(uint32_t id) {
+    uint32_t z = id * 0x9E3779B1u;
+    z ^= z >> 15;
+    z *= 0x85EBCA77u;
+    z ^= z >> 13;
+    return z;
+}
+
+// Replica owning boid slot i / cell c (tables sorted by offset).
+__device__ __forceinline__ int rep_of_boid(const Rep* reps, int nrep, uint32_t i) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&reps[mid].boid_off) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int rep_of_cell(const Rep* reps, int nrep, uint32_t c) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&reps[mid].cell_off) <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------- force pass
+// One thread per boid of the read buffer: Bird::step (bird.rs:39-154)
+// against the read buffer, next state into the write list at the same slot.
+template <bool STRICT>
+struct Acc {
+    float xa = 0.f, ya = 0.f, xc = 0.f, yc = 0.f, xs = 0.f, ys = 0.f;
+    int count = 0;
+    uint32_t vec = 0;  // candidates including self (the reference's vec.len())
+
+    __device__ __forceinline__ void add(const Rep& R, float sx, float sy, float4 o) {
+        using M = F<STRICT>;
+        // toroidal_distance's first branch is taken for every pair when the
+        // replica guarantees it (Rep::nowrap): the same bits, no test
+        float dx = R.nowrap ? __fsub_rn(sx, o.x) : toroidal_distance(sx, o.x, R.w);
+        float dy = R.nowrap ? __fsub_rn(sy, o.y) : toroidal_distance(sy, o.y, R.h);
+        count += 1;
+        float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
+        float q = M::add(M::mul(sq, sq), 1.0f);
+        if (STRICT) {
+            xa = M::add(xa, M::div(dx, q));
+            ya = M::add(ya, M::div(dy, q));
+        } else {
+            float inv = __fdividef(1.0f, q);
+            xa = xa + dx * inv;
+            ya = ya + dy * inv;
+        }
+        xc = M::add(xc, dx);
+        yc = M::add(yc, dy);
+        xs = M::add(xs, o.z);
+        ys = M::add(ys, o.w);
+    }
+};
+
+// k-th candidate source line of line X (where a bag can receive boids from in one step): the
+// low seam lines, X-1..X+1, the high seam lines.  -1 when absent.  For
+// maxv >= 3 the sequence is non-decreasing, so skipping values <= the last
+// one taken yields the ascending unique set.
+__device__ __forceinline__ int src_line(int k, int X, int maxv) {
+    switch (k) {
+        case 0: return X >= maxv - 1 ? 0 : -1;
+        case 1: return X >= maxv - 1 ? 1 : -1;
+        case 2: return X - 1;
+        case 3: return X;
+        case 4: return X + 1;
+        case 5: return X <= 1 ? maxv - 1 : -1;
+        default: return X <= 1 ? maxv : -1;
+    }
+}
+
+// bird.rs:84-149: averages, avoidance/cohesion/consistency, Philox jitter
+// (only when the candidate list is non-empty), the weighted sum, the JUMP
+// normalisation and the toroidal move.  Returns {x, y, dx, dy}.
+template <bool STRICT>
+__device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t my_id,
+                                              unsigned long long step, const Acc<STRICT>& acc) {
+    using M = F<STRICT>;
+    float avx = 0.f, avy = 0.f, cox = 0.f, coy = 0.f, rax = 0.f, ray = 0.f, csx = 0.f, csy = 0.f;
+    if (acc.vec > 0) {
+        float xa = acc.xa, ya = acc.ya, xc = acc.xc, yc = acc.yc, xs = acc.xs, ys = acc.ys;
+        if (acc.count > 0) {
+            const float c = (float)acc.count;
+            xa = M::div(xa, c); ya = M::div(ya, c);
+            xc = M::div(xc, c); yc = M::div(yc, c);
+            xs = M::div(xs, c); ys = M::div(ys, c);
+            csx = M::div(xs, c);  // bird.rs:91-94: a second division by count
+            csy = M::div(ys, c);
+        } else {
+            csx = xs;
+            csy = ys;
+        }
+        avx = M::mul(400.0f, xa);
+        avy = M::mul(400.0f, ya);
+        cox = M::div(-xc, 10.0f);
+        coy = M::div(-yc, 10.0f);
+        const U4 o = philox4x32_10(U4{my_id, (uint32_t)step, (uint32_t)(step >> 32), STREAM_JITTER},
+                                   R.seed_lo, R.seed_hi);
+        const float xr = M::sub(M::mul(unit_f32(o.x), 2.0f), 1.0f);
+        const float yr = M::sub(M::mul(unit_f32(o.y), 2.0f), 1.0f);
+        const float sq = M::sqrt(M::add(M::mul(xr, xr), M::mul(yr, yr)));
+        rax = M::div(M::mul(0.05f, xr), sq);
+        ray = M::div(M::mul(0.05f, yr), sq);
+    }
+    float dx = M::add(M::add(M::add(M::add(M::mul(R.coh, cox), M::mul(R.avo, avx)),
+                                    M::mul(R.con, csx)),
+                             M::mul(R.rnd, rax)),
+                      M::mul(R.mom, me.z));
+    float dy = M::add(M::add(M::add(M::add(M::mul(R.coh, coy), M::mul(R.avo, avy)),
+                                    M::mul(R.con, csy)),
+                             M::mul(R.rnd, ray)),
+                      M::mul(R.mom, me.w));
+    const float dis = M::sqrt(M::add(M::mul(dx, dx), M::mul(dy, dy)));
+    if (dis > 0.0f) {
+        dx = M::mul(M::div(dx, dis), R.jump);
+        dy = M::mul(M::div(dy, dis), R.jump);
+    }
+    const float nx = toroidal_transform(__fadd_rn(me.x, dx), R.w);
+    const float ny = toroidal_transform(__fadd_rn(me.y, dy), R.w);  // bird.rs:147: y wraps with w
+
+    return make_float4(nx, ny, dx, dy);
+}
+
+}  // namespace kb

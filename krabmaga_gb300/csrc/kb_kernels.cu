@@ -14,166 +14,10 @@
 #include "kb_common.h"
 #include "kb_launch.h"
 #include "kb_runtime.h"
+#include "kb_device.cuh"
 
 namespace kb {
 namespace {
-
-// ---------------------------------------------------------- f32 arithmetic
-// STRICT: every operation rounds once, as the reference's Rust f32 code does
-// (no fused multiply-add, IEEE division and square root).  FAST: the
-// compiler may fuse, and divisions use the approximate reciprocal.
-template <bool STRICT>
-struct F;
-template <>
-struct F<true> {
-    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
-    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
-};
-template <>
-struct F<false> {
-    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
-    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
-    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
-    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
-    static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
-};
-
-// field_2d.rs:1004-1014
-__device__ __forceinline__ float toroidal_transform(float v, float dim) {
-    if (v >= 0.0f && v < dim) return v;
-    float r = fmodf(v, dim);
-    if (r < 0.0f) r = __fadd_rn(r, dim);
-    return r;
-}
-
-// field_2d.rs:988-1002
-__device__ __forceinline__ float toroidal_distance(float a, float b, float dim) {
-    float d0 = __fsub_rn(a, b);
-    if (fabsf(d0) <= __fdiv_rn(dim, 2.0f)) return d0;
-    float d = __fsub_rn(toroidal_transform(a, dim), toroidal_transform(b, dim));
-    float d2 = __fmul_rn(d, 2.0f);
-    if (d2 > dim) return __fsub_rn(d, dim);
-    if (d2 < -dim) return __fadd_rn(d, dim);
-    return d;
-}
-
-// field_2d.rs:974-986
-__device__ __forceinline__ float distance(float x1, float y1, float x2, float y2, float w, float h,
-                                          bool tor) {
-    float dx, dy;
-    if (tor) {
-        dx = toroidal_distance(x1, x2, w);
-        dy = toroidal_distance(y1, y2, h);
-    } else {
-        dx = __fsub_rn(x1, x2);
-        dy = __fsub_rn(y1, y2);
-    }
-    return __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
-}
-
-// field_2d.rs:934-972: 1 = whole bag inside, -1 = bag skipped, 0 = filter.
-__device__ __forceinline__ int check_circle(int bx, int by, const Rep& R, float lx, float ly,
-                                            float dis) {
-    float nw_x = __fmul_rn((float)bx, R.d), nw_y = __fmul_rn((float)by, R.d);
-    float ne_y = fminf(__fadd_rn(nw_y, R.d), R.h);
-    float sw_x = fminf(__fadd_rn(nw_x, R.d), R.w);
-    bool tor = R.toroidal != 0;
-    float a = distance(nw_x, nw_y, lx, ly, R.w, R.h, tor);
-    float b = distance(nw_x, ne_y, lx, ly, R.w, R.h, tor);
-    float c = distance(sw_x, nw_y, lx, ly, R.w, R.h, tor);
-    float e = distance(sw_x, ne_y, lx, ly, R.w, R.h, tor);
-    if (a <= dis && b <= dis && c <= dis && e <= dis) return 1;
-    if (a > dis && b > dis && c > dis && e > dis) return -1;
-    return 0;
-}
-
-// discretize (field_2d.rs:328-339), always IEEE (bag choice is index work).
-__device__ __forceinline__ int32_t disc(float v, float d) { return as_i32(floorf(__fdiv_rn(v, d))); }
-
-// The query's cell range (field_2d.rs:398-418 / 484-500).  False: dist <= 0.
-__device__ __forceinline__ bool cell_range(const Rep& R, float x, float y, int32_t dd, int* mi,
-                                           int* Mi, int* mj, int* Mj) {
-    if (dd < 0) return false;
-    int cx = disc(x, R.d), cy = disc(y, R.d);
-    int a = cx - dd, b = cx + dd, c = cy - dd, e = cy + dd;
-    if (R.toroidal) {
-        a = max(0, a);
-        b = min(b, R.max_x - 1);
-        c = max(0, c);
-        e = min(e, R.max_y - 1);
-    }
-    *mi = a; *Mi = b; *mj = c; *Mj = e;
-    return true;
-}
-
-// Reference bag index ((x*dh)+y) with i32 wrapping; -1 outside the matrix.
-__device__ __forceinline__ int64_t bag_index(const Rep& R, int32_t cx, int32_t cy) {
-    int32_t idx = (int32_t)((uint32_t)cx * (uint32_t)R.dh + (uint32_t)cy);
-    if (idx < 0 || (uint32_t)idx >= R.ncells) return -1;
-    return idx;
-}
-
-__device__ __forceinline__ uint32_t id_mix(uint32_t id) {
-    uint32_t z = id * 0x9E3779B1u;
-    z ^= z >> 15;
-    z *= 0x85EBCA77u;
-    z ^= z >> 13;
-    return z;
-}
-
-// Replica owning boid slot i / cell c (tables sorted by offset).
-__device__ __forceinline__ int rep_of_boid(const Rep* reps, int nrep, uint32_t i) {
-    int lo = 0, hi = nrep - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&reps[mid].boid_off) <= i) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-__device__ __forceinline__ int rep_of_cell(const Rep* reps, int nrep, uint32_t c) {
-    int lo = 0, hi = nrep - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&reps[mid].cell_off) <= c) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// ---------------------------------------------------------- force pass
-// One thread per boid of the read buffer: Bird::step (bird.rs:39-154)
-// against the read buffer, next state into the write list at the same slot.
-template <bool STRICT>
-struct Acc {
-    float xa = 0.f, ya = 0.f, xc = 0.f, yc = 0.f, xs = 0.f, ys = 0.f;
-    int count = 0;
-    uint32_t vec = 0;  // candidates including self (the reference's vec.len())
-
-    __device__ __forceinline__ void add(const Rep& R, float sx, float sy, float4 o) {
-        using M = F<STRICT>;
-        float dx = toroidal_distance(sx, o.x, R.w);
-        float dy = toroidal_distance(sy, o.y, R.h);
-        count += 1;
-        float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
-        float q = M::add(M::mul(sq, sq), 1.0f);
-        if (STRICT) {
-            xa = M::add(xa, M::div(dx, q));
-            ya = M::add(ya, M::div(dy, q));
-        } else {
-            float inv = __fdividef(1.0f, q);
-            xa = xa + dx * inv;
-            ya = ya + dy * inv;
-        }
-        xc = M::add(xc, dx);
-        yc = M::add(yc, dy);
-        xs = M::add(xs, o.z);
-        ys = M::add(ys, o.w);
-    }
-};
 
 template <bool STRICT, int QMODE, bool MULTI>
 __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
@@ -225,48 +69,8 @@ __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
         }
     }
 
-    float avx = 0.f, avy = 0.f, cox = 0.f, coy = 0.f, rax = 0.f, ray = 0.f, csx = 0.f, csy = 0.f;
-    if (acc.vec > 0) {
-        float xa = acc.xa, ya = acc.ya, xc = acc.xc, yc = acc.yc, xs = acc.xs, ys = acc.ys;
-        if (acc.count > 0) {
-            const float c = (float)acc.count;
-            xa = M::div(xa, c); ya = M::div(ya, c);
-            xc = M::div(xc, c); yc = M::div(yc, c);
-            xs = M::div(xs, c); ys = M::div(ys, c);
-            csx = M::div(xs, c);  // bird.rs:91-94: a second division by count
-            csy = M::div(ys, c);
-        } else {
-            csx = xs;
-            csy = ys;
-        }
-        avx = M::mul(400.0f, xa);
-        avy = M::mul(400.0f, ya);
-        cox = M::div(-xc, 10.0f);
-        coy = M::div(-yc, 10.0f);
-        const U4 o = philox4x32_10(U4{my_id, (uint32_t)step, (uint32_t)(step >> 32), STREAM_JITTER},
-                                   R.seed_lo, R.seed_hi);
-        const float xr = M::sub(M::mul(unit_f32(o.x), 2.0f), 1.0f);
-        const float yr = M::sub(M::mul(unit_f32(o.y), 2.0f), 1.0f);
-        const float sq = M::sqrt(M::add(M::mul(xr, xr), M::mul(yr, yr)));
-        rax = M::div(M::mul(0.05f, xr), sq);
-        ray = M::div(M::mul(0.05f, yr), sq);
-    }
-    float dx = M::add(M::add(M::add(M::add(M::mul(R.coh, cox), M::mul(R.avo, avx)),
-                                    M::mul(R.con, csx)),
-                             M::mul(R.rnd, rax)),
-                      M::mul(R.mom, me.z));
-    float dy = M::add(M::add(M::add(M::add(M::mul(R.coh, coy), M::mul(R.avo, avy)),
-                                    M::mul(R.con, csy)),
-                             M::mul(R.rnd, ray)),
-                      M::mul(R.mom, me.w));
-    const float dis = M::sqrt(M::add(M::mul(dx, dx), M::mul(dy, dy)));
-    if (dis > 0.0f) {
-        dx = M::mul(M::div(dx, dis), R.jump);
-        dy = M::mul(M::div(dy, dis), R.jump);
-    }
-    const float nx = toroidal_transform(__fadd_rn(me.x, dx), R.w);
-    const float ny = toroidal_transform(__fadd_rn(me.y, dy), R.w);  // bird.rs:147: y wraps with w
-
+    const float4 nxt = finish_bird<STRICT>(R, me, my_id, step, acc);
+    const float nx = nxt.x, ny = nxt.y, dx = nxt.z, dy = nxt.w;
     a.out_st[i] = make_float4(nx, ny, dx, dy);
     a.out_ids[i] = my_id;
     const int32_t ncx = disc(nx, R.d), ncy = disc(ny, R.d);
@@ -284,7 +88,7 @@ __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
                      (ncx >= R.max_x - 1 && ocx <= 1);
     const bool oky = abs(ncy - ocy) <= 1 || (ncy <= 1 && ocy >= R.max_y - 1) ||
                      (ncy >= R.max_y - 1 && ocy <= 1);
-    if (!(okx && oky)) flags |= ERR_REBIN_MISS;
+    if (a.check_moves && !(okx && oky)) flags |= ERR_REBIN_MISS;
     if (flags) atomicOr(a.err, flags);
     const uint32_t key = R.cell_off + (uint32_t)idx;
     a.out_key[i] = key;
@@ -438,32 +242,6 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 }
 
 // ---------------------------------------------------------- rebin
-// Source lines of the bags that can receive boids landing in line X: X-1..X+1
-// and, across the seam, the first two / last two lines.  Ascending, unique.
-__device__ __forceinline__ int source_lines(int X, int maxv, int* out) {
-    int tmp[7];
-    int n = 0;
-    if (X >= maxv - 1) { tmp[n++] = 0; tmp[n++] = 1; }
-    if (X - 1 >= 0) tmp[n++] = X - 1;
-    tmp[n++] = X;
-    if (X + 1 <= maxv) tmp[n++] = X + 1;
-    if (X <= 1) { tmp[n++] = maxv - 1; tmp[n++] = maxv; }
-    // insertion sort + unique, clipped to [0, maxv]
-    for (int a = 1; a < n; ++a) {
-        int v = tmp[a], b = a - 1;
-        while (b >= 0 && tmp[b] > v) { tmp[b + 1] = tmp[b]; --b; }
-        tmp[b + 1] = v;
-    }
-    int m = 0;
-    for (int a = 0; a < n; ++a) {
-        int v = tmp[a];
-        if (v < 0 || v > maxv) continue;
-        if (m > 0 && out[m - 1] == v) continue;
-        out[m++] = v;
-    }
-    return m;
-}
-
 template <bool MULTI>
 __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -476,19 +254,31 @@ __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
     const Rep R = a.reps[r];
     const uint32_t local = c - R.cell_off;
     const int X = (int)(local / (uint32_t)R.dh), Y = (int)(local % (uint32_t)R.dh);
-    int cols[7], rows[7];
-    const int nc = source_lines(X, R.max_x, cols);
-    const int nr = source_lines(Y, R.max_y, rows);
-    for (int ia = 0; ia < nc; ++ia) {
-        const uint32_t colbase = R.cell_off + (uint32_t)cols[ia] * (uint32_t)R.dh;
-        int ib = 0;
-        while (ib < nr) {
-            int jb = ib;  // merge consecutive rows into one contiguous run
-            while (jb + 1 < nr && rows[jb + 1] == rows[jb] + 1) ++jb;
-            const uint32_t s = a.start_cur[colbase + rows[ib]];
-            const uint32_t e = a.start_cur[colbase + rows[jb] + 1];
+    int lastx = -1;
+#pragma unroll 1
+    for (int kx = 0; kx < 7; ++kx) {
+        const int sx = src_line(kx, X, R.max_x);
+        if (sx < 0 || sx > R.max_x || sx <= lastx) continue;
+        lastx = sx;
+        const uint32_t colbase = R.cell_off + (uint32_t)sx * (uint32_t)R.dh;
+        int lasty = -1;
+#pragma unroll 1
+        for (int ky = 0; ky < 7; ++ky) {
+            const int sy = src_line(ky, Y, R.max_y);
+            if (sy < 0 || sy > R.max_y || sy <= lasty) continue;
+            lasty = sy;
+            const uint32_t s = a.start_cur[colbase + sy];
+            const uint32_t e = a.start_cur[colbase + sy + 1];
             for (uint32_t p = s; p < e; ++p) {
-                if (a.key[p] == c) {
+                uint32_t k;
+                if (a.key) {
+                    k = a.key[p];
+                } else {  // key from the record's own position
+                    const float4 r = a.a_st[p];
+                    const int64_t b = bag_index(R, disc(r.x, R.d), disc(r.y, R.d));
+                    k = b >= 0 ? R.cell_off + (uint32_t)b : 0xFFFFFFFFu;
+                }
+                if (k == c) {
                     if (dst < end) {
                         a.s_st[dst] = a.a_st[p];
                         a.s_ids[dst] = a.a_ids[p];
@@ -496,7 +286,6 @@ __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
                     ++dst;
                 }
             }
-            ib = jb + 1;
         }
     }
     if (dst != end) atomicOr(a.err, ERR_REBIN_MISS);

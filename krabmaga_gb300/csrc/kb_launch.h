@@ -43,12 +43,14 @@ struct ForceArgs {
     uint32_t* out_key;
     uint32_t* hist;
     uint32_t* err;
+    int32_t check_moves;  // flag moves the stencil-gather rebin cannot follow
 };
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
 
 // Stencil-gather rebin: builds the canonical read buffer of the next step
 // from the write list (in the previous canonical order) and the scanned
-// histogram.  Bumps *step when step != nullptr.
+// histogram.  Bumps *step when step != nullptr.  With key == nullptr each
+// record's bag is recomputed from its position.
 struct RebinArgs {
     const Rep* reps;
     int32_t nrep;

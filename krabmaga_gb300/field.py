@@ -247,6 +247,17 @@ class Field2D:
                C.c_size_t(len(q)), L.fptr(q), L.uptr(counts), L.uptr(dig))
         return counts[: len(q)], dig[: len(q)]
 
+    def set_step_options(self, fused: bool = True, tile_tx: int = 0, tile_ty: int = 0) -> None:
+        """Persistent fused step on/off and its tile shape (0 = automatic)."""
+        L.call("kb_field_set_step_options", self._h, C.c_int32(1 if fused else 0),
+               C.c_int32(tile_tx), C.c_int32(tile_ty))
+
+    def step_stats(self) -> dict:
+        v = np.zeros(4, np.uint32)
+        L.call("kb_field_step_stats", self._h, L.uptr(v))
+        return {"overflow_tiles": int(v[0]), "tiles": int(v[1]), "ctas": int(v[2]),
+                "tile": (int(v[3]) >> 16, int(v[3]) & 0xFFFF)}
+
     def device_flags(self, clear: bool = False) -> int:
         v = C.c_uint32()
         L.call("kb_field_device_flags", self._h, C.byref(v), C.c_int32(1 if clear else 0))

@@ -103,6 +103,54 @@ def test_compute_plus_lazy_update_equals_fused_steps(gpu):
     assert np.array_equal(ia, ib) and same_bits(sa, sb)
 
 
+@pytest.mark.parametrize("tile", [(0, 0), (1, 1), (4, 4), (16, 8), (64, 128)])
+@pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
+def test_fused_tiles_match_oracle(gpu, tile, kind):
+    # every tile shape gives the oracle's trajectory bit for bit; 64x128-bag
+    # tiles exceed the shared-memory capacity and run the global scratch path
+    n, side = 6000, 490.0
+    ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 21, 1.0)
+    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+    f.set_step_options(True, *tile)
+    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=5, query_mode=kind)
+    step(f, p, 0, 7)
+    step(f, p, 7, 6)
+    o.flock_run(oracle.params_from(p), 0, 13)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+    stats = f.step_stats()
+    assert stats["ctas"] > 0
+    if tile == (64, 128):
+        assert stats["overflow_tiles"] > 0
+
+
+def test_fused_equals_separate_kernels(gpu):
+    ids0, xy0, dxy0 = kg.gen_uniform(50000, 1400.0, 1400.0, 8, 1.0)
+    p = kg.FlockParams(seed=2, arith=kg.KB_ARITH_FAST)
+    out = []
+    for fused in (True, False):
+        f = gpu_field(1400.0, C1_D, ids0, xy0, dxy0)
+        f.set_step_options(fused)
+        step(f, p, 0, 40)
+        out.append(f.get_state())
+    assert np.array_equal(out[0][0], out[1][0]) and same_bits(out[0][1], out[1][1])
+
+
+def test_fused_sweep_radius_two_rings(gpu):
+    # radius 14 with bags of 10/1.5 gives a query ring of two bags
+    ids0, xy0, dxy0 = kg.gen_uniform(3000, 350.0, 350.0, 13, 1.0)
+    p = kg.FlockParams(seed=3, neighbor_radius=14.0, jump=0.9, cohesion=0.6, avoidance=1.4)
+    f = gpu_field(350.0, C1_D, ids0, xy0, dxy0)
+    o = oracle_field(350.0, C1_D, ids0, xy0, dxy0)
+    step(f, p, 0, 20)
+    o.flock_run(oracle.params_from(p), 0, 20)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+
+
 def test_general_rebuild_path_matches_oracle(gpu):
     # A jump longer than a bag (1.2 > d = 1.0) can carry a boid past the
     # neighbouring bag, so every step takes the general stable sort instead of
