@@ -162,6 +162,108 @@ def cpu_reference(wl, steps):
                                     f"schedule (oracle restatement of the reference, 1 core)")
 
 
+def run_sweep(args, dev):
+    """Batched exploration sweep: `sweep_reps` replicas (N log-uniform over
+    [1024, 65536] at density 0.025, per-replica weights/jump/radius, seed =
+    replica index), `sweep_steps` steps as CUDA graphs of 100 launches of one
+    persistent step each, tile shape from the autotuner; against running the
+    plain path replica by replica on the same GPU."""
+    import torch
+
+    import krabmaga_gb300 as kg
+    from krabmaga_gb300 import _lib as L
+
+    reps = kg.sweep_replicas(args.sweep_reps)
+    total = sum(r.n for r in reps)
+    steps = args.sweep_steps
+    b = kg.Batch(reps, device=dev)
+    tx, ty, used, tune_ms = b.autotune(0, 4)
+    step = used
+    b.step(step, 10, 1, 0)
+    step += 10
+    b.synchronize()
+    stream = torch.cuda.ExternalStream(b.cuda_stream(), device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(step, steps, 1, 100)  # one persistent launch per step, 100-launch graphs
+    e1.record(stream)
+    b.synchronize()
+    batched_s = e0.elapsed_time(e1) / 1e3
+    step += steps
+    e0.record(stream)
+    b.step(step, steps, steps, 0)  # all steps in one persistent launch
+    e1.record(stream)
+    b.synchronize()
+    one_launch_s = e0.elapsed_time(e1) / 1e3
+    stats = b.step_stats()
+    b.close()
+    plain_s = 0.0
+    for r in reps:
+        f = kg.Field2D(r.width, r.height, r.discretization, True, device=dev, capacity_hint=r.n)
+        f.set_locations(*r.state)
+        f.lazy_update()
+        pc = r.params.to_c()
+        L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(0), C.c_uint32(2))
+        f.synchronize()
+        fs = torch.cuda.ExternalStream(f.cuda_stream(), device=dev)
+        e0.record(fs)
+        L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(2), C.c_uint32(steps))
+        e1.record(fs)
+        f.synchronize()
+        plain_s += e0.elapsed_time(e1) / 1e3
+        f.close()
+    bv = total * steps / batched_s
+    pv = total * steps / plain_s
+    return {
+        "workload": f"{args.sweep_reps} Flockers replicas, N log-uniform [1024, 65536] "
+                    f"(total {total}), density 0.025, per-replica weights/jump/radius, "
+                    f"{steps} steps",
+        "batched_value": bv, "plain_replica_by_replica_value": pv, "speedup": bv / pv,
+        "one_launch_value": total * steps / one_launch_s, "unit": UNIT,
+        "batched_ms_per_step": 1e3 * batched_s / steps,
+        "launch": "one persistent launch per step, CUDA graphs of 100 launches",
+        "autotuned_tile": [tx, ty], "autotune_ms_per_step": tune_ms, "fused": stats,
+        "data": "synthetic (seeded)", "l2": "working set larger than L2 (no flush)",
+    }
+
+
+def run_serving(args, dev):
+    """Served request stream: Poisson arrivals (`serve_rate` per second for
+    `serve_seconds`), each a Flockers simulation with N log-uniform over
+    [1024, 262144], steps uniform in [100, 1000], per-request weights/jump/
+    radius and seeds; admitted under a 120 GB HBM budget and `serve_slots`
+    slots, merged into batched persistent launches (continuous batching)."""
+    import krabmaga_gb300 as kg
+
+    stream = kg.request_stream(args.serve_rate, args.serve_seconds)
+    srv = kg.Server(max_slots=args.serve_slots, hbm_budget_bytes=120 << 30,
+                    quantum_steps=args.serve_quantum, max_request_boids=262144,
+                    max_request_cells=1 << 20, device=dev)
+    t0 = time.perf_counter()
+    tickets = []
+    for ta, req in stream:
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        tickets.append(srv.submit(req))
+    srv.wait_idle(max(600.0, 10 * args.serve_seconds))
+    st = srv.stats()
+    srv.close()
+    offered = sum(r.nboids * r.steps for _, r in stream) / args.serve_seconds
+    return {
+        "workload": f"Poisson {args.serve_rate:g} req/s for {args.serve_seconds:g} s "
+                    f"({len(stream)} requests), N log-uniform [1024, 262144], steps U[100, 1000]",
+        "requests": len(stream), "completed": st["completed"], "failed": st["failed"],
+        "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "max_latency_s": st["max_s"],
+        "aggregate_value": st["boid_updates"] / st["wall_s"] if st["wall_s"] else None,
+        "offered_boid_updates_per_s": offered, "unit": UNIT,
+        "busy_fraction": st["busy_s"] / st["wall_s"] if st["wall_s"] else None,
+        "launches": st["launches"], "repacks": st["repacks"], "max_active": st["max_active"],
+        "slots": args.serve_slots, "quantum_steps": args.serve_quantum,
+        "latency": "arrival -> final state on the host",
+    }
+
+
 def run_reference(args, wl):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -304,6 +406,9 @@ def run_ours(args, wl):
     achieved = step_bytes / force_s / 1e9
     clocks = clk.summary()
 
+    sweep = run_sweep(args, dev) if (args.sweep_reps > 0 and ws == 1) else None
+    serving = run_serving(args, dev) if (args.serve_seconds > 0 and ws == 1) else None
+
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         cval, sample = cpu_reference(wl, args.cpu_steps)
@@ -333,6 +438,8 @@ def run_ours(args, wl):
                 "call": f"Field2D create + set_locations + lazy_update + {e2e_steps} steps + "
                         f"get_state, host arrays in and out"},
         "gpu_launches": K,
+        "sweep": sweep,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
 
@@ -353,6 +460,12 @@ def main():
     ap.add_argument("--tile", default="0x0", help="fused tile shape TXxTY in bags (0x0: automatic)")
     ap.add_argument("--unfused", action="store_true", help="separate force/scan/rebin kernels")
     ap.add_argument("--profile", action="store_true", help="short plain run for ncu, no timing")
+    ap.add_argument("--sweep-reps", type=int, default=512)
+    ap.add_argument("--sweep-steps", type=int, default=500)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--serve-quantum", type=int, default=50)
     ap.add_argument("--phase-clocks", action="store_true", help="with --profile: per-phase cycles")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]

@@ -170,6 +170,13 @@ kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]);
  * accumulate per-phase cycle counts; out16 (may be NULL) receives the sums
  * over CTAs of the 16 phase counters. */
 kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long* out16);
+/* Tile-shape autotuner (no reference counterpart): runs steps_per_trial + 1
+ * real steps (numbered from first_step) under each candidate shape
+ * (candidates = ncand pairs tx, ty; NULL for the built-in list), keeps the
+ * fastest; best = {tx, ty, steps consumed}, *ms_per_step its time. */
+kb_status kb_field_autotune(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                            uint32_t steps_per_trial, const int32_t* candidates, int32_t ncand,
+                            int32_t best[3], float* ms_per_step);
 /* Read buffer in its stored order (bags ascending, insertion order inside a
  * bag): ids and {x, y, dx, dy} states; either may be NULL. */
 kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n);
@@ -193,6 +200,103 @@ kb_status kb_field_neighbor_lists(kb_field* f, int32_t kind, float dist, size_t 
  * the candidate ids (sum of a 32-bit mix of each id). */
 kb_status kb_field_neighbor_digest(kb_field* f, int32_t kind, float dist, size_t nq,
                                    const float* qxy, uint32_t* counts, uint32_t* digest);
+
+/* ------------------------------------------------------ batched replicas */
+/* Many independent Flockers simulations (the model-exploration workload of
+ * explore_parallel!, src/explore/model_exploration.rs:354-432: one
+ * simulate_explore! per configuration, lines 160-190) packed into one
+ * device field and stepped by one persistent launch per step (or per
+ * steps_per_launch steps), each replica with its own geometry and
+ * parameters. */
+typedef struct kb_batch kb_batch;
+typedef struct {
+    float width;
+    float height;
+    float discretization;
+    int32_t toroidal;
+    uint32_t nboids; /* boids this replica holds */
+    uint32_t _pad;
+    kb_flock_params params; /* query_mode and arith must be equal across a batch */
+} kb_replica_desc;
+
+kb_status kb_batch_create(int32_t device, uint32_t nrep, const kb_replica_desc* reps,
+                          kb_batch** out);
+kb_status kb_batch_destroy(kb_batch* b);
+/* Initial boids of replica r (n == its nboids; positions in its own frame);
+ * the replica's Flocker::init (state.rs:41-56). */
+kb_status kb_batch_set_replica(kb_batch* b, uint32_t r, size_t n, const uint32_t* ids,
+                               const float* xy, const float* dxy);
+/* Pack every replica into the read buffer (the step-0 lazy_update). */
+kb_status kb_batch_commit(kb_batch* b);
+/* nsteps steps of every replica; steps_per_launch persistent steps per kernel
+ * launch (0 = all in one); graph_launches > 1 captures that many launches
+ * into one CUDA graph and replays it. */
+kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps,
+                        uint32_t steps_per_launch, uint32_t graph_launches);
+/* Replica r's read buffer (ids, {x,y,dx,dy}) in its stored order. */
+kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* states, size_t cap,
+                               size_t* n);
+kb_status kb_batch_synchronize(kb_batch* b);
+kb_status kb_batch_cuda_stream(kb_batch* b, void** stream);
+kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty);
+kb_status kb_batch_step_stats(kb_batch* b, uint32_t out4[4]);
+kb_status kb_batch_device_flags(kb_batch* b, uint32_t* flags, int32_t clear);
+/* The tile-shape autotuner of kb_field_autotune for a batch. */
+kb_status kb_batch_autotune(kb_batch* b, uint64_t first_step, uint32_t steps_per_trial,
+                            const int32_t* candidates, int32_t ncand, int32_t best[3],
+                            float* ms_per_step);
+
+/* --------------------------------------------------------------- serving */
+/* A continuous-batching request server (no reference counterpart: the
+ * reference runs one simulate! per process).  Requests are whole Flockers
+ * simulations; admitted ones share batched persistent launches and join or
+ * leave between epochs of at most quantum_steps steps.  Admission needs a
+ * free slot and the request's device state within hbm_budget_bytes. */
+typedef struct kb_server kb_server;
+typedef struct {
+    int32_t device;
+    uint32_t max_slots;         /* requests running at once */
+    uint64_t hbm_budget_bytes;  /* device-state budget for running requests */
+    uint32_t quantum_steps;     /* longest epoch between admissions (0 = 100) */
+    uint32_t max_request_boids; /* largest request (sizes the device pool) */
+    uint32_t max_request_cells; /* largest request bag matrix */
+    int32_t query_mode;         /* shared by all requests */
+    int32_t arith;
+    uint32_t _pad;
+} kb_server_desc;
+typedef struct {
+    uint32_t nboids;      /* ids 0..nboids-1, uniform flock from init_seed */
+    float side;           /* square torus */
+    float discretization;
+    uint32_t steps;
+    kb_flock_params params;
+    uint64_t init_seed;
+    float heading_scale;  /* as kb_gen_uniform */
+    uint32_t _pad;
+} kb_request;
+typedef struct {
+    uint64_t completed, failed, queued, running;
+    double p50_s, p99_s, max_s; /* arrival -> result on the host */
+    double boid_updates;        /* over completed epochs */
+    double wall_s;              /* first arrival -> last completion */
+    double busy_s;              /* time the loop spent in epochs */
+    uint64_t launches, repacks, max_active;
+} kb_server_report;
+
+kb_status kb_server_create(const kb_server_desc* desc, kb_server** out);
+/* Stops the loop (unfinished requests are dropped) and frees everything. */
+kb_status kb_server_destroy(kb_server* s);
+/* Thread-safe; the arrival time is taken here. */
+kb_status kb_server_submit(kb_server* s, const kb_request* r, uint64_t* ticket);
+/* *state: 0 queued, 1 running, 2 done, 3 failed; latency once done. */
+kb_status kb_server_poll(kb_server* s, uint64_t ticket, int32_t* state, double* latency_s);
+/* Final read buffer of a finished request (ids, {x,y,dx,dy}), stored order. */
+kb_status kb_server_result(kb_server* s, uint64_t ticket, uint32_t* ids, float* states, size_t cap,
+                           size_t* n);
+/* Forget a finished request. */
+kb_status kb_server_release(kb_server* s, uint64_t ticket);
+kb_status kb_server_wait_idle(kb_server* s, double timeout_s);
+kb_status kb_server_stats(kb_server* s, kb_server_report* out);
 
 /* ------------------------------------------------------------ workloads */
 

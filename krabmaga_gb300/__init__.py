@@ -7,6 +7,8 @@ reference's API names (Field2D, State, Schedule, simulate, Flocker).
 from . import _lib
 from ._lib import KbError, lib, LIB_PATH, KB_QUERY_RELAX, KB_QUERY_EXACT, KB_ARITH_STRICT, KB_ARITH_FAST
 from .field import Bird, Field2D, Real2D
+from .batch import Batch, Replica, sweep_replicas
+from .serve import Request, Server, request_stream
 from .model import (FlockParams, Flocker, Schedule, State, gen_clustered, gen_uniform, simulate,
                     simulate_old)
 
@@ -14,6 +16,7 @@ __all__ = [
     "Bird", "Field2D", "Real2D", "FlockParams", "Flocker", "Schedule", "State", "simulate",
     "simulate_old", "gen_uniform", "gen_clustered", "KbError", "lib", "LIB_PATH",
     "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
+    "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
 ]
 
 

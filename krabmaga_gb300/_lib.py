@@ -70,6 +70,55 @@ class FlockParamsC(C.Structure):
     ]
 
 
+class ReplicaDesc(C.Structure):
+    _fields_ = [
+        ("width", C.c_float),
+        ("height", C.c_float),
+        ("discretization", C.c_float),
+        ("toroidal", C.c_int32),
+        ("nboids", C.c_uint32),
+        ("_pad", C.c_uint32),
+        ("params", FlockParamsC),
+    ]
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("max_slots", C.c_uint32),
+        ("hbm_budget_bytes", C.c_uint64),
+        ("quantum_steps", C.c_uint32),
+        ("max_request_boids", C.c_uint32),
+        ("max_request_cells", C.c_uint32),
+        ("query_mode", C.c_int32),
+        ("arith", C.c_int32),
+        ("_pad", C.c_uint32),
+    ]
+
+
+class RequestC(C.Structure):
+    _fields_ = [
+        ("nboids", C.c_uint32),
+        ("side", C.c_float),
+        ("discretization", C.c_float),
+        ("steps", C.c_uint32),
+        ("params", FlockParamsC),
+        ("init_seed", C.c_uint64),
+        ("heading_scale", C.c_float),
+        ("_pad", C.c_uint32),
+    ]
+
+
+class ServerReport(C.Structure):
+    _fields_ = [
+        ("completed", C.c_uint64), ("failed", C.c_uint64), ("queued", C.c_uint64),
+        ("running", C.c_uint64), ("p50_s", C.c_double), ("p99_s", C.c_double),
+        ("max_s", C.c_double), ("boid_updates", C.c_double), ("wall_s", C.c_double),
+        ("busy_s", C.c_double), ("launches", C.c_uint64), ("repacks", C.c_uint64),
+        ("max_active", C.c_uint64),
+    ]
+
+
 if not os.path.exists(LIB_PATH):
     raise ImportError(
         f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
@@ -117,6 +166,30 @@ _SIGS = {
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32, C.c_size_t, _SZ]),
     "kb_field_neighbor_digest": (
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
+    "kb_batch_create": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(ReplicaDesc), C.POINTER(_P)]),
+    "kb_batch_destroy": (C.c_int32, [_P]),
+    "kb_batch_set_replica": (C.c_int32, [_P, C.c_uint32, C.c_size_t, _U32, _F, _F]),
+    "kb_batch_commit": (C.c_int32, [_P]),
+    "kb_batch_step": (C.c_int32, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "kb_batch_get_replica": (C.c_int32, [_P, C.c_uint32, _U32, _F, C.c_size_t, _SZ]),
+    "kb_batch_synchronize": (C.c_int32, [_P]),
+    "kb_batch_cuda_stream": (C.c_int32, [_P, C.POINTER(_P)]),
+    "kb_batch_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "kb_batch_step_stats": (C.c_int32, [_P, _U32]),
+    "kb_batch_device_flags": (C.c_int32, [_P, _U32, C.c_int32]),
+    "kb_batch_autotune": (C.c_int32, [_P, C.c_uint64, C.c_uint32, C.POINTER(C.c_int32), C.c_int32,
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "kb_field_autotune": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_uint32,
+                                      C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_float)]),
+    "kb_server_create": (C.c_int32, [C.POINTER(ServerDesc), C.POINTER(_P)]),
+    "kb_server_destroy": (C.c_int32, [_P]),
+    "kb_server_submit": (C.c_int32, [_P, C.POINTER(RequestC), C.POINTER(C.c_uint64)]),
+    "kb_server_poll": (C.c_int32, [_P, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "kb_server_result": (C.c_int32, [_P, C.c_uint64, _U32, _F, C.c_size_t, _SZ]),
+    "kb_server_release": (C.c_int32, [_P, C.c_uint64]),
+    "kb_server_wait_idle": (C.c_int32, [_P, C.c_double]),
+    "kb_server_stats": (C.c_int32, [_P, C.POINTER(ServerReport)]),
     "kb_gen_uniform": (C.c_int32, [C.c_size_t, C.c_float, C.c_float, C.c_uint64, C.c_float,
                                    _U32, _F, _F]),
     "kb_gen_clustered": (C.c_int32, [C.c_size_t, C.c_float, C.c_float, C.c_uint32, C.c_float,

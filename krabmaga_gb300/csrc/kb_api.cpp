@@ -3,6 +3,7 @@
 // replay, and the Field2D query entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -83,6 +84,12 @@ void set_rep_params(Rep* R, const kb_flock_params* p) {
     // whenever (dd+1)*d stays clear of half the side.
     const double reach = ((double)std::max(R->dd, 0) + 1.0) * (double)R->d;
     R->nowrap = (R->toroidal && reach * 1.01 + 1e-3 < 0.5 * (double)std::min(R->w, R->h)) ? 1 : 0;
+    // A move of at most |jump| wraps to line 0 only from x > w - |jump|, i.e.
+    // from lines >= floor((w - |jump|)/d); one line lower covers the f32
+    // rounding of x/d.  A narrow last column can put that two or three lines
+    // below max_x.
+    const double lo = std::floor(((double)R->w - 1.01 * std::fabs((double)p->jump)) / (double)R->d) - 1.0;
+    R->seam = (int32_t)std::max(0.0, std::min(lo, (double)R->max_x));
 }
 
 bool params_ok(const kb_flock_params* p, std::string* why) {
@@ -108,7 +115,8 @@ bool params_ok(const kb_flock_params* p, std::string* why) {
 // it was (or across the seam): a move shorter than a bag, and y wrapped by
 // the same length as x (bird.rs:147 wraps y with the width).
 bool fast_rebin_ok(const Rep& R) {
-    return R.w == R.h && R.max_x == R.max_y && std::fabs(R.jump) * 1.001f < R.d && R.max_x >= 3;
+    return R.w == R.h && R.max_x == R.max_y && std::fabs(R.jump) * 1.001f < R.d && R.max_x >= 4 &&
+           R.seam >= 2 && R.max_x - R.seam <= 4;
 }
 
 }  // namespace kb
@@ -119,7 +127,11 @@ using namespace kb;
 struct kb_field {
     int device = 0;
     cudaStream_t stream = nullptr;
-    Rep rep{};                  // geometry + last parameters
+    Rep rep{};                  // replica 0: the plain field's geometry + last parameters
+    std::vector<Rep> reps;      // every replica (a plain field holds one, == rep)
+    uint32_t ncells_total = 0;  // bags over all replicas
+    uint32_t cells_cap = 0;     // bag arrays are sized for this many bags
+    bool is_batch = false;
     DevBuf<Rep> d_rep;
     // read buffer
     uint32_t cap = 0;
@@ -178,6 +190,9 @@ struct kb_field {
         DevBuf<uint32_t> ctl;  // [0] tile counter, [1..2] barrier, [3] scan epoch, [4] overflow tiles
         DevBuf<unsigned long long> phase_cycles;  // per-CTA phase clocks when profiling
         bool profile = false;
+        bool occ_valid = false;  // cached occupancy of the last configuration
+        FusedCfg occ_cfg{};
+        int occ_strict = -1, occ_qmode = -1, occ_ctas = 0;
     } fused;
     int fused_mode = 1;  // 0 off, 1 on when eligible
     // After fused steps the read buffer can stay virtual: the last write list
@@ -259,8 +274,22 @@ kb_status grow(kb_field* f, uint32_t need) {
 }
 
 kb_status upload_rep(kb_field* f) {
-    KB_CUDA(launch_set_rep(f->d_rep.p, f->rep, f->stream));
+    if (!f->is_batch) {
+        f->reps[0] = f->rep;
+        KB_CUDA(launch_set_rep(f->d_rep.p, f->rep, f->stream));
+    } else {
+        KB_CUDA(cudaMemcpyAsync(f->d_rep.p, f->reps.data(), sizeof(Rep) * f->reps.size(), cudaMemcpyHostToDevice, f->stream));
+        KB_CUDA(cudaStreamSynchronize(f->stream));
+    }
     return KB_OK;
+}
+
+int32_t nrep(const kb_field* f) { return (int32_t)f->reps.size(); }
+
+bool all_fast_rebin_ok(const kb_field* f) {
+    for (const Rep& R : f->reps)
+        if (!fast_rebin_ok(R)) return false;
+    return true;
 }
 
 // Append the host-side pending writes to the device write list.
@@ -322,9 +351,9 @@ kb_status general_rebuild(kb_field* f, bool counted) {
     cudaStream_t s = f->stream;
     const int nxt = 1 - f->cur;
     if (!counted) KB_CUDA(launch_hist_list(f->wkey.p, f->wdead.p, f->wn, f->hist.p, s));
-    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->rep.ncells, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
     KB_CUDA(launch_scatter_list(f->wkey.p, f->wdead.p, f->wst.p, f->wid.p, f->wn, f->start[nxt].p, f->cursor.p, f->tst.p, f->tid.p, f->tsrc.p, s));
-    KB_CUDA(launch_canon(f->start[nxt].p, f->rep.ncells, f->tst.p, f->tid.p, f->tsrc.p, f->cursor.p, f->rst.p, f->rid.p, s));
+    KB_CUDA(launch_canon(f->start[nxt].p, f->ncells_total, f->tst.p, f->tid.p, f->tsrc.p, f->cursor.p, f->rst.p, f->rid.p, s));
     f->cur = nxt;
     return KB_OK;
 }
@@ -332,16 +361,16 @@ kb_status general_rebuild(kb_field* f, bool counted) {
 kb_status fast_rebuild(kb_field* f, bool bump_step) {
     cudaStream_t s = f->stream;
     const int nxt = 1 - f->cur;
-    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->rep.ncells, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
     RebinArgs a;
     a.reps = f->d_rep.p;
-    a.nrep = 1;
+    a.nrep = nrep(f);
     a.start_cur = f->start[f->cur].p;
     a.start_next = f->start[nxt].p;
     a.key = f->wkey.p;
     a.a_st = f->wst.p;
     a.a_ids = f->wid.p;
-    a.ncells = f->rep.ncells;
+    a.ncells = f->ncells_total;
     a.s_st = f->rst.p;
     a.s_ids = f->rid.p;
     a.step = bump_step ? f->dstep.p : nullptr;
@@ -354,7 +383,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
 kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     ForceArgs a;
     a.reps = f->d_rep.p;
-    a.nrep = 1;
+    a.nrep = nrep(f);
     a.st = f->rst.p;
     a.ids = f->rid.p;
     a.start = f->start[f->cur].p;
@@ -365,7 +394,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     a.out_key = f->wkey.p;
     a.hist = f->hist.p;
     a.err = f->err.p;
-    a.check_moves = fast_rebin_ok(f->rep) ? 1 : 0;
+    a.check_moves = all_fast_rebin_ok(f) ? 1 : 0;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
     return KB_OK;
 }
@@ -381,13 +410,13 @@ kb_status materialize(kb_field* f) {
     if (f->a_last == 0) dst = 1;  // the write list sits in rst: gather into wst, then swap roles
     RebinArgs r;
     r.reps = f->d_rep.p;
-    r.nrep = 1;
+    r.nrep = nrep(f);
     r.start_cur = f->start[1 - f->cur].p;
     r.start_next = f->start[f->cur].p;
     r.key = nullptr;
     r.a_st = buf_st(f, f->a_last);
     r.a_ids = buf_ids(f, f->a_last);
-    r.ncells = f->rep.ncells;
+    r.ncells = f->ncells_total;
     r.s_st = buf_st(f, dst);
     r.s_ids = buf_ids(f, dst);
     r.step = nullptr;
@@ -410,7 +439,7 @@ FusedCfg fused_config(const kb_field* f, int dd) {
     c.tx = f->tile_tx > 0 ? f->tile_tx : 16;
     c.ty = f->tile_ty > 0 ? f->tile_ty : 32;
     c.dd = dd;
-    const double rho = (double)f->rn / (double)f->rep.ncells;
+    const double rho = (double)f->rn / (double)f->ncells_total;
     const double staged_cells = (double)(c.tx + 2 * dd + 2) * (c.ty + 2 * dd + 2);
     const double sord_cells = (double)(c.tx + 2 * dd) * (c.ty + 2 * dd);
     auto cap = [](double mean) {
@@ -424,40 +453,73 @@ FusedCfg fused_config(const kb_field* f, int dd) {
 }
 
 bool fused_eligible(const kb_field* f, const kb_flock_params* p) {
-    return f->fused_mode != 0 && f->rep.toroidal && fast_rebin_ok(f->rep) &&
-           f->layout_is_positions && f->rn > 0 && f->rep.dd <= FUSED_DD_MAX &&
-           (p->query_mode == KB_QUERY_RELAX || p->query_mode == KB_QUERY_EXACT);
+    if (f->fused_mode == 0 || !f->layout_is_positions || f->rn == 0) return false;
+    if (p->query_mode != KB_QUERY_RELAX && p->query_mode != KB_QUERY_EXACT) return false;
+    for (const Rep& R : f->reps)
+        if (!R.toroidal || !fast_rebin_ok(R) || R.dd > FUSED_DD_MAX || R.dw > 65535 || R.dh > 65535)
+            return false;
+    return true;
 }
 
 kb_status fused_prepare(kb_field* f, const kb_flock_params* p) {
     auto& F = f->fused;
     const int strict = p->arith == KB_ARITH_STRICT ? 1 : 0;
-    const int dd = std::max(f->rep.dd, 0);
+    int dd = 0;
+    for (const Rep& R : f->reps) dd = std::max(dd, R.dd);
     if (F.ready && F.n == f->rn && F.strict == strict && F.qmode == p->query_mode && F.dd == dd)
         return KB_OK;
     F.ready = false;
     FusedCfg cfg = fused_config(f, dd);
-    int maxc = fused_max_ctas(cfg, strict != 0, p->query_mode, f->device);
+    int maxc = 0;
+    if (F.occ_valid && std::memcmp(&F.occ_cfg, &cfg, sizeof cfg) == 0 && F.occ_strict == strict &&
+        F.occ_qmode == p->query_mode)
+        maxc = F.occ_ctas;
+    else
+        maxc = fused_max_ctas(cfg, strict != 0, p->query_mode, f->device);
     while (maxc <= 0 && (cfg.stage_cap > 256 || cfg.sord_cap > 256)) {
         cfg.stage_cap = std::max(256u, cfg.stage_cap / 2);
         cfg.sord_cap = std::max(256u, cfg.sord_cap / 2);
         maxc = fused_max_ctas(cfg, strict != 0, p->query_mode, f->device);
     }
     if (maxc <= 0) return fail(KB_ERR_CUDA, "fused step: no co-resident CTA fits");
+    F.occ_valid = true;
+    F.occ_cfg = cfg;
+    F.occ_strict = strict;
+    F.occ_qmode = p->query_mode;
+    F.occ_ctas = maxc;
+    // tiles of every replica, largest replicas first (long tiles start early)
+    std::vector<uint32_t> order(f->reps.size());
+    for (uint32_t r = 0; r < order.size(); ++r) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        return f->reps[a].nboids > f->reps[b].nboids;
+    });
     std::vector<Tile> tiles;
-    for (int x = 0; x < f->rep.dw; x += cfg.tx)
-        for (int y = 0; y < f->rep.dh; y += cfg.ty)
-            tiles.push_back(Tile{0u, (uint16_t)x, (uint16_t)y});
-    if (f->rep.dw > 65535 || f->rep.dh > 65535) return fail(KB_ERR_ARG, "bag matrix side above 65535");
-    cudaError_t e = F.tiles.alloc(tiles.size());
-    if (!e) e = F.g_st.alloc(f->rn);
-    if (!e) e = F.g_ids.alloc(f->rn);
-    if (!e) e = F.scan_state.alloc((size_t)maxc);
-    if (!e) e = F.ctl.alloc(8);
+    for (uint32_t r : order) {
+        const Rep& R = f->reps[r];
+        for (int x = 0; x < R.dw; x += cfg.tx)
+            for (int y = 0; y < R.dh; y += cfg.ty) tiles.push_back(Tile{r, (uint16_t)x, (uint16_t)y});
+    }
+    // grow-only scratch (a serving loop re-plans on every repack)
+    cudaError_t e = cudaSuccess;
+    if (F.tiles.n < tiles.size()) e = F.tiles.alloc(std::max<size_t>(tiles.size(), 2 * F.tiles.n));
+    if (!e && F.g_st.n < f->cap) e = F.g_st.alloc(f->cap);
+    if (!e && F.g_ids.n < f->cap) e = F.g_ids.alloc(f->cap);
+    bool fresh_ctl = false;
+    if (!e && F.scan_state.n < (size_t)maxc) {
+        e = F.scan_state.alloc((size_t)maxc);
+        fresh_ctl = true;
+    }
+    if (!e && F.ctl.n < 8) {
+        e = F.ctl.alloc(8);
+        fresh_ctl = true;
+    }
     if (e) return cuda_fail(e, "fused step buffers");
     KB_CUDA(cudaMemcpyAsync(F.tiles.p, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, f->stream));
-    KB_CUDA(cudaMemsetAsync(F.scan_state.p, 0, sizeof(unsigned long long) * maxc, f->stream));
-    KB_CUDA(cudaMemsetAsync(F.ctl.p, 0, sizeof(uint32_t) * 8, f->stream));
+    if (fresh_ctl) {
+        // a new look-back array starts at epoch 0: restart the epoch counter too
+        KB_CUDA(cudaMemsetAsync(F.scan_state.p, 0, sizeof(unsigned long long) * F.scan_state.n, f->stream));
+        KB_CUDA(cudaMemsetAsync(F.ctl.p, 0, sizeof(uint32_t) * 8, f->stream));
+    }
     KB_CUDA(cudaStreamSynchronize(f->stream));
     F.cfg = cfg;
     F.nctas = (uint32_t)maxc;
@@ -481,7 +543,7 @@ kb_status fused_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
     const int cur0 = f->cur;
     int in = 0;
     if (!f->virt) {
-        const size_t sb = sizeof(uint32_t) * ((size_t)f->rep.ncells + 1);
+        const size_t sb = sizeof(uint32_t) * ((size_t)f->ncells_total + 1);
         KB_CUDA(cudaMemcpyAsync(f->start[1 - cur0].p, f->start[cur0].p, sb, cudaMemcpyDeviceToDevice, s));
         in = 0;
     } else {
@@ -490,11 +552,11 @@ kb_status fused_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
     const int o0 = in == 0 ? 1 : 0, o1 = in == 2 ? 1 : 2;  // the two buffers that are not the input
     FusedArgs a{};
     a.reps = f->d_rep.p;
-    a.nrep = 1;
+    a.nrep = nrep(f);
     a.tiles = F.tiles.p;
     a.ntiles = F.ntiles;
     a.cfg = F.cfg;
-    a.ncells = f->rep.ncells;
+    a.ncells = f->ncells_total;
     a.n = f->rn;
     a.a_in_st = buf_st(f, in);
     a.a_in_ids = buf_ids(f, in);
@@ -540,8 +602,7 @@ kb_status field_lazy_update(kb_field* f) {
     // field_2d.rs:905-921: the first swap fixes nagents' density estimate.
     if (!f->density_check) f->density_check = true;
     if (f->w_from_compute && !f->w_has_dead) {
-        Rep R = f->rep;
-        if (fast_rebin_ok(R) && f->layout_is_positions) st = fast_rebuild(f, false);
+        if (all_fast_rebin_ok(f) && f->layout_is_positions) st = fast_rebuild(f, false);
         else st = general_rebuild(f, true);
         if (st) return st;
         f->rn = f->wn;
@@ -550,7 +611,7 @@ kb_status field_lazy_update(kb_field* f) {
         st = general_rebuild(f, false);
         if (st) return st;
         uint32_t total = 0;
-        st = read_u32(f, f->start[f->cur].p + f->rep.ncells, &total);
+        st = read_u32(f, f->start[f->cur].p + f->ncells_total, &total);
         if (st) return st;
         f->rn = total;
     }
@@ -577,50 +638,60 @@ int32_t kb_device_count(void) {
     return n;
 }
 
-kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
-    if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
+}  // extern "C"
+
+namespace {
+
+// Allocate a field over a replica table (cell_off/boid_off already set).
+kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uint32_t capacity,
+                    kb_field** out, uint32_t cells_cap = 0) {
     *out = nullptr;
-    Rep R;
-    std::string why;
-    if (!make_rep_geometry(desc->width, desc->height, desc->discretization, desc->toroidal, &R, &why))
-        return fail(KB_ERR_ARG, why);
     int ndev = kb_device_count();
     if (ndev <= 0) return fail(KB_ERR_NO_DEVICE, "no CUDA device visible");
-    if (desc->device < 0 || desc->device >= ndev) return fail(KB_ERR_ARG, "bad device ordinal");
-    DeviceGuard g(desc->device);
+    if (device < 0 || device >= ndev) return fail(KB_ERR_ARG, "bad device ordinal");
+    uint64_t total = 0;
+    for (const Rep& R : reps) total += R.ncells;
+    if (total == 0 || total > 0xF0000000ull) return fail(KB_ERR_ARG, "bag matrix too large");
+    const uint32_t ncells = (uint32_t)total;
+    const uint32_t nc = std::max(ncells, cells_cap);
+    DeviceGuard g(device);
     kb_field* f = new kb_field();
-    f->device = desc->device;
-    f->rep = R;
+    f->device = device;
+    f->reps = reps;
+    f->rep = reps[0];
+    f->ncells_total = ncells;
+    f->cells_cap = nc;
+    f->is_batch = is_batch;
     cudaError_t e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking);
-    const uint32_t nt = scan_tiles(R.ncells) + 1;
-    if (!e) e = f->d_rep.alloc(1);
-    if (!e) e = f->start[0].alloc((size_t)R.ncells + 1);
-    if (!e) e = f->start[1].alloc((size_t)R.ncells + 1);
-    if (!e) e = f->hist.alloc(R.ncells);
-    if (!e) e = f->cursor.alloc(R.ncells);
+    const uint32_t nt = scan_tiles(nc) + 1;
+    if (!e) e = f->d_rep.alloc(reps.size());
+    if (!e) e = f->start[0].alloc((size_t)nc + 1);
+    if (!e) e = f->start[1].alloc((size_t)nc + 1);
+    if (!e) e = f->hist.alloc(nc);
+    if (!e) e = f->cursor.alloc(nc);
     if (!e) e = f->scan_ctl.alloc(1);
     if (!e) e = f->aux_ctl.alloc(1);
     if (!e) e = f->tstate.alloc(nt);
     if (!e) e = f->err.alloc(1);
     if (!e) e = f->dstep.alloc(1);
     if (!e) e = f->small.alloc(16);
-    if (!e) e = cudaMemsetAsync(f->start[0].p, 0, sizeof(uint32_t) * ((size_t)R.ncells + 1), f->stream);
-    if (!e) e = cudaMemsetAsync(f->start[1].p, 0, sizeof(uint32_t) * ((size_t)R.ncells + 1), f->stream);
-    if (!e) e = cudaMemsetAsync(f->hist.p, 0, sizeof(uint32_t) * R.ncells, f->stream);
-    if (!e) e = cudaMemsetAsync(f->cursor.p, 0, sizeof(uint32_t) * R.ncells, f->stream);
+    if (!e) e = cudaMemsetAsync(f->start[0].p, 0, sizeof(uint32_t) * ((size_t)nc + 1), f->stream);
+    if (!e) e = cudaMemsetAsync(f->start[1].p, 0, sizeof(uint32_t) * ((size_t)nc + 1), f->stream);
+    if (!e) e = cudaMemsetAsync(f->hist.p, 0, sizeof(uint32_t) * nc, f->stream);
+    if (!e) e = cudaMemsetAsync(f->cursor.p, 0, sizeof(uint32_t) * nc, f->stream);
     if (!e) e = cudaMemsetAsync(f->scan_ctl.p, 0, sizeof(ScanCtl), f->stream);
     if (!e) e = cudaMemsetAsync(f->aux_ctl.p, 0, sizeof(ScanCtl), f->stream);
     if (!e) e = cudaMemsetAsync(f->tstate.p, 0, sizeof(unsigned long long) * nt, f->stream);
     if (!e) e = cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream);
     if (!e) e = cudaMemsetAsync(f->dstep.p, 0, sizeof(unsigned long long), f->stream);
-    if (!e) e = launch_set_rep(f->d_rep.p, f->rep, f->stream);
+    if (!e) e = cudaMemcpyAsync(f->d_rep.p, f->reps.data(), sizeof(Rep) * reps.size(), cudaMemcpyHostToDevice, f->stream);
     if (!e) e = cudaStreamSynchronize(f->stream);
     if (e) {
         delete f;
         return cuda_fail(e, "creating field");
     }
-    if (desc->capacity_hint) {
-        kb_status st = grow(f, desc->capacity_hint);
+    if (capacity) {
+        kb_status st = grow(f, capacity);
         if (st) {
             delete f;
             return st;
@@ -628,6 +699,40 @@ kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
     }
     *out = f;
     return KB_OK;
+}
+
+// Replace the replica table of a capacity-sized field (the contents are
+// rebuilt by the caller).
+kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
+    uint64_t total = 0;
+    for (const Rep& R : reps) total += R.ncells;
+    if (total == 0 || total > f->cells_cap) return fail(KB_ERR_ARG, "bag capacity exceeded");
+    if (reps.size() > f->d_rep.n) {
+        cudaError_t e = f->d_rep.alloc(std::max<size_t>(reps.size(), 2 * f->d_rep.n));
+        if (e) return cuda_fail(e, "replica table");
+    }
+    f->reps = reps;
+    f->rep = reps[0];
+    f->ncells_total = (uint32_t)total;
+    f->fused.ready = false;
+    f->drop_graphs();
+    KB_CUDA(cudaMemcpyAsync(f->d_rep.p, f->reps.data(), sizeof(Rep) * reps.size(), cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return KB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
+    if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
+    *out = nullptr;
+    Rep R;
+    std::string why;
+    if (!make_rep_geometry(desc->width, desc->height, desc->discretization, desc->toroidal, &R, &why))
+        return fail(KB_ERR_ARG, why);
+    return field_new(desc->device, std::vector<Rep>{R}, false, desc->capacity_hint, out);
 }
 
 kb_status kb_field_destroy(kb_field* f) {
@@ -1056,6 +1161,33 @@ kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long*
     return KB_OK;
 }
 
+static kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                                uint32_t steps, const int32_t* cand, int32_t ncand,
+                                int32_t* best_out, float* best_ms_out,
+                                kb_status (*run)(void*, uint64_t, uint32_t), void* ctx);
+
+struct FieldTuneCtx {
+    kb_field* f;
+    const kb_flock_params* p;
+};
+static kb_status run_field_steps(void* ctx, uint64_t first, uint32_t n) {
+    FieldTuneCtx* c = (FieldTuneCtx*)ctx;
+    return kb_flock_step(c->f, c->p, first, n);
+}
+
+kb_status kb_field_autotune(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                            uint32_t steps_per_trial, const int32_t* candidates, int32_t ncand,
+                            int32_t best[3], float* ms_per_step) {
+    if (!f || !p || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
+    DeviceGuard g(f->device);
+    set_rep_params(&f->rep, p);
+    f->reps[0] = f->rep;
+    if (!fused_eligible(f, p)) return fail(KB_ERR_STATE, "field not eligible for the fused step");
+    FieldTuneCtx ctx{f, p};
+    return autotune_tiles(f, p, first_step, steps_per_trial, candidates, ncand, best, ms_per_step,
+                          run_field_steps, &ctx);
+}
+
 kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]) {
     if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
@@ -1106,6 +1238,7 @@ static kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t n
 
 kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                         uint32_t nsteps) {
+    if (f && f->is_batch) return fail(KB_ERR_ARG, "a batch field: use kb_batch_step");
     if (!f || !p) return fail(KB_ERR_ARG, "null argument");
     std::string why;
     if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
@@ -1132,7 +1265,7 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         return KB_OK;
     }
     if (f->virt && (st = materialize(f))) return st;
-    const bool use_fast = fast_rebin_ok(f->rep);
+    const bool use_fast = all_fast_rebin_ok(f);
     // CUDA-graph replay of chunks of up to 100 steps (one graph per chunk
     // length and start parity; the graph reads the step number from device
     // memory, so one capture serves every step range).
@@ -1147,7 +1280,7 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         kb_field::GraphKey key;
         key.steps = k;
         key.parity = f->cur;
-        key.params.assign((const uint8_t*)&f->rep, (const uint8_t*)&f->rep + sizeof(Rep));
+        key.params.assign((const uint8_t*)f->reps.data(), (const uint8_t*)f->reps.data() + sizeof(Rep) * f->reps.size());
         key.params.push_back((uint8_t)p->arith);
         key.params.push_back((uint8_t)(f->rn & 0xff));
         key.params.push_back((uint8_t)((f->rn >> 8) & 0xff));
@@ -1177,6 +1310,729 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         f->cur = (k & 1u) ? 1 - cur0 : cur0;
         done += k;
     }
+    return KB_OK;
+}
+
+}  // extern "C"
+
+// ====================================================================== batch
+struct kb_batch {
+    kb_field* f = nullptr;
+    kb_flock_params common{};  // query mode and arithmetic shared by the replicas
+    std::vector<uint8_t> have;  // replica initialised
+    struct GKey {
+        uint32_t launches, spl;
+        int cur, a_last, virt;
+        bool operator<(const GKey& o) const {
+            if (launches != o.launches) return launches < o.launches;
+            if (spl != o.spl) return spl < o.spl;
+            if (cur != o.cur) return cur < o.cur;
+            if (a_last != o.a_last) return a_last < o.a_last;
+            return virt < o.virt;
+        }
+    };
+    struct GVal {
+        cudaGraphExec_t exec;
+        int cur, a_last;
+    };
+    std::map<GKey, GVal> graphs;
+    ~kb_batch() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+        if (f) {
+            cudaStreamSynchronize(f->stream);
+            delete f;
+        }
+    }
+};
+
+extern "C" {
+
+kb_status kb_batch_create(int32_t device, uint32_t nrep, const kb_replica_desc* reps,
+                          kb_batch** out) {
+    if (!reps || !out || nrep == 0) return fail(KB_ERR_ARG, "null argument or no replicas");
+    *out = nullptr;
+    std::vector<Rep> table(nrep);
+    uint64_t cells = 0, boids = 0;
+    std::string why;
+    for (uint32_t r = 0; r < nrep; ++r) {
+        const kb_replica_desc& d = reps[r];
+        if (!make_rep_geometry(d.width, d.height, d.discretization, d.toroidal, &table[r], &why))
+            return fail(KB_ERR_ARG, "replica " + std::to_string(r) + ": " + why);
+        if (!params_ok(&d.params, &why)) return fail(KB_ERR_ARG, "replica " + std::to_string(r) + ": " + why);
+        if (d.params.query_mode != reps[0].params.query_mode || d.params.arith != reps[0].params.arith)
+            return fail(KB_ERR_ARG, "all replicas of a batch share query_mode and arith");
+        set_rep_params(&table[r], &d.params);
+        table[r].cell_off = (uint32_t)cells;
+        table[r].boid_off = (uint32_t)boids;
+        table[r].nboids = d.nboids;
+        cells += table[r].ncells;
+        boids += d.nboids;
+        if (cells > 0xF0000000ull || boids > 0xF0000000ull) return fail(KB_ERR_ARG, "batch too large");
+    }
+    kb_field* f = nullptr;
+    kb_status st = field_new(device, table, true, (uint32_t)boids, &f);
+    if (st) return st;
+    kb_batch* b = new kb_batch();
+    b->f = f;
+    b->common = reps[0].params;
+    b->have.assign(nrep, 0);
+    *out = b;
+    return KB_OK;
+}
+
+kb_status kb_batch_destroy(kb_batch* b) {
+    if (!b) return KB_OK;
+    DeviceGuard g(b->f->device);
+    delete b;
+    return KB_OK;
+}
+
+kb_status kb_batch_set_replica(kb_batch* b, uint32_t r, size_t n, const uint32_t* ids,
+                               const float* xy, const float* dxy) {
+    if (!b || (n && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
+    kb_field* f = b->f;
+    if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
+    if (b->have[r]) return fail(KB_ERR_STATE, "replica already set (create a new batch to reset)");
+    if (n != f->reps[r].nboids) return fail(KB_ERR_ARG, "boid count differs from the replica's nboids");
+    const Rep& R = f->reps[r];
+    const size_t old = f->p_id.size();
+    for (size_t i = 0; i < n; ++i) {
+        if (!(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) && std::isfinite(dxy[2 * i]) &&
+              std::isfinite(dxy[2 * i + 1]))) {
+            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
+            return fail(KB_ERR_ARG, "non-finite position or heading");
+        }
+        const int64_t idx = host_bag_index(R, xy[2 * i], xy[2 * i + 1]);
+        if (idx < 0) {
+            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
+            return fail(KB_ERR_RANGE, "location outside the replica's bag matrix");
+        }
+        f->p_st.push_back(make_float4(xy[2 * i], xy[2 * i + 1], dxy[2 * i], dxy[2 * i + 1]));
+        f->p_id.push_back(ids[i]);
+        f->p_key.push_back(R.cell_off + (uint32_t)idx);
+    }
+    b->have[r] = 1;
+    return KB_OK;
+}
+
+// Build the packed read buffer (every replica must be set).
+kb_status kb_batch_commit(kb_batch* b) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    for (size_t r = 0; r < b->have.size(); ++r)
+        if (!b->have[r]) return fail(KB_ERR_STATE, "replica " + std::to_string(r) + " not set");
+    kb_field* f = b->f;
+    DeviceGuard g(f->device);
+    kb_status st = field_lazy_update(f);
+    if (st) return st;
+    uint64_t expect = 0;
+    for (const Rep& R : f->reps) expect += R.nboids;
+    if (f->rn != expect) return fail(KB_ERR_STATE, "packed boid count mismatch");
+    return upload_rep(f);
+}
+
+// nsteps steps of every replica, each replica with its own parameters.
+// steps_per_launch (0 = all) persistent steps per kernel launch; with
+// graph_launches > 1 that many launches are captured into one CUDA graph
+// and replayed.
+kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint32_t steps_per_launch,
+                        uint32_t graph_launches) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    kb_field* f = b->f;
+    if (f->wn || !f->p_id.empty()) return fail(KB_ERR_STATE, "batch not committed");
+    if (nsteps == 0) return KB_OK;
+    DeviceGuard g(f->device);
+    const kb_flock_params* p = &b->common;
+    kb_status st;
+    KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
+    if (!fused_eligible(f, p)) {
+        if ((st = materialize(f))) return st;
+        if ((st = grow(f, f->rn))) return st;
+        return enqueue_steps(f, p, nsteps, all_fast_rebin_ok(f) && f->layout_is_positions);
+    }
+    if ((st = grow(f, f->rn))) return st;
+    if ((st = fused_prepare(f, p))) return st;
+    const uint32_t spl = steps_per_launch == 0 ? nsteps : std::min(steps_per_launch, nsteps);
+    uint32_t done = 0;
+    while (done < nsteps) {
+        const uint32_t left = nsteps - done;
+        const uint32_t full = left / spl;
+        if (graph_launches > 1 && full >= 2) {
+            const uint32_t L = std::min(graph_launches, full);
+            kb_batch::GKey key{L, spl, f->cur, f->a_last, f->virt ? 1 : 0};
+            auto it = b->graphs.find(key);
+            if (it == b->graphs.end()) {
+                const int cur0 = f->cur, al0 = f->a_last;
+                const bool v0 = f->virt;
+                cudaGraph_t graph = nullptr;
+                KB_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
+                st = KB_OK;
+                for (uint32_t k = 0; k < L && !st; ++k) st = fused_steps(f, p, spl);
+                cudaError_t ce = cudaStreamEndCapture(f->stream, &graph);
+                if (st) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return st;
+                }
+                if (ce) return cuda_fail(ce, "cudaStreamEndCapture");
+                cudaGraphExec_t exec = nullptr;
+                ce = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ce) return cuda_fail(ce, "cudaGraphInstantiate");
+                it = b->graphs.emplace(key, kb_batch::GVal{exec, f->cur, f->a_last}).first;
+                f->cur = cur0;
+                f->a_last = al0;
+                f->virt = v0;
+            }
+            KB_CUDA(cudaGraphLaunch(it->second.exec, f->stream));
+            f->cur = it->second.cur;
+            f->a_last = it->second.a_last;
+            f->virt = true;
+            done += L * spl;
+        } else {
+            const uint32_t k = std::min(spl, left);
+            if ((st = fused_steps(f, p, k))) return st;
+            done += k;
+        }
+    }
+    return KB_OK;
+}
+
+// Time `steps` fused steps under each candidate tile shape (real steps of
+// the simulation, numbered from first_step) and keep the fastest shape.
+static kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                                uint32_t steps, const int32_t* cand, int32_t ncand,
+                                int32_t* best_out, float* best_ms_out,
+                                kb_status (*run)(void*, uint64_t, uint32_t), void* ctx) {
+    static const int32_t defaults[] = {8, 16, 8, 32, 16, 16, 16, 32, 32, 32, 16, 64, 32, 16};
+    if (!cand || ncand <= 0) {
+        cand = defaults;
+        ncand = (int32_t)(sizeof(defaults) / sizeof(defaults[0]) / 2);
+    }
+    cudaEvent_t e0, e1;
+    KB_CUDA(cudaEventCreate(&e0));
+    KB_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_i = -1;
+    uint64_t step = first_step;
+    kb_status st = KB_OK;
+    for (int32_t i = 0; i < ncand && !st; ++i) {
+        f->tile_tx = cand[2 * i];
+        f->tile_ty = cand[2 * i + 1];
+        f->fused.ready = false;
+        if ((st = run(ctx, step, 1))) break;  // prepares the layout, warms up
+        step += 1;
+        if (cudaEventRecord(e0, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        if ((st = run(ctx, step, steps))) break;
+        step += steps;
+        if (cudaEventRecord(e1, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        if (cudaEventSynchronize(e1) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            best_i = i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    f->tile_tx = cand[2 * best_i];
+    f->tile_ty = cand[2 * best_i + 1];
+    f->fused.ready = false;
+    if (best_out) {
+        best_out[0] = f->tile_tx;
+        best_out[1] = f->tile_ty;
+        best_out[2] = (int32_t)(step - first_step);  // steps consumed
+    }
+    if (best_ms_out) *best_ms_out = best / (float)steps;
+    return KB_OK;
+}
+
+static kb_status run_batch_steps(void* ctx, uint64_t first, uint32_t n) {
+    return kb_batch_step((kb_batch*)ctx, first, n, 0, 0);
+}
+
+kb_status kb_batch_autotune(kb_batch* b, uint64_t first_step, uint32_t steps_per_trial,
+                            const int32_t* candidates, int32_t ncand, int32_t best[3],
+                            float* ms_per_step) {
+    if (!b || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
+    DeviceGuard g(b->f->device);
+    if (!fused_eligible(b->f, &b->common)) return fail(KB_ERR_STATE, "batch not eligible for the fused step");
+    return autotune_tiles(b->f, &b->common, first_step, steps_per_trial, candidates, ncand, best,
+                          ms_per_step, run_batch_steps, b);
+}
+
+kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* states, size_t cap,
+                               size_t* n) {
+    if (!b || !n) return fail(KB_ERR_ARG, "null argument");
+    kb_field* f = b->f;
+    if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
+    DeviceGuard g(f->device);
+    kb_status st = materialize(f);
+    if (st) return st;
+    const Rep& R = f->reps[r];
+    uint32_t lo = 0, hi = 0;
+    KB_CUDA(cudaMemcpyAsync(&lo, f->start[f->cur].p + R.cell_off, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaMemcpyAsync(&hi, f->start[f->cur].p + R.cell_off + R.ncells, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    *n = hi - lo;
+    const size_t take = std::min<size_t>(hi - lo, cap);
+    if (take) {
+        if (ids) KB_CUDA(cudaMemcpyAsync(ids, f->rid.p + lo, sizeof(uint32_t) * take, cudaMemcpyDeviceToHost, f->stream));
+        if (states) KB_CUDA(cudaMemcpyAsync(states, f->rst.p + lo, sizeof(float4) * take, cudaMemcpyDeviceToHost, f->stream));
+    }
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return check_flags(f);
+}
+
+kb_status kb_batch_synchronize(kb_batch* b) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    return kb_field_synchronize(b->f);
+}
+
+kb_status kb_batch_cuda_stream(kb_batch* b, void** stream) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    return kb_field_cuda_stream(b->f, stream);
+}
+
+kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    return kb_field_set_step_options(b->f, fused, tile_tx, tile_ty);
+}
+
+kb_status kb_batch_step_stats(kb_batch* b, uint32_t out4[4]) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    return kb_field_step_stats(b->f, out4);
+}
+
+kb_status kb_batch_device_flags(kb_batch* b, uint32_t* flags, int32_t clear) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    return kb_field_device_flags(b->f, flags, clear);
+}
+
+}  // extern "C"
+
+// ====================================================================== serving
+// A continuous-batching request loop.  Requests (each a whole Flockers
+// simulation) are admitted while a slot is free and their device state fits
+// the HBM budget; all admitted requests advance together in one batched
+// field, one persistent launch per epoch.  An epoch runs until the next
+// request finishes, at most `quantum` steps; between epochs finished
+// requests are copied out (their latency ends when the result is on the
+// host) and queued ones join: the batch is repacked on the device (running
+// replicas copied in canonical order, new ones generated in place) and one
+// stable sort rebuilds the bag offsets.  Each request keeps its own step
+// numbering (Rep::origin), so its result equals a run of it alone.
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct SrvReq {
+    uint64_t ticket = 0;
+    kb_request r{};
+    Rep geom{};
+    uint64_t bytes = 0;
+    Clock::time_point t_arrive, t_admit, t_done;
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+    uint32_t remaining = 0;
+    uint32_t boid_off = 0;  // in the current packing
+    bool fresh = true;
+    std::vector<uint32_t> ids;
+    std::vector<float> st;
+    std::string error;
+};
+
+uint64_t request_bytes(const Rep& R, uint32_t n) {
+    // read buffer + two write lists + sort scratch per boid; offsets per bag
+    return (uint64_t)n * (16 + 4) * 6 + (uint64_t)R.ncells * 4 * 4;
+}
+
+}  // namespace
+
+struct kb_server {
+    kb_server_desc desc{};
+    kb_field* f = nullptr;
+    kb_flock_params common{};
+    std::thread loop;
+    std::mutex mu;
+    std::condition_variable cv, cv_done;
+    bool stop = false;
+    std::deque<SrvReq*> queue;
+    std::vector<SrvReq*> active;
+    std::map<uint64_t, SrvReq*> all;
+    uint64_t next_ticket = 1;
+    uint64_t used_bytes = 0;
+    uint64_t global_step = 0;
+    DevBuf<PackEntry> plan;
+    // stats
+    std::vector<double> latencies;
+    double updates = 0.0;
+    uint64_t launches = 0, repacks = 0, max_active = 0, completed = 0, failed = 0;
+    Clock::time_point t_first, t_last;
+    bool any = false;
+    double busy_s = 0.0;
+};
+
+namespace {
+
+kb_status srv_repack(kb_server* S, std::vector<SrvReq*>& act) {
+    kb_field* f = S->f;
+    kb_status st = materialize(f);
+    if (st) return st;
+    std::vector<Rep> reps;
+    std::vector<PackEntry> plan;
+    uint64_t cells = 0, boids = 0;
+    for (SrvReq* q : act) {
+        Rep R = q->geom;
+        R.cell_off = (uint32_t)cells;
+        R.boid_off = (uint32_t)boids;
+        R.nboids = q->r.nboids;
+        if (q->fresh) {
+            R.origin_lo = (uint32_t)S->global_step;
+            R.origin_hi = (uint32_t)(S->global_step >> 32);
+        }
+        PackEntry e{};
+        e.dst_off = (uint32_t)boids;
+        e.n = q->r.nboids;
+        e.rep = (uint32_t)reps.size();
+        e.src_off = q->boid_off;
+        e.kind = q->fresh ? 1u : 0u;
+        e.seed_lo = (uint32_t)q->r.init_seed;
+        e.seed_hi = (uint32_t)(q->r.init_seed >> 32);
+        e.heading_scale = q->r.heading_scale;
+        plan.push_back(e);
+        q->geom = R;
+        q->boid_off = (uint32_t)boids;
+        cells += R.ncells;
+        boids += q->r.nboids;
+        reps.push_back(R);
+    }
+    if (boids > f->cap) return fail(KB_ERR_OOM, "server boid capacity exceeded");
+    if (plan.size() > S->plan.n) {
+        cudaError_t e = S->plan.alloc(std::max<size_t>(plan.size(), 2 * S->plan.n + 16));
+        if (e) return cuda_fail(e, "repack plan");
+    }
+    KB_CUDA(cudaMemcpyAsync(S->plan.p, plan.data(), sizeof(PackEntry) * plan.size(), cudaMemcpyHostToDevice, f->stream));
+    // the old read buffer (rst) is the copy source; the write list the target
+    if ((st = field_set_reps(f, reps))) return st;  // synchronises the stream (plan copied)
+    KB_CUDA(launch_repack(S->plan.p, (int32_t)plan.size(), (uint32_t)boids, f->d_rep.p, f->rst.p, f->rid.p,
+                          f->wst.p, f->wid.p, f->wkey.p, f->wdead.p, f->err.p, f->stream));
+    f->wn = (uint32_t)boids;
+    f->w_from_compute = false;
+    f->w_has_dead = false;
+    f->virt = false;
+    if ((st = general_rebuild(f, false))) return st;
+    f->rn = (uint32_t)boids;
+    f->wn = 0;
+    f->layout_is_positions = true;
+    for (SrvReq* q : act) q->fresh = false;
+    S->repacks++;
+    return KB_OK;
+}
+
+void srv_fail_all(kb_server* S, std::vector<SrvReq*>& act, const std::string& why) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (SrvReq* q : act) {
+        q->state = 3;
+        q->error = why;
+        q->t_done = Clock::now();
+        S->used_bytes -= q->bytes;
+        S->failed++;
+    }
+    act.clear();
+    S->cv_done.notify_all();
+}
+
+void srv_loop(kb_server* S) {
+    cudaSetDevice(S->desc.device);
+    kb_field* f = S->f;
+    std::vector<SrvReq*> act;
+    bool changed = false;
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            while (!S->stop && S->queue.empty() && act.empty()) S->cv.wait(lk);
+            if (S->stop) break;
+            while (!S->queue.empty() && act.size() < S->desc.max_slots &&
+                   S->used_bytes + S->queue.front()->bytes <= S->desc.hbm_budget_bytes) {
+                SrvReq* q = S->queue.front();
+                S->queue.pop_front();
+                q->state = 1;
+                q->t_admit = Clock::now();
+                q->fresh = true;
+                S->used_bytes += q->bytes;
+                act.push_back(q);
+                changed = true;
+            }
+            S->active = act;
+            S->max_active = std::max<uint64_t>(S->max_active, act.size());
+        }
+        if (act.empty()) continue;
+        const auto t0 = Clock::now();
+        kb_status st = KB_OK;
+        if (changed) st = srv_repack(S, act);
+        changed = false;
+        uint32_t K = S->desc.quantum_steps ? S->desc.quantum_steps : 100;
+        for (SrvReq* q : act) K = std::min(K, q->remaining);
+        if (!st) {
+            st = launch_set_u64(f->dstep.p, S->global_step, f->stream) ? fail(KB_ERR_CUDA, "step") : KB_OK;
+        }
+        if (!st && K > 0) {
+            if (fused_eligible(f, &S->common)) {
+                if (!(st = fused_prepare(f, &S->common))) st = fused_steps(f, &S->common, K);
+            } else {
+                if (!(st = materialize(f))) st = enqueue_steps(f, &S->common, K, all_fast_rebin_ok(f));
+            }
+            S->launches++;
+        }
+        if (st) {
+            srv_fail_all(S, act, g_last_error);
+            changed = true;
+            continue;
+        }
+        S->global_step += K;
+        double upd = 0.0;
+        for (SrvReq* q : act) {
+            q->remaining -= K;
+            upd += (double)q->r.nboids * K;
+        }
+        // copy out the finished requests
+        bool any_done = false;
+        for (SrvReq* q : act) any_done |= (q->remaining == 0);
+        if (any_done) {
+            if (!(st = materialize(f))) {
+                std::vector<uint32_t> lohi(2 * act.size());
+                for (size_t i = 0; i < act.size(); ++i) {
+                    if (act[i]->remaining) continue;
+                    const Rep& R = act[i]->geom;
+                    cudaMemcpyAsync(&lohi[2 * i], f->start[f->cur].p + R.cell_off, 4, cudaMemcpyDeviceToHost, f->stream);
+                    cudaMemcpyAsync(&lohi[2 * i + 1], f->start[f->cur].p + R.cell_off + R.ncells, 4, cudaMemcpyDeviceToHost, f->stream);
+                }
+                if (cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
+                for (size_t i = 0; i < act.size() && !st; ++i) {
+                    SrvReq* q = act[i];
+                    if (q->remaining) continue;
+                    const uint32_t lo = lohi[2 * i], n = lohi[2 * i + 1] - lohi[2 * i];
+                    q->ids.resize(n);
+                    q->st.resize((size_t)n * 4);
+                    if (n) {
+                        cudaMemcpyAsync(q->ids.data(), f->rid.p + lo, 4ull * n, cudaMemcpyDeviceToHost, f->stream);
+                        cudaMemcpyAsync(q->st.data(), f->rst.p + lo, 16ull * n, cudaMemcpyDeviceToHost, f->stream);
+                    }
+                }
+                if (!st && cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
+                uint32_t flags = 0;
+                if (!st) {
+                    cudaMemcpy(&flags, f->err.p, 4, cudaMemcpyDeviceToHost);
+                    if (flags) st = fail(KB_ERR_DEVICE_FLAG, "device error word set during serving");
+                }
+            }
+            if (st) {
+                srv_fail_all(S, act, g_last_error);
+                changed = true;
+                continue;
+            }
+        }
+        const auto t1 = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->busy_s += std::chrono::duration<double>(t1 - t0).count();
+            S->updates += upd;
+            std::vector<SrvReq*> keep;
+            for (SrvReq* q : act) {
+                if (q->remaining == 0) {
+                    q->state = 2;
+                    q->t_done = t1;
+                    S->used_bytes -= q->bytes;
+                    S->latencies.push_back(std::chrono::duration<double>(q->t_done - q->t_arrive).count());
+                    S->completed++;
+                    S->t_last = t1;
+                    changed = true;
+                } else {
+                    keep.push_back(q);
+                }
+            }
+            act.swap(keep);
+            S->active = act;
+            if (changed) S->cv_done.notify_all();
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+kb_status kb_server_create(const kb_server_desc* desc, kb_server** out) {
+    if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
+    if (desc->max_slots == 0 || desc->max_request_boids == 0)
+        return fail(KB_ERR_ARG, "max_slots and max_request_boids must be positive");
+    *out = nullptr;
+    kb_flock_params p{};
+    p.query_mode = desc->query_mode;
+    p.arith = desc->arith;
+    p.jump = 0.5f;
+    p.neighbor_radius = 1.0f;
+    std::string why;
+    if (!params_ok(&p, &why)) return fail(KB_ERR_ARG, why);
+    const uint64_t cap = (uint64_t)desc->max_slots * desc->max_request_boids;
+    const uint64_t cells = (uint64_t)desc->max_slots * desc->max_request_cells;
+    if (cap > 0xF0000000ull || cells > 0xF0000000ull) return fail(KB_ERR_ARG, "capacity too large");
+    Rep R;
+    if (!make_rep_geometry(16.0f, 16.0f, 4.0f, 1, &R, &why)) return fail(KB_ERR_ARG, why);
+    kb_field* f = nullptr;
+    kb_status st = field_new(desc->device, std::vector<Rep>{R}, true, (uint32_t)cap, &f,
+                             (uint32_t)std::max<uint64_t>(cells, R.ncells));
+    if (st) return st;
+    kb_server* S = new kb_server();
+    S->desc = *desc;
+    S->f = f;
+    S->common = p;
+    S->loop = std::thread(srv_loop, S);
+    *out = S;
+    return KB_OK;
+}
+
+kb_status kb_server_destroy(kb_server* S) {
+    if (!S) return KB_OK;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->cv.notify_all();
+    if (S->loop.joinable()) S->loop.join();
+    {
+        DeviceGuard g(S->f->device);
+        cudaStreamSynchronize(S->f->stream);
+        delete S->f;
+    }
+    for (auto& kv : S->all) delete kv.second;
+    delete S;
+    return KB_OK;
+}
+
+kb_status kb_server_submit(kb_server* S, const kb_request* r, uint64_t* ticket) {
+    if (!S || !r || !ticket) return fail(KB_ERR_ARG, "null argument");
+    std::string why;
+    if (!params_ok(&r->params, &why)) return fail(KB_ERR_ARG, why);
+    if (r->params.query_mode != S->desc.query_mode || r->params.arith != S->desc.arith)
+        return fail(KB_ERR_ARG, "request query_mode/arith differ from the server's");
+    if (r->nboids == 0 || r->nboids > S->desc.max_request_boids || r->steps == 0)
+        return fail(KB_ERR_ARG, "request size out of range");
+    SrvReq* q = new SrvReq();
+    q->r = *r;
+    if (!make_rep_geometry(r->side, r->side, r->discretization, 1, &q->geom, &why)) {
+        delete q;
+        return fail(KB_ERR_ARG, why);
+    }
+    if (q->geom.ncells > S->desc.max_request_cells) {
+        delete q;
+        return fail(KB_ERR_ARG, "request bag matrix above max_request_cells");
+    }
+    set_rep_params(&q->geom, &r->params);
+    q->bytes = request_bytes(q->geom, r->nboids);
+    if (q->bytes > S->desc.hbm_budget_bytes) {
+        delete q;
+        return fail(KB_ERR_BUSY, "request larger than the whole HBM budget");
+    }
+    q->remaining = r->steps;
+    q->t_arrive = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        q->ticket = S->next_ticket++;
+        S->all[q->ticket] = q;
+        S->queue.push_back(q);
+        if (!S->any) {
+            S->any = true;
+            S->t_first = q->t_arrive;
+        }
+    }
+    S->cv.notify_all();
+    *ticket = q->ticket;
+    return KB_OK;
+}
+
+kb_status kb_server_poll(kb_server* S, uint64_t ticket, int32_t* state, double* latency_s) {
+    if (!S || !state) return fail(KB_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) return fail(KB_ERR_ARG, "unknown ticket");
+    *state = it->second->state;
+    if (latency_s)
+        *latency_s = it->second->state >= 2
+                         ? std::chrono::duration<double>(it->second->t_done - it->second->t_arrive).count()
+                         : 0.0;
+    if (it->second->state == 3) return fail(KB_ERR_STATE, it->second->error);
+    return KB_OK;
+}
+
+kb_status kb_server_result(kb_server* S, uint64_t ticket, uint32_t* ids, float* states, size_t cap,
+                           size_t* n) {
+    if (!S || !n) return fail(KB_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) return fail(KB_ERR_ARG, "unknown ticket");
+    SrvReq* q = it->second;
+    if (q->state != 2) return fail(KB_ERR_STATE, q->state == 3 ? q->error : "request not finished");
+    *n = q->ids.size();
+    const size_t take = std::min(cap, q->ids.size());
+    if (ids && take) std::memcpy(ids, q->ids.data(), 4 * take);
+    if (states && take) std::memcpy(states, q->st.data(), 16 * take);
+    return KB_OK;
+}
+
+kb_status kb_server_release(kb_server* S, uint64_t ticket) {
+    if (!S) return fail(KB_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) return fail(KB_ERR_ARG, "unknown ticket");
+    if (it->second->state < 2) return fail(KB_ERR_STATE, "request still queued or running");
+    delete it->second;
+    S->all.erase(it);
+    return KB_OK;
+}
+
+kb_status kb_server_wait_idle(kb_server* S, double timeout_s) {
+    if (!S) return fail(KB_ERR_ARG, "null argument");
+    std::unique_lock<std::mutex> lk(S->mu);
+    const auto until = Clock::now() + std::chrono::duration<double>(timeout_s);
+    while (!(S->queue.empty() && S->active.empty())) {
+        if (S->cv_done.wait_until(lk, until) == std::cv_status::timeout &&
+            !(S->queue.empty() && S->active.empty()))
+            return fail(KB_ERR_TIMEOUT, "requests still pending");
+    }
+    return KB_OK;
+}
+
+kb_status kb_server_stats(kb_server* S, kb_server_report* out) {
+    if (!S || !out) return fail(KB_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    std::vector<double> v = S->latencies;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double p) {
+        if (v.empty()) return 0.0;
+        const size_t i = (size_t)std::min<double>(v.size() - 1, std::ceil(p * v.size()) - 1);
+        return v[i];
+    };
+    std::memset(out, 0, sizeof(*out));
+    out->completed = S->completed;
+    out->failed = S->failed;
+    out->queued = S->queue.size();
+    out->running = S->active.size();
+    out->p50_s = pct(0.50);
+    out->p99_s = pct(0.99);
+    out->max_s = v.empty() ? 0.0 : v.back();
+    out->boid_updates = S->updates;
+    out->wall_s = S->any && S->completed ? std::chrono::duration<double>(S->t_last - S->t_first).count() : 0.0;
+    out->busy_s = S->busy_s;
+    out->launches = S->launches;
+    out->repacks = S->repacks;
+    out->max_active = S->max_active;
     return KB_OK;
 }
 

@@ -19,6 +19,12 @@ enum : uint32_t {
     ERR_REBIN_MISS = 0x2u,
     ERR_SPIN_TIMEOUT = 0x4u,
     ERR_NONFINITE = 0x8u,
+    // which check raised a rebin miss (set together with ERR_REBIN_MISS)
+    ERR_MISS_GATHER = 0x10u,   // a bag gathered a different count than its offsets say
+    ERR_MISS_OUTSIDE = 0x20u,  // a boid sits outside the bag its slot belongs to
+    ERR_MISS_MOVE = 0x40u,     // a boid moved further than the neighbouring bag
+    ERR_MISS_TILE = 0x80u,     // a tile was refused (ring wider than the layout)
+    ERR_MISS_MATERIALIZE = 0x100u,  // the standalone rebin found a different count
 };
 
 // One simulation on the device: its Field2D geometry (field_2d.rs:304-322),
@@ -40,6 +46,8 @@ struct Rep {
     int32_t qmode;          // 0 relax, 1 exact
     uint32_t seed_lo, seed_hi;
     int32_t nowrap;         // 1: no candidate pair can straddle the seam ((dd+1)*d < min(w,h)/2)
+    uint32_t origin_lo, origin_hi;  // global step at which this replica's step 0 ran
+    int32_t seam;           // first line from which a one-step move can wrap to line 0
 };
 
 // ------------------------------------------------------------------ Philox

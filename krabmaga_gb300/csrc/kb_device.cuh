@@ -170,20 +170,22 @@ struct Acc {
     }
 };
 
-// k-th candidate source line of line X (where a bag can receive boids from in one step): the
-// low seam lines, X-1..X+1, the high seam lines.  -1 when absent.  For
-// maxv >= 3 the sequence is non-decreasing, so skipping values <= the last
-// one taken yields the ascending unique set.
-__device__ __forceinline__ int src_line(int k, int X, int maxv) {
-    switch (k) {
-        case 0: return X >= maxv - 1 ? 0 : -1;
-        case 1: return X >= maxv - 1 ? 1 : -1;
-        case 2: return X - 1;
-        case 3: return X;
-        case 4: return X + 1;
-        case 5: return X <= 1 ? maxv - 1 : -1;
-        default: return X <= 1 ? maxv : -1;
-    }
+// k-th candidate source line of line X (k = 0..7): the lines a bag of line X
+// can receive boids from in one step.  X >= seam receives from line 0 (moves
+// wrapping past x = w), line 0 from every line >= seam (moves wrapping below
+// x = 0), every line from X-1..X+1.  -1 when absent.  With seam >= 2 the
+// sequence is non-decreasing, so skipping values <= the last taken (and
+// outside 0..maxv) yields the ascending unique set.
+__device__ __forceinline__ int src_line(int k, int X, int maxv, int seam) {
+    if (k == 0) return X >= seam ? 0 : -1;
+    if (k <= 3) return X + (k - 2);
+    return X == 0 ? seam + (k - 4) : -1;
+}
+constexpr int SRC_LINES = 8;
+
+// The one-step move check of the stencil rebin (see src_line).
+__device__ __forceinline__ bool move_ok(int o, int n, int seam) {
+    return abs(n - o) <= 1 || (n == 0 && o >= seam) || (o == 0 && n >= seam);
 }
 
 // bird.rs:84-149: averages, avoidance/cohesion/consistency, Philox jitter
@@ -211,7 +213,10 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
         avy = M::mul(400.0f, ya);
         cox = M::div(-xc, 10.0f);
         coy = M::div(-yc, 10.0f);
-        const U4 o = philox4x32_10(U4{my_id, (uint32_t)step, (uint32_t)(step >> 32), STREAM_JITTER},
+        // the replica's own step number keys the jitter stream
+        const unsigned long long ls =
+            step - (((unsigned long long)R.origin_hi << 32) | (unsigned long long)R.origin_lo);
+        const U4 o = philox4x32_10(U4{my_id, (uint32_t)ls, (uint32_t)(ls >> 32), STREAM_JITTER},
                                    R.seed_lo, R.seed_hi);
         const float xr = M::sub(M::mul(unit_f32(o.x), 2.0f), 1.0f);
         const float yr = M::sub(M::mul(unit_f32(o.y), 2.0f), 1.0f);

@@ -31,9 +31,11 @@ struct TileCtx {
     int32_t X0, X1, Y0, Y1;          // owned bags [X0,X1) x [Y0,Y1)
     int32_t qx0, qx1, qy0, qy1;      // canonical-order region (inclusive)
     int32_t nqx, nqy;
-    int32_t sxlo, nsxm, nsxe, nsx;   // staged columns: [sxlo, sxlo+nsxm) + extras
-    int32_t sylo, nsym, nsye, nsy;   // staged rows
-    int32_t sxe[4], sye[4];
+    // staged lines: up to three disjoint ascending runs of line values
+    // [lo, hi] (the low seam line 0, the main run, the high seam run), run r
+    // starting at staged index off[r]
+    int32_t xlo[3], xhi[3], xoff[3], nxr, nsx;
+    int32_t ylo[3], yhi[3], yoff[3], nyr, nsy;
     int32_t hx0, hy0, hnx, hny;      // shared histogram region
     uint32_t nseg, staged, sord, owned;
     int32_t overflow;
@@ -78,36 +80,54 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 
 // ------------------------------------------------------------ small helpers
-__device__ __forceinline__ int line_index(int v, int lo, int nm, const int32_t* e, int ne) {
-    if (v >= lo && v < lo + nm) return v - lo;
-    for (int k = 0; k < ne; ++k)
-        if (e[k] == v) return nm + k;
+// Staged index of line value v (-1 if not staged) / value of staged index i.
+__device__ __forceinline__ int run_index(int v, const int32_t* lo, const int32_t* hi,
+                                         const int32_t* off, int nr) {
+    for (int r = 0; r < nr; ++r)
+        if (v >= lo[r] && v <= hi[r]) return off[r] + (v - lo[r]);
     return -1;
 }
-__device__ __forceinline__ int line_value(int i, int lo, int nm, const int32_t* e) {
-    return i < nm ? lo + i : e[i - nm];
+__device__ __forceinline__ int run_value(int i, const int32_t* lo, const int32_t* hi,
+                                         const int32_t* off, int nr, int* run) {
+    int r = 0;
+    while (r + 1 < nr && i >= off[r + 1]) ++r;
+    *run = r;
+    return lo[r] + (i - off[r]);
 }
 
-// Staged lines for a canonical region [q0, q1] of lines 0..maxv: the main
-// run [q0-1, q1+1] clipped, plus the seam lines the region can receive from.
-__device__ void staged_lines(int q0, int q1, int maxv, int32_t* lo, int32_t* nm, int32_t* e,
-                             int32_t* ne) {
-    const int a = max(q0 - 1, 0), b = min(q1 + 1, maxv);
-    *lo = a;
-    *nm = b - a + 1;
-    int n = 0;
-    int cand[4];
-    int nc = 0;
-    if (q1 >= maxv - 1) { cand[nc++] = 0; cand[nc++] = 1; }
-    if (q0 <= 1) { cand[nc++] = maxv - 1; cand[nc++] = maxv; }
-    for (int k = 0; k < nc; ++k) {
-        const int v = cand[k];
-        if (v < 0 || v > maxv || (v >= a && v <= b)) continue;
-        bool dup = false;
-        for (int m = 0; m < n; ++m) dup |= (e[m] == v);
-        if (!dup) e[n++] = v;
+// Staged lines for a canonical region [q0, q1] of lines 0..maxv: the rebin
+// sources of every line in it (see src_line): the main run [q0-1, q1+1]
+// clipped, line 0 when the region reaches the seam line, and the high run
+// [seam, maxv] when the region holds line 0.  Disjoint ascending runs.
+__device__ void staged_lines(int q0, int q1, int maxv, int seam, int32_t* lo, int32_t* hi,
+                             int32_t* off, int32_t* nr, int32_t* n) {
+    int a[3], b[3], k = 0;
+    if (q1 >= seam) { a[k] = 0; b[k] = 0; ++k; }
+    a[k] = max(q0 - 1, 0); b[k] = min(q1 + 1, maxv); ++k;
+    if (q0 == 0) { a[k] = seam; b[k] = maxv; ++k; }
+    // sort by start (at most three), then merge overlapping or adjacent runs
+    for (int i = 1; i < k; ++i)
+        for (int j = i; j > 0 && a[j] < a[j - 1]; --j) {
+            int t = a[j]; a[j] = a[j - 1]; a[j - 1] = t;
+            t = b[j]; b[j] = b[j - 1]; b[j - 1] = t;
+        }
+    int m = 0;
+    for (int i = 0; i < k; ++i) {
+        if (m > 0 && a[i] <= hi[m - 1] + 1) {
+            hi[m - 1] = max(hi[m - 1], b[i]);
+        } else {
+            lo[m] = a[i];
+            hi[m] = b[i];
+            ++m;
+        }
     }
-    *ne = n;
+    int o = 0;
+    for (int r = 0; r < m; ++r) {
+        off[r] = o;
+        o += hi[r] - lo[r] + 1;
+    }
+    *nr = m;
+    *n = o;
 }
 
 __device__ __forceinline__ uint32_t ldcg_u32(const uint32_t* p) { return __ldcg(p); }
@@ -332,7 +352,7 @@ __device__ __forceinline__ void gather_bag_smem(const FusedArgs& a, const Rep& R
             }
         }
     }
-    if (m != expected) atomicOr(a.err, ERR_REBIN_MISS);
+    if (m != expected) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_GATHER);
 }
 
 // Global form (tiles over capacity): read the previous write list through L2.
@@ -347,14 +367,14 @@ __device__ __forceinline__ void gather_bag_global(const FusedArgs& a, const Rep&
     uint32_t m = 0;
     int lastx = -1;
 #pragma unroll 1
-    for (int kx = 0; kx < 7; ++kx) {
-        const int sx = src_line(kx, Xq, R.max_x);
+    for (int kx = 0; kx < SRC_LINES; ++kx) {
+        const int sx = src_line(kx, Xq, R.max_x, R.seam);
         if (sx < 0 || sx > R.max_x || sx <= lastx) continue;
         lastx = sx;
         int lasty = -1;
 #pragma unroll 1
-        for (int ky = 0; ky < 7; ++ky) {
-            const int sy = src_line(ky, Yq, R.max_y);
+        for (int ky = 0; ky < SRC_LINES; ++ky) {
+            const int sy = src_line(ky, Yq, R.max_y, R.seam);
             if (sy < 0 || sy > R.max_y || sy <= lasty) continue;
             lasty = sy;
             const uint32_t cell = R.cell_off + (uint32_t)sx * (uint32_t)R.dh + (uint32_t)sy;
@@ -372,7 +392,7 @@ __device__ __forceinline__ void gather_bag_global(const FusedArgs& a, const Rep&
             }
         }
     }
-    if (m != expected) atomicOr(a.err, ERR_REBIN_MISS);
+    if (m != expected) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_GATHER);
 }
 
 // Source lists of the tile's canonical lines (thread t < nqx: column qx0+t;
@@ -381,25 +401,27 @@ __device__ __forceinline__ void build_sources(const Rep& R, const TileCtx& c, co
     if (t < c.nqx) {
         const int X = c.qx0 + t;
         int n = 0, last = -1;
-        for (int k = 0; k < 7; ++k) {
-            const int v = src_line(k, X, R.max_x);
+        for (int k = 0; k < SRC_LINES; ++k) {
+            const int v = src_line(k, X, R.max_x, R.seam);
             if (v < 0 || v > R.max_x || v <= last) continue;
             last = v;
-            const int i = line_index(v, c.sxlo, c.nsxm, c.sxe, c.nsxe);
+            const int i = run_index(v, c.xlo, c.xhi, c.xoff, c.nxr);
             if (i >= 0 && n < 8) S.srcx[t * 8 + n++] = (uint8_t)i;
         }
         S.nsrcx[t] = (uint8_t)n;
     } else if (t < c.nqx + c.nqy) {
         const int jq = t - c.nqx, Y = c.qy0 + jq;
-        int n = 0, last = -1;
-        for (int k = 0; k < 7; ++k) {
-            const int v = src_line(k, Y, R.max_y);
+        int n = 0, last = -1, last_run = -1;
+        for (int k = 0; k < SRC_LINES; ++k) {
+            const int v = src_line(k, Y, R.max_y, R.seam);
             if (v < 0 || v > R.max_y || v <= last) continue;
-            const int j = line_index(v, c.sylo, c.nsym, c.sye, c.nsye);
+            const int j = run_index(v, c.ylo, c.yhi, c.yoff, c.nyr);
             if (j < 0) continue;
-            // extend the previous run when both rows sit in the main run
-            if (n > 0 && last == v - 1 && j < c.nsym && S.srcy[(jq * 4 + n - 1) * 2 + 1] == j - 1 &&
-                S.srcy[(jq * 4 + n - 1) * 2 + 1] < c.nsym) {
+            int run = 0;
+            while (run + 1 < c.nyr && j >= c.yoff[run + 1]) ++run;
+            // extend the previous run of rows when contiguous in the staging
+            if (n > 0 && last == v - 1 && run == last_run &&
+                S.srcy[(jq * 4 + n - 1) * 2 + 1] == j - 1) {
                 S.srcy[(jq * 4 + n - 1) * 2 + 1] = (uint8_t)j;
             } else if (n < 4) {
                 S.srcy[(jq * 4 + n) * 2] = (uint8_t)j;
@@ -407,6 +429,7 @@ __device__ __forceinline__ void build_sources(const Rep& R, const TileCtx& c, co
                 ++n;
             }
             last = v;
+            last_run = run;
         }
         S.nsrcy[jq] = (uint8_t)n;
     }
@@ -442,7 +465,7 @@ __device__ __forceinline__ void force_boid(const FusedArgs& a, const Rep& R, con
     if (R.dd >= 0) {
         int cx = disc(me.x, R.d), cy = disc(me.y, R.d);
         if (cx < c.X0 || cx >= c.X1 || cy < c.Y0 || cy >= c.Y1) {
-            atomicOr(a.err, ERR_REBIN_MISS);  // a boid outside its own bag
+            atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_OUTSIDE);  // a boid outside its own bag
             cx = min(max(cx, c.X0), c.X1 - 1);
             cy = min(max(cy, c.Y0), c.Y1 - 1);
         }
@@ -495,11 +518,8 @@ __device__ __forceinline__ void force_boid(const FusedArgs& a, const Rep& R, con
     }
     if (!isfinite(nxt.x) || !isfinite(nxt.y)) flags |= ERR_NONFINITE;
     const int32_t ocx = disc(me.x, R.d), ocy = disc(me.y, R.d);
-    const bool okx = abs(ncx - ocx) <= 1 || (ncx <= 1 && ocx >= R.max_x - 1) ||
-                     (ncx >= R.max_x - 1 && ocx <= 1);
-    const bool oky = abs(ncy - ocy) <= 1 || (ncy <= 1 && ocy >= R.max_y - 1) ||
-                     (ncy >= R.max_y - 1 && ocy <= 1);
-    if (!(okx && oky)) flags |= ERR_REBIN_MISS;
+    const bool okx = move_ok(ocx, ncx, R.seam), oky = move_ok(ocy, ncy, R.seam);
+    if (!(okx && oky)) flags |= ERR_REBIN_MISS | ERR_MISS_MOVE;
     if (flags) atomicOr(a.err, flags);
     const int hx = ncx - c.hx0, hy = ncy - c.hy0;
     if (idx >= 0 && hx >= 0 && hx < c.hnx && hy >= 0 && hy < c.hny && flags == 0)
@@ -529,18 +549,16 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
         c.qy1 = min(c.Y1 - 1 + dd, R.dh - 1);
         c.nqx = c.qx1 - c.qx0 + 1;
         c.nqy = c.qy1 - c.qy0 + 1;
-        staged_lines(c.qx0, c.qx1, R.max_x, &c.sxlo, &c.nsxm, c.sxe, &c.nsxe);
-        staged_lines(c.qy0, c.qy1, R.max_y, &c.sylo, &c.nsym, c.sye, &c.nsye);
-        c.nsx = c.nsxm + c.nsxe;
-        c.nsy = c.nsym + c.nsye;
-        c.nseg = (uint32_t)(c.nsx * (1 + c.nsye));
+        staged_lines(c.qx0, c.qx1, R.max_x, R.seam, c.xlo, c.xhi, c.xoff, &c.nxr, &c.nsx);
+        staged_lines(c.qy0, c.qy1, R.max_y, R.seam, c.ylo, c.yhi, c.yoff, &c.nyr, &c.nsy);
+        c.nseg = (uint32_t)(c.nsx * c.nyr);
         c.hx0 = max(c.X0 - 1, 0);
         c.hy0 = max(c.Y0 - 1, 0);
         c.hnx = min(c.X1 + 1, R.dw) - c.hx0;
         c.hny = min(c.Y1 + 1, R.dh) - c.hy0;
         // a ring wider than the layout was sized for: refuse the tile
         c.overflow = (dd > a.cfg.dd || c.X0 >= c.X1 || c.Y0 >= c.Y1) ? 2 : 0;
-        if (c.overflow) atomicOr(a.err, ERR_REBIN_MISS);
+        if (c.overflow) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_TILE);
     }
     __syncthreads();
     pc.mark(0);
@@ -553,10 +571,10 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
             const uint32_t k = k0 + lane;
             uint32_t glo = 0, cnt = 0;
             if (k < c.nseg) {
-                const int i = (int)(k / (uint32_t)(1 + c.nsye)), r = (int)(k % (uint32_t)(1 + c.nsye));
-                const int vx = line_value(i, c.sxlo, c.nsxm, c.sxe);
-                const int ra = r == 0 ? c.sylo : c.sye[r - 1];
-                const int rb = r == 0 ? c.sylo + c.nsym - 1 : c.sye[r - 1];
+                const int i = (int)(k / (uint32_t)c.nyr), r = (int)(k % (uint32_t)c.nyr);
+                int xr;
+                const int vx = run_value(i, c.xlo, c.xhi, c.xoff, c.nxr, &xr);
+                const int ra = c.ylo[r], rb = c.yhi[r];
                 const uint32_t cb = R.cell_off + (uint32_t)vx * (uint32_t)R.dh;
                 glo = ldcg_u32(B.start_prev + cb + ra);
                 cnt = ldcg_u32(B.start_prev + cb + rb + 1) - glo;
@@ -653,10 +671,10 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
         }
         for (int t = tid; t < c.nsx * c.nsy; t += FT) {
             const int i = t / c.nsy, j = t % c.nsy;
-            const int vx = line_value(i, c.sxlo, c.nsxm, c.sxe);
-            const int vy = line_value(j, c.sylo, c.nsym, c.sye);
-            const int r = j < c.nsym ? 0 : 1 + (j - c.nsym);
-            const Seg g = S.seg[i * (1 + c.nsye) + r];
+            int xr, r;
+            const int vx = run_value(i, c.xlo, c.xhi, c.xoff, c.nxr, &xr);
+            const int vy = run_value(j, c.ylo, c.yhi, c.yoff, c.nyr, &r);
+            const Seg g = S.seg[i * c.nyr + r];
             const uint32_t cell = R.cell_off + (uint32_t)vx * (uint32_t)R.dh + (uint32_t)vy;
             const uint32_t s0 = ldcg_u32(B.start_prev + cell), s1 = ldcg_u32(B.start_prev + cell + 1);
             S.cell_lo[t] = g.soff + (s0 - g.glo);

@@ -55,9 +55,9 @@ KB_HD FusedLayout fused_layout(const FusedCfg& c) {
     FusedLayout L;
     L.maxqx = c.tx + 2 * c.dd;
     L.maxqy = c.ty + 2 * c.dd;
-    L.maxlx = L.maxqx + 2 + 4;  // rebin ring + seam lines
-    L.maxly = L.maxqy + 2 + 4;
-    L.maxseg = L.maxlx * 5;     // per staged column: the main run + up to 4 seam rows
+    L.maxlx = L.maxqx + 2 + 6;  // rebin ring + seam lines (line 0, up to 5 high lines)
+    L.maxly = L.maxqy + 2 + 6;
+    L.maxseg = L.maxlx * 3;     // per staged column: up to three row runs
     L.maxhx = c.tx + 2;
     L.maxhy = c.ty + 2;
     uint32_t o = 0;

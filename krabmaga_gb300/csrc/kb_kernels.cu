@@ -84,11 +84,8 @@ __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
     // the rebin gathers a bag's arrivals from the 3x3 old bags around it
     // (plus the seam columns/rows); anything else must take the general sort
     const int32_t ocx = disc(me.x, R.d), ocy = disc(me.y, R.d);
-    const bool okx = abs(ncx - ocx) <= 1 || (ncx <= 1 && ocx >= R.max_x - 1) ||
-                     (ncx >= R.max_x - 1 && ocx <= 1);
-    const bool oky = abs(ncy - ocy) <= 1 || (ncy <= 1 && ocy >= R.max_y - 1) ||
-                     (ncy >= R.max_y - 1 && ocy <= 1);
-    if (a.check_moves && !(okx && oky)) flags |= ERR_REBIN_MISS;
+    const bool okx = move_ok(ocx, ncx, R.seam), oky = move_ok(ocy, ncy, R.seam);
+    if (a.check_moves && !(okx && oky)) flags |= ERR_REBIN_MISS | ERR_MISS_MOVE;
     if (flags) atomicOr(a.err, flags);
     const uint32_t key = R.cell_off + (uint32_t)idx;
     a.out_key[i] = key;
@@ -256,15 +253,15 @@ __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
     const int X = (int)(local / (uint32_t)R.dh), Y = (int)(local % (uint32_t)R.dh);
     int lastx = -1;
 #pragma unroll 1
-    for (int kx = 0; kx < 7; ++kx) {
-        const int sx = src_line(kx, X, R.max_x);
+    for (int kx = 0; kx < SRC_LINES; ++kx) {
+        const int sx = src_line(kx, X, R.max_x, R.seam);
         if (sx < 0 || sx > R.max_x || sx <= lastx) continue;
         lastx = sx;
         const uint32_t colbase = R.cell_off + (uint32_t)sx * (uint32_t)R.dh;
         int lasty = -1;
 #pragma unroll 1
-        for (int ky = 0; ky < 7; ++ky) {
-            const int sy = src_line(ky, Y, R.max_y);
+        for (int ky = 0; ky < SRC_LINES; ++ky) {
+            const int sy = src_line(ky, Y, R.max_y, R.seam);
             if (sy < 0 || sy > R.max_y || sy <= lasty) continue;
             lasty = sy;
             const uint32_t s = a.start_cur[colbase + sy];
@@ -288,7 +285,7 @@ __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
             }
         }
     }
-    if (dst != end) atomicOr(a.err, ERR_REBIN_MISS);
+    if (dst != end) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_MATERIALIZE);
 }
 
 // ---------------------------------------------------------- general sort
@@ -466,6 +463,66 @@ __global__ void k_cell_xy(Rep R, const uint32_t* cell_of, uint32_t n, float2* ou
     out[k] = make_float2(__fmul_rn((float)i, R.d), __fmul_rn((float)j, R.d));
 }
 
+// Initial uniform flock of one boid: kb_gen_uniform (kb_gen.cpp) with every
+// operation rounded once, so host and device draw the same bits.
+__device__ void gen_uniform_boid(uint32_t id, uint32_t seed_lo, uint32_t seed_hi, float w, float h,
+                                 float scale, float4* out) {
+    U4 o = philox4x32_10(U4{id, 0u, 0u, STREAM_INIT}, seed_lo, seed_hi);
+    const float x = __fmul_rn(w, unit_f32(o.x));
+    const float y = __fmul_rn(h, unit_f32(o.y));
+    uint32_t z = o.z, ww = o.w;
+    float hx = 0.f, hy = 0.f;
+    for (uint32_t attempt = 1; attempt < 1000u; ++attempt) {
+        const float a = __fsub_rn(__fmul_rn(unit_f32(z), 2.0f), 1.0f);
+        const float b = __fsub_rn(__fmul_rn(unit_f32(ww), 2.0f), 1.0f);
+        const float r2 = __fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b));
+        if (r2 > 0.0f && r2 <= 1.0f) {
+            const float r = __fsqrt_rn(r2);
+            hx = __fdiv_rn(a, r);
+            hy = __fdiv_rn(b, r);
+            break;
+        }
+        o = philox4x32_10(U4{id, attempt, 0u, STREAM_INIT}, seed_lo, seed_hi);
+        z = o.z;
+        ww = o.w;
+    }
+    *out = make_float4(x, y, __fmul_rn(hx, scale), __fmul_rn(hy, scale));
+}
+
+__global__ void k_repack(const PackEntry* __restrict__ plan, int32_t nplan, uint32_t total,
+                         const Rep* __restrict__ reps, const float4* __restrict__ src_st,
+                         const uint32_t* __restrict__ src_ids, float4* __restrict__ dst_st,
+                         uint32_t* __restrict__ dst_ids, uint32_t* __restrict__ dst_key,
+                         uint8_t* __restrict__ dst_dead, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int lo = 0, hi = nplan - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (plan[mid].dst_off <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const PackEntry e = plan[lo];
+    const uint32_t k = i - e.dst_off;
+    if (k >= e.n) return;
+    const Rep R = reps[e.rep];
+    float4 st;
+    uint32_t id;
+    if (e.kind == 0) {
+        st = src_st[e.src_off + k];
+        id = src_ids[e.src_off + k];
+    } else {
+        id = k;
+        gen_uniform_boid(k, e.seed_lo, e.seed_hi, R.w, R.h, e.heading_scale, &st);
+    }
+    const int64_t b = bag_index(R, disc(st.x, R.d), disc(st.y, R.d));
+    if (b < 0) atomicOr(err, ERR_KEY_RANGE);
+    dst_st[i] = st;
+    dst_ids[i] = id;
+    dst_key[i] = R.cell_off + (uint32_t)(b < 0 ? 0 : b);
+    dst_dead[i] = 0;
+}
+
 __global__ void k_set_rep(Rep* dst, Rep v) { *dst = v; }
 __global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
 __global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst += v; }
@@ -473,6 +530,16 @@ __global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst 
 inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
 }  // namespace
+
+cudaError_t launch_repack(const PackEntry* plan, int32_t nplan, uint32_t total, const Rep* reps,
+                          const float4* src_st, const uint32_t* src_ids, float4* dst_st,
+                          uint32_t* dst_ids, uint32_t* dst_key, uint8_t* dst_dead, uint32_t* err,
+                          cudaStream_t s) {
+    if (total == 0 || nplan <= 0) return cudaSuccess;
+    k_repack<<<grid_for(total, 256), 256, 0, s>>>(plan, nplan, total, reps, src_st, src_ids, dst_st,
+                                                   dst_ids, dst_key, dst_dead, err);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_set_rep(Rep* dst, const Rep& v, cudaStream_t s) {
     k_set_rep<<<1, 1, 0, s>>>(dst, v);

@@ -119,4 +119,18 @@ cudaError_t launch_cell_of(const uint32_t* start, uint32_t ncells, uint32_t* cel
 cudaError_t launch_cell_xy(const Rep& rep, const uint32_t* cell_of, uint32_t n, float2* out,
                            cudaStream_t s);
 
+// Repacking plan for a continuous batch: each entry fills write-list slots
+// [dst_off, dst_off+n) for replica `rep`, either copying its canonical
+// records from the read buffer (kind 0, from src_off) or generating its
+// initial uniform flock (kind 1: kb_gen_uniform's draws, bit for bit).
+struct PackEntry {
+    uint32_t dst_off, n, rep, src_off;
+    uint32_t kind, seed_lo, seed_hi;
+    float heading_scale;
+};
+cudaError_t launch_repack(const PackEntry* plan, int32_t nplan, uint32_t total, const Rep* reps,
+                          const float4* src_st, const uint32_t* src_ids, float4* dst_st,
+                          uint32_t* dst_ids, uint32_t* dst_key, uint8_t* dst_dead, uint32_t* err,
+                          cudaStream_t s);
+
 }  // namespace kb

@@ -252,6 +252,21 @@ class Field2D:
         L.call("kb_field_set_step_options", self._h, C.c_int32(1 if fused else 0),
                C.c_int32(tile_tx), C.c_int32(tile_ty))
 
+    def autotune(self, params, first_step: int, steps_per_trial: int = 5, candidates=None):
+        """Pick the fastest fused tile shape by timing real steps; returns
+        (tx, ty, steps consumed, ms per step)."""
+        cand = None
+        nc = 0
+        if candidates:
+            flat = [v for pair in candidates for v in pair]
+            cand = (C.c_int32 * len(flat))(*flat)
+            nc = len(candidates)
+        best = (C.c_int32 * 3)()
+        ms = C.c_float()
+        L.call("kb_field_autotune", self._h, C.byref(params.to_c()), C.c_uint64(first_step),
+               C.c_uint32(steps_per_trial), cand, C.c_int32(nc), best, C.byref(ms))
+        return int(best[0]), int(best[1]), int(best[2]), float(ms.value)
+
     def step_stats(self) -> dict:
         v = np.zeros(4, np.uint32)
         L.call("kb_field_step_stats", self._h, L.uptr(v))

@@ -1,0 +1,89 @@
+"""Batched replicas on the GPU: every replica of a packed batch equals the
+oracle run of that replica alone, bit for bit (strict arithmetic), whatever
+the launch grouping; and a batch equals plain single-field runs."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import krabmaga_gb300 as kg
+import oracle
+from krabmaga_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+
+def same_bits(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def small_sweep(arith, qmode=kg.KB_QUERY_RELAX):
+    reps = kg.sweep_replicas(7, n_min=300, n_max=5000, arith=arith, query_mode=qmode, table_seed=5)
+    # one replica with a two-bag query ring (bags of radius / 2.5)
+    r = reps[3]
+    r.discretization = float(np.float32(r.params.neighbor_radius) / np.float32(2.5))
+    return reps
+
+
+def oracle_run(rep, nsteps):
+    o = oracle.OracleField(rep.width, rep.height, rep.discretization, True)
+    o.set_many(*rep.state)
+    o.lazy_update()
+    o.flock_run(oracle.params_from(rep.params), 0, nsteps)
+    ids, st, _ = o.iter(1)
+    return ids, st
+
+
+@pytest.mark.parametrize("grouping", [(0, 0), (1, 0), (1, 4), (3, 2)])
+def test_batch_replicas_match_oracle(gpu, grouping):
+    spl, graphs = grouping
+    reps = small_sweep(kg.KB_ARITH_STRICT)
+    b = kg.Batch(reps)
+    b.step(0, 12, spl, graphs)
+    b.step(12, 9, spl, graphs)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 21)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
+def test_batch_exact_query_matches_oracle(gpu):
+    reps = small_sweep(kg.KB_ARITH_STRICT, kg.KB_QUERY_EXACT)[:4]
+    b = kg.Batch(reps)
+    b.step(0, 10, 1, 5)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 10)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
+def test_batch_equals_plain_fields(gpu):
+    reps = small_sweep(kg.KB_ARITH_FAST)
+    b = kg.Batch(reps)
+    b.step(0, 30, 1, 10)
+    for i, rep in enumerate(reps):
+        f = kg.Field2D(rep.width, rep.height, rep.discretization, True)
+        f.set_locations(*rep.state)
+        f.lazy_update()
+        L.call("kb_flock_step", f.handle, C.byref(rep.params.to_c()), C.c_uint64(0), C.c_uint32(30))
+        fi, fs = f.get_state()
+        bi, bs = b.get_replica(i)
+        assert np.array_equal(fi, bi) and same_bits(fs, bs), f"replica {i}"
+
+
+def test_batch_unfused_path_matches(gpu):
+    reps = small_sweep(kg.KB_ARITH_STRICT)[:3]
+    b = kg.Batch(reps)
+    b.set_step_options(False)
+    b.step(0, 8)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 8)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
+def test_batch_rejects_mixed_modes(gpu):
+    reps = small_sweep(kg.KB_ARITH_FAST)[:2]
+    reps[1].params.arith = kg.KB_ARITH_STRICT
+    with pytest.raises(kg.KbError):
+        kg.Batch(reps)

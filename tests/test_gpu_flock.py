@@ -151,6 +151,31 @@ def test_fused_sweep_radius_two_rings(gpu):
     assert np.array_equal(ids, oids) and same_bits(st, ost)
 
 
+@pytest.mark.parametrize("side,d,jump,radius", [
+    (284.82, 2.005, 0.795, 5.012),   # last column 0.12 wide: wraps from three lines in
+    (200.0, C1_D, 0.7, 10.0),        # side/d an exact integer: the x = w line exists
+    (101.3, 4.99, 0.98, 12.0),       # ring of two bags, last column 1.5 wide
+    (60.05, 6.0, 0.6, 6.5),          # small field, last column 0.05 wide
+])
+def test_seam_geometries_match_oracle(gpu, side, d, jump, radius):
+    n = int(side * side * 0.03)
+    ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 17, 1.0)
+    # crowd a band along each seam so wrapping moves happen every step
+    xy0[: n // 4, 0] = np.float32(side) - (xy0[: n // 4, 0] % np.float32(1.5))
+    xy0[n // 4: n // 2, 1] = xy0[n // 4: n // 2, 1] % np.float32(1.5)
+    p = kg.FlockParams(seed=4, jump=jump, neighbor_radius=radius)
+    for fused in (True, False):
+        f = gpu_field(side, d, ids0, xy0, dxy0)
+        f.set_step_options(fused)
+        o = oracle_field(side, d, ids0, xy0, dxy0)
+        step(f, p, 0, 15)
+        o.flock_run(oracle.params_from(p), 0, 15)
+        ids, st = f.get_state()
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"fused={fused}"
+        assert f.device_flags() == 0
+
+
 def test_general_rebuild_path_matches_oracle(gpu):
     # A jump longer than a bag (1.2 > d = 1.0) can carry a boid past the
     # neighbouring bag, so every step takes the general stable sort instead of

@@ -1,0 +1,117 @@
+"""The continuous-batching server on the GPU: every request's result equals
+the same simulation run alone on a plain field (bit for bit), whether it ran
+alone, joined a running batch, or waited for a slot."""
+import ctypes as C
+import time
+
+import numpy as np
+import pytest
+
+import krabmaga_gb300 as kg
+from krabmaga_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+
+def same_bits(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def alone(req: kg.Request):
+    f = kg.Field2D(req.side, req.side, req.discretization, True, capacity_hint=req.nboids)
+    f.set_locations(*kg.gen_uniform(req.nboids, req.side, req.side, req.init_seed,
+                                    req.heading_scale))
+    f.lazy_update()
+    L.call("kb_flock_step", f.handle, C.byref(req.params.to_c()), C.c_uint64(0),
+           C.c_uint32(req.steps))
+    return f.get_state()
+
+
+def small_stream(arith, n=10):
+    rs = kg.request_stream(400.0, 1.0, n_min=500, n_max=6000, steps_min=20, steps_max=90,
+                           arith=arith, seed=3)[:n]
+    return [r for _, r in rs]
+
+
+@pytest.mark.parametrize("arith", [kg.KB_ARITH_STRICT, kg.KB_ARITH_FAST])
+def test_results_equal_alone_and_in_the_mix(gpu, arith):
+    reqs = small_stream(arith)
+    srv = kg.Server(max_slots=4, quantum_steps=16, max_request_boids=8000, arith=arith)
+    tickets = []
+    for i, r in enumerate(reqs):
+        tickets.append(srv.submit(r))
+        if i % 3 == 2:
+            time.sleep(0.002)  # some arrive while others run
+    srv.wait_idle(120.0)
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["max_active"] >= 2 and st["repacks"] >= 2
+    for t, r in zip(tickets, reqs):
+        state, lat = srv.poll(t)
+        assert state == 2 and lat > 0
+        ids, s = srv.result(t, r.nboids)
+        ai, a_s = alone(r)
+        assert np.array_equal(ids, ai) and same_bits(s, a_s), f"request {t}"
+        srv.release(t)
+    srv.close()
+
+
+def test_single_slot_serialises_but_finishes(gpu):
+    reqs = small_stream(kg.KB_ARITH_FAST, 4)
+    srv = kg.Server(max_slots=1, quantum_steps=8, max_request_boids=8000)
+    ts = [srv.submit(r) for r in reqs]
+    srv.wait_idle(60.0)
+    assert srv.stats()["max_active"] == 1
+    for t, r in zip(ts, reqs):
+        ids, s = srv.result(t, r.nboids)
+        ai, a_s = alone(r)
+        assert np.array_equal(ids, ai) and same_bits(s, a_s)
+    srv.close()
+
+
+def test_budget_admits_what_fits(gpu):
+    # six requests of one size; a budget for two of them at a time
+    base = small_stream(kg.KB_ARITH_FAST, 6)
+    n, side, d = 3000, float(np.float32(np.sqrt(3000 / 0.025))), 5.0
+    reqs = [kg.Request(n, side, d, 30, r.params, r.init_seed) for r in base]
+    ncells = (int(np.ceil(np.float32(side) / np.float32(d))) + 1) ** 2
+    one = n * 20 * 6 + ncells * 16  # the server's per-request device-state estimate
+    srv = kg.Server(max_slots=8, quantum_steps=8, max_request_boids=8000,
+                    hbm_budget_bytes=2 * one + 100)
+    ts = [srv.submit(r) for r in reqs]
+    srv.wait_idle(60.0)
+    st = srv.stats()
+    assert st["completed"] == 6 and st["max_active"] == 2
+    for t, r in zip(ts, reqs):
+        ids, s = srv.result(t, r.nboids)
+        ai, a_s = alone(r)
+        assert np.array_equal(ids, ai) and same_bits(s, a_s)
+    srv.close()
+
+
+def test_oversized_and_mismatched_requests_are_refused(gpu):
+    srv = kg.Server(max_slots=2, max_request_boids=1000, arith=kg.KB_ARITH_FAST)
+    r = small_stream(kg.KB_ARITH_FAST, 1)[0]
+    r.nboids = 5000
+    with pytest.raises(kg.KbError):
+        srv.submit(r)
+    r.nboids = 500
+    r.params.arith = kg.KB_ARITH_STRICT
+    with pytest.raises(kg.KbError):
+        srv.submit(r)
+    srv.close()
+
+
+def test_device_generator_matches_host_generator(gpu):
+    # the server draws each request's initial flock on the device; with zero
+    # steps run... a one-step request alone vs served already covers it, but
+    # check the draws directly through a 1-step strict run of a lone boid set
+    r = small_stream(kg.KB_ARITH_STRICT, 1)[0]
+    r.steps = 1
+    srv = kg.Server(max_slots=1, max_request_boids=8000, arith=kg.KB_ARITH_STRICT)
+    t = srv.submit(r)
+    srv.wait_idle(30.0)
+    ids, s = srv.result(t, r.nboids)
+    ai, a_s = alone(r)
+    assert np.array_equal(ids, ai) and same_bits(s, a_s)
+    srv.close()
