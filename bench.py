@@ -177,6 +177,7 @@ def run_sweep(args, dev):
     total = sum(r.n for r in reps)
     steps = args.sweep_steps
     b = kg.Batch(reps, device=dev)
+    b.set_step_options(args.mode)
     tx, ty, used, tune_ms = b.autotune(0, 4)
     step = used
     b.step(step, 10, 1, 0)
@@ -200,6 +201,7 @@ def run_sweep(args, dev):
     plain_s = 0.0
     for r in reps:
         f = kg.Field2D(r.width, r.height, r.discretization, True, device=dev, capacity_hint=r.n)
+        f.set_step_options(args.mode)
         f.set_locations(*r.state)
         f.lazy_update()
         pc = r.params.to_c()
@@ -301,7 +303,7 @@ def run_ours(args, wl):
 
     f = kg.Field2D(side, side, D_C, True, device=dev, capacity_hint=n)
     tx, ty = (int(v) for v in args.tile.split("x"))
-    f.set_step_options(not args.unfused, tx, ty)
+    f.set_step_options(args.mode, tx, ty)
     f.set_locations(ids, xy, dxy)
     f.lazy_update()
     stream = torch.cuda.ExternalStream(f.cuda_stream(), device=dev)
@@ -311,6 +313,11 @@ def run_ours(args, wl):
         L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(t), C.c_uint32(1))
 
     step_no = 0
+    tuned = None
+    if args.mode in (1, 2) and args.tile == "0x0" and not args.profile:
+        # the autotuner's trials are real steps of this simulation (warm-up)
+        tuned = f.autotune(params, step_no, 4)
+        step_no += tuned[2]
     for _ in range(args.warmup):
         one_step(step_no)
         step_no += 1
@@ -328,7 +335,8 @@ def run_ours(args, wl):
             L.call("kb_field_phase_clocks", f.handle, C.c_int32(0), clk)
             names = ["tile_setup", "segments_offsets", "serial_prefix", "stage_wait", "keys",
                      "gather", "force", "hist_flush", "tile_fetch", "barrier1", "scan", "barrier2"]
-            ctas = out["stats"]["ctas"]
+            ctas = out["stats"]["ctas"] if args.mode == 1 else 1
+            # mode 1: per CTA (persistent); mode 2: summed over all tile CTAs
             out["phase_us_per_step"] = {nm: clk[i] / ctas / args.steps / 2070.0
                                         for i, nm in enumerate(names)}
         print(json.dumps(out))
@@ -423,13 +431,16 @@ def run_ours(args, wl):
                    "parallelism": f"replicas{ws}", "arith": args.arith, "query": "relax",
                    "l2": "flushed (512 MiB write) before every timed step",
                    "warm_l2_value": warm_value},
-        "roofline": {"bound": "hbm", "kernel": "k_fused (whole step, one launch)",
+        "roofline": {"bound": "hbm",
+                     "kernel": {2: "k_tile_step + k_scan (two launches per step)",
+                                1: "k_fused (whole step, one launch)",
+                                0: "k_flock_force + k_scan + k_rebin"}[args.mode],
                      "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None,
                      "algorithmic_bytes_per_launch": step_bytes,
                      "launch_ms_mean": statistics.mean(step_ms),
                      "launch_ms_median": statistics.median(step_ms),
-                     "fused": stats},
+                     "fused": stats, "autotuned": tuned},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
@@ -437,7 +448,7 @@ def run_ours(args, wl):
                 "d2h_bytes_per_call": d2h,
                 "call": f"Field2D create + set_locations + lazy_update + {e2e_steps} steps + "
                         f"get_state, host arrays in and out"},
-        "gpu_launches": K,
+        "gpu_launches": K * {2: 3, 1: 1, 0: 3}[args.mode],
         "sweep": sweep,
         "serving": serving,
     }
@@ -458,7 +469,8 @@ def main():
     ap.add_argument("--e2e-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile", default="0x0", help="fused tile shape TXxTY in bags (0x0: automatic)")
-    ap.add_argument("--unfused", action="store_true", help="separate force/scan/rebin kernels")
+    ap.add_argument("--mode", type=int, default=2,
+                    help="step path: 2 tiled split (default), 1 persistent, 0 separate kernels")
     ap.add_argument("--profile", action="store_true", help="short plain run for ncu, no timing")
     ap.add_argument("--sweep-reps", type=int, default=512)
     ap.add_argument("--sweep-steps", type=int, default=500)

@@ -158,10 +158,13 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
  * initialisation, as Schedule::step does at step 0, schedule.rs:349-351). */
 kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                         uint32_t nsteps);
-/* Step implementation options (no reference counterpart; tuning only):
- * fused = 1 runs eligible fields (toroidal, square, jump < discretization)
- * through the persistent fused step, 0 through the separate force / scan /
- * rebin kernels; tile_tx x tile_ty bags per tile (0 = automatic). */
+/* Step implementation options (no reference counterpart; tuning only).
+ * mode (the `fused` argument) for eligible fields (toroidal, square,
+ * jump < discretization): 2 (default) the tiled step as two launches per
+ * step (stage + rebin + force per tile, then the bag-offset scan), replayed
+ * from CUDA graphs; 1 the same tiles in one persistent cooperative launch;
+ * 0 the separate force / scan / rebin kernels.  tile_tx x tile_ty bags per
+ * tile (0 = automatic). */
 kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty);
 /* Counters of the fused step: out4 = {tiles that ran through the global
  * scratch path (cumulative), tiles per step, CTAs, tx << 16 | ty}. */

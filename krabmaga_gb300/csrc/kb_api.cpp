@@ -64,6 +64,8 @@ bool make_rep_geometry(float w, float h, float d, int toroidal, Rep* R, std::str
     R->dw = R->max_x + 1;
     R->dh = R->max_y + 1;
     R->ncells = (uint32_t)R->dw * (uint32_t)R->dh;
+    R->inv_d = 1.0f / d;
+    R->dh_magic = (~0ull / (unsigned long long)R->dh) + 1ull;
     return true;
 }
 
@@ -131,6 +133,9 @@ struct kb_field {
     std::vector<Rep> reps;      // every replica (a plain field holds one, == rep)
     uint32_t ncells_total = 0;  // bags over all replicas
     uint32_t cells_cap = 0;     // bag arrays are sized for this many bags
+    Rep rep_uploaded{};         // last replica record written to the device (plain fields)
+    bool rep_valid = false;
+    unsigned long long dstep_host = 0;  // the device step counter once queued work has run
     bool is_batch = false;
     DevBuf<Rep> d_rep;
     // read buffer
@@ -152,7 +157,7 @@ struct kb_field {
     std::vector<uint32_t> p_id, p_key;
     bool p_loc_differs = false;
     // step temporaries
-    DevBuf<uint32_t> hist, cursor, tid, tsrc;
+    DevBuf<uint32_t> hist, cursor, tid, tsrc, rkey, tkey;
     DevBuf<float4> tst;
     DevBuf<ScanCtl> scan_ctl, aux_ctl;
     DevBuf<unsigned long long> tstate, aux_tstate;
@@ -175,6 +180,12 @@ struct kb_field {
         }
     };
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    // split-step graphs: (steps, cur, a_last, virt) -> exec + end state
+    struct SGraph {
+        cudaGraphExec_t exec;
+        int cur, a_last;
+    };
+    std::map<std::vector<uint32_t>, SGraph> sgraphs;
     // persistent fused step (kb_fused.cu)
     struct Fused {
         bool ready = false;
@@ -194,12 +205,13 @@ struct kb_field {
         FusedCfg occ_cfg{};
         int occ_strict = -1, occ_qmode = -1, occ_ctas = 0;
     } fused;
-    int fused_mode = 1;  // 0 off, 1 on when eligible
+    int fused_mode = 2;  // 0 separate kernels, 1 persistent fused, 2 split tile step (default)
     // After fused steps the read buffer can stay virtual: the last write list
     // (in buffer a_last: 0 rst, 1 wst, 2 tst) plus start[1-cur] (its bag
     // offsets) and start[cur] (the read buffer's bag offsets).
     bool virt = false;
     int a_last = 0;
+    bool keys_valid = false;  // buf_key(a_last) holds the bag keys of the virtual write list
     int32_t tile_tx = 0, tile_ty = 0;  // 0: automatic
 
     ~kb_field() {
@@ -209,6 +221,8 @@ struct kb_field {
     void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         graphs.clear();
+        for (auto& kv : sgraphs) cudaGraphExecDestroy(kv.second.exec);
+        sgraphs.clear();
     }
 };
 
@@ -247,12 +261,12 @@ kb_status grow(kb_field* f, uint32_t need) {
     if (need > nc) return fail(KB_ERR_ARG, "object count exceeds 2^32-16");
     const uint32_t c = (uint32_t)nc;
     DevBuf<float4> rst, wst, tst;
-    DevBuf<uint32_t> rid, wid, wkey, tid, tsrc;
+    DevBuf<uint32_t> rid, wid, wkey, tid, tsrc, rkey, tkey;
     DevBuf<uint8_t> wdead;
     cudaError_t e;
     if ((e = rst.alloc(c)) || (e = wst.alloc(c)) || (e = tst.alloc(c)) || (e = rid.alloc(c)) ||
         (e = wid.alloc(c)) || (e = wkey.alloc(c)) || (e = tid.alloc(c)) || (e = tsrc.alloc(c)) ||
-        (e = wdead.alloc(c)))
+        (e = wdead.alloc(c)) || (e = rkey.alloc(c)) || (e = tkey.alloc(c)))
         return cuda_fail(e, "growing object storage");
     if (f->rn) {
         KB_CUDA(cudaMemcpyAsync(rst.p, f->rst.p, sizeof(float4) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
@@ -268,6 +282,7 @@ kb_status grow(kb_field* f, uint32_t need) {
     f->rst.swap(rst); f->wst.swap(wst); f->tst.swap(tst);
     f->rid.swap(rid); f->wid.swap(wid); f->wkey.swap(wkey);
     f->tid.swap(tid); f->tsrc.swap(tsrc); f->wdead.swap(wdead);
+    f->rkey.swap(rkey); f->tkey.swap(tkey);
     f->cap = c;
     f->drop_graphs();
     return KB_OK;
@@ -276,7 +291,10 @@ kb_status grow(kb_field* f, uint32_t need) {
 kb_status upload_rep(kb_field* f) {
     if (!f->is_batch) {
         f->reps[0] = f->rep;
+        if (f->rep_valid && std::memcmp(&f->rep_uploaded, &f->rep, sizeof(Rep)) == 0) return KB_OK;
         KB_CUDA(launch_set_rep(f->d_rep.p, f->rep, f->stream));
+        f->rep_uploaded = f->rep;
+        f->rep_valid = true;
     } else {
         KB_CUDA(cudaMemcpyAsync(f->d_rep.p, f->reps.data(), sizeof(Rep) * f->reps.size(), cudaMemcpyHostToDevice, f->stream));
         KB_CUDA(cudaStreamSynchronize(f->stream));
@@ -365,6 +383,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     RebinArgs a;
     a.reps = f->d_rep.p;
     a.nrep = nrep(f);
+    a.rep0 = f->reps[0];
     a.start_cur = f->start[f->cur].p;
     a.start_next = f->start[nxt].p;
     a.key = f->wkey.p;
@@ -384,6 +403,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     ForceArgs a;
     a.reps = f->d_rep.p;
     a.nrep = nrep(f);
+    a.rep0 = f->reps[0];
     a.st = f->rst.p;
     a.ids = f->rid.p;
     a.start = f->start[f->cur].p;
@@ -401,6 +421,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
 
 float4* buf_st(kb_field* f, int i) { return i == 0 ? f->rst.p : (i == 1 ? f->wst.p : f->tst.p); }
 uint32_t* buf_ids(kb_field* f, int i) { return i == 0 ? f->rid.p : (i == 1 ? f->wid.p : f->tid.p); }
+uint32_t* buf_key(kb_field* f, int i) { return i == 0 ? f->rkey.p : (i == 1 ? f->wkey.p : f->tkey.p); }
 
 // Rebuild the read buffer from a virtual state (the stencil gather of the
 // last write list into canonical order).
@@ -411,9 +432,10 @@ kb_status materialize(kb_field* f) {
     RebinArgs r;
     r.reps = f->d_rep.p;
     r.nrep = nrep(f);
+    r.rep0 = f->reps[0];
     r.start_cur = f->start[1 - f->cur].p;
     r.start_next = f->start[f->cur].p;
-    r.key = nullptr;
+    r.key = f->keys_valid ? buf_key(f, f->a_last) : nullptr;
     r.a_st = buf_st(f, f->a_last);
     r.a_ids = buf_ids(f, f->a_last);
     r.ncells = f->ncells_total;
@@ -592,7 +614,132 @@ kb_status fused_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
     // the newest offsets are in start_b[last]; the previous ones in the other
     f->cur = (last == 0) ? 1 - cur0 : cur0;
     f->virt = true;
+    f->keys_valid = false;  // the persistent kernel does not write keys
     return KB_OK;
+}
+
+FusedArgs fused_args(kb_field* f) {
+    auto& F = f->fused;
+    FusedArgs a{};
+    a.reps = f->d_rep.p;
+    a.nrep = nrep(f);
+    a.tiles = F.tiles.p;
+    a.ntiles = F.ntiles;
+    a.cfg = F.cfg;
+    a.ncells = f->ncells_total;
+    a.n = f->rn;
+    a.hist = f->hist.p;
+    a.g_sord_st = F.g_st.p;
+    a.g_sord_ids = F.g_ids.p;
+    a.step = f->dstep.p;
+    a.err = f->err.p;
+    a.stats = F.ctl.p + 4;
+    a.phase_cycles = nullptr;
+    if (F.profile) {
+        if (F.phase_cycles.n < 16) {
+            if (F.phase_cycles.alloc(16)) return a;
+            cudaMemsetAsync(F.phase_cycles.p, 0, sizeof(unsigned long long) * 16, f->stream);
+        }
+        a.phase_cycles = F.phase_cycles.p;
+    }
+    return a;
+}
+
+// nsteps steps in the split form: per step one tile launch (stage, rebin,
+// force) and one scan launch; the step counter advances at the end.  Same
+// buffer discipline as fused_steps; leaves the read buffer virtual.
+kb_status split_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
+    auto& F = f->fused;
+    cudaStream_t s = f->stream;
+    int cur = f->cur;
+    int in = 0;
+    if (!f->virt) {
+        const size_t sb = sizeof(uint32_t) * ((size_t)f->ncells_total + 1);
+        KB_CUDA(cudaMemcpyAsync(f->start[1 - cur].p, f->start[cur].p, sb, cudaMemcpyDeviceToDevice, s));
+        in = 0;
+    } else {
+        in = f->a_last;
+    }
+    const FusedArgs a = fused_args(f);
+    // keys travel with the write lists; a materialised read buffer has none
+    bool in_keys = f->virt && f->keys_valid;
+    for (uint32_t k = 0; k < nsteps; ++k) {
+        const int out = (in + 1) % 3;
+        KB_CUDA(launch_tile_step(a, buf_st(f, in), buf_ids(f, in), in_keys ? buf_key(f, in) : nullptr,
+                                 buf_st(f, out), buf_ids(f, out), buf_key(f, out),
+                                 f->start[1 - cur].p, f->start[cur].p, k, F.strict != 0, F.qmode, s));
+        in_keys = true;
+        KB_CUDA(launch_scan(f->hist.p, f->start[1 - cur].p, f->ncells_total, f->scan_ctl.p,
+                            f->tstate.p, f->err.p, true, s));
+        cur = 1 - cur;
+        in = out;
+    }
+    KB_CUDA(launch_add_u64(f->dstep.p, nsteps, s));
+    f->cur = cur;
+    f->a_last = in;
+    f->virt = true;
+    f->keys_valid = true;
+    return KB_OK;
+}
+
+// split_steps in CUDA-graph chunks of at most `chunk` steps, cached by the
+// buffer state they start from.
+kb_status split_steps_graphed(kb_field* f, const kb_flock_params* p, uint32_t nsteps, uint32_t chunk) {
+    uint32_t done = 0;
+    while (done < nsteps) {
+        const uint32_t k = std::min(chunk, nsteps - done);
+        if (k < 2) {
+            kb_status st = split_steps(f, p, k);
+            if (st) return st;
+            done += k;
+            continue;
+        }
+        std::vector<uint32_t> key = {k, (uint32_t)f->cur, (uint32_t)f->a_last, f->virt ? 1u : 0u,
+                                     f->keys_valid ? 1u : 0u, (uint32_t)f->fused.strict,
+                                     (uint32_t)f->fused.qmode};
+        auto it = f->sgraphs.find(key);
+        if (it == f->sgraphs.end()) {
+            const int cur0 = f->cur, al0 = f->a_last;
+            const bool v0 = f->virt, kv0 = f->keys_valid;
+            cudaGraph_t graph = nullptr;
+            KB_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
+            kb_status st = split_steps(f, p, k);
+            cudaError_t ce = cudaStreamEndCapture(f->stream, &graph);
+            if (st) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (ce) return cuda_fail(ce, "cudaStreamEndCapture");
+            cudaGraphExec_t exec = nullptr;
+            ce = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce) return cuda_fail(ce, "cudaGraphInstantiate");
+            if (f->sgraphs.size() > 24) {
+                for (auto& kv : f->sgraphs) cudaGraphExecDestroy(kv.second.exec);
+                f->sgraphs.clear();
+            }
+            it = f->sgraphs.emplace(key, kb_field::SGraph{exec, f->cur, f->a_last}).first;
+            f->cur = cur0;
+            f->a_last = al0;
+            f->virt = v0;
+            f->keys_valid = kv0;
+        }
+        KB_CUDA(cudaGraphLaunch(it->second.exec, f->stream));
+        f->cur = it->second.cur;
+        f->a_last = it->second.a_last;
+        f->virt = true;
+        f->keys_valid = true;
+        done += k;
+    }
+    return KB_OK;
+}
+
+// Run nsteps through the configured tiled path (split or persistent).
+kb_status tiled_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
+    kb_status st = fused_prepare(f, p);
+    if (st) return st;
+    if (f->fused_mode == 1) return fused_steps(f, p, nsteps);
+    return split_steps_graphed(f, p, nsteps, 100);
 }
 
 kb_status field_lazy_update(kb_field* f) {
@@ -658,7 +805,7 @@ kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uin
     kb_field* f = new kb_field();
     f->device = device;
     f->reps = reps;
-    f->rep = reps[0];
+    f->rep = f->reps[0];
     f->ncells_total = ncells;
     f->cells_cap = nc;
     f->is_batch = is_batch;
@@ -712,7 +859,7 @@ kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
         if (e) return cuda_fail(e, "replica table");
     }
     f->reps = reps;
-    f->rep = reps[0];
+    f->rep = f->reps[0];
     f->ncells_total = (uint32_t)total;
     f->fused.ready = false;
     f->drop_graphs();
@@ -1137,7 +1284,8 @@ kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx,
     if (!f) return fail(KB_ERR_ARG, "null argument");
     if (tile_tx < 0 || tile_ty < 0 || tile_tx > 64 || tile_ty > 128)
         return fail(KB_ERR_ARG, "tile shape out of range (tx <= 64, ty <= 128)");
-    f->fused_mode = fused ? 1 : 0;
+    if (fused < 0 || fused > 2) return fail(KB_ERR_ARG, "step mode must be 0, 1 or 2");
+    f->fused_mode = fused;
     f->tile_tx = tile_tx;
     f->tile_ty = tile_ty;
     f->fused.ready = false;
@@ -1215,6 +1363,7 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
     set_rep_params(&f->rep, p);
     if ((st = upload_rep(f))) return st;
     KB_CUDA(launch_set_u64(f->dstep.p, step, f->stream));
+    f->dstep_host = step;
     if ((st = enqueue_force(f, p))) return st;
     f->wn = f->rn;
     f->w_from_compute = true;
@@ -1236,8 +1385,8 @@ static kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t n
     return KB_OK;
 }
 
-kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
-                        uint32_t nsteps) {
+static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                                 uint32_t nsteps) {
     if (f && f->is_batch) return fail(KB_ERR_ARG, "a batch field: use kb_batch_step");
     if (!f || !p) return fail(KB_ERR_ARG, "null argument");
     std::string why;
@@ -1251,7 +1400,10 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
     if (f->virt && !fused_eligible(f, p) && (st = materialize(f))) return st;
     if (!f->virt && (st = grow(f, f->rn))) return st;
     if ((st = upload_rep(f))) return st;
-    KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
+    if (f->dstep_host != first_step) {  // the counter already holds it after consecutive calls
+        KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
+        f->dstep_host = first_step;
+    }
     uint32_t done = 0;
     if (!f->layout_is_positions) {
         // the first step after arbitrary set_object_location calls re-sorts generally
@@ -1259,11 +1411,7 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         f->layout_is_positions = true;
         done = 1;
     }
-    if (done < nsteps && fused_eligible(f, p)) {
-        if ((st = fused_prepare(f, p))) return st;
-        if ((st = fused_steps(f, p, nsteps - done))) return st;
-        return KB_OK;
-    }
+    if (done < nsteps && fused_eligible(f, p)) return tiled_steps(f, p, nsteps - done);
     if (f->virt && (st = materialize(f))) return st;
     const bool use_fast = all_fast_rebin_ok(f);
     // CUDA-graph replay of chunks of up to 100 steps (one graph per chunk
@@ -1311,6 +1459,13 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
         done += k;
     }
     return KB_OK;
+}
+
+kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+                        uint32_t nsteps) {
+    kb_status st = flock_step_impl(f, p, first_step, nsteps);
+    if (f) f->dstep_host = st ? ~0ull : first_step + nsteps;  // unknown after a failure
+    return st;
 }
 
 }  // extern "C"
@@ -1444,6 +1599,7 @@ kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint3
     const kb_flock_params* p = &b->common;
     kb_status st;
     KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
+    f->dstep_host = ~0ull;
     if (!fused_eligible(f, p)) {
         if ((st = materialize(f))) return st;
         if ((st = grow(f, f->rn))) return st;
@@ -1451,6 +1607,8 @@ kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint3
     }
     if ((st = grow(f, f->rn))) return st;
     if ((st = fused_prepare(f, p))) return st;
+    if (f->fused_mode == 2)  // split: two launches per step, graphs of graph_launches steps
+        return split_steps_graphed(f, p, nsteps, graph_launches > 1 ? graph_launches : 100);
     const uint32_t spl = steps_per_launch == 0 ? nsteps : std::min(steps_per_launch, nsteps);
     uint32_t done = 0;
     while (done < nsteps) {
@@ -1781,10 +1939,11 @@ void srv_loop(kb_server* S) {
         for (SrvReq* q : act) K = std::min(K, q->remaining);
         if (!st) {
             st = launch_set_u64(f->dstep.p, S->global_step, f->stream) ? fail(KB_ERR_CUDA, "step") : KB_OK;
+            f->dstep_host = ~0ull;
         }
         if (!st && K > 0) {
             if (fused_eligible(f, &S->common)) {
-                if (!(st = fused_prepare(f, &S->common))) st = fused_steps(f, &S->common, K);
+                st = tiled_steps(f, &S->common, K);
             } else {
                 if (!(st = materialize(f))) st = enqueue_steps(f, &S->common, K, all_fast_rebin_ok(f));
             }

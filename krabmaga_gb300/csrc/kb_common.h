@@ -48,6 +48,9 @@ struct Rep {
     int32_t nowrap;         // 1: no candidate pair can straddle the seam ((dd+1)*d < min(w,h)/2)
     uint32_t origin_lo, origin_hi;  // global step at which this replica's step 0 ran
     int32_t seam;           // first line from which a one-step move can wrap to line 0
+    float inv_d;            // fl(1/d), for the exact fast discretisation
+    uint32_t _pad2;
+    unsigned long long dh_magic;  // ceil(2^64 / dh): n / dh == umul64hi(n, dh_magic) for n < 2^32
 };
 
 // ------------------------------------------------------------------ Philox

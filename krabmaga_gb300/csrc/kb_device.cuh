@@ -24,13 +24,31 @@ struct F<true> {
     static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
     static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
 };
+// Single-instruction approximations (PTX rcp/sqrt/rsqrt .approx.ftz) for
+// the fast arithmetic.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 template <>
 struct F<false> {
     static __device__ __forceinline__ float add(float a, float b) { return a + b; }
     static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
     static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
-    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
-    static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
+    static __device__ __forceinline__ float div(float a, float b) { return a * rcp_approx(b); }
+    static __device__ __forceinline__ float sqrt(float a) { return sqrt_approx(a); }
 };
 
 // field_2d.rs:1004-1014
@@ -83,14 +101,31 @@ __device__ __forceinline__ int check_circle(int bx, int by, const Rep& R, float 
     return 0;
 }
 
-// discretize (field_2d.rs:328-339), always IEEE (bag choice is index work).
-__device__ __forceinline__ int32_t disc(float v, float d) { return as_i32(floorf(__fdiv_rn(v, d))); }
+// floor(fl(v/d)) as i32 (field_2d.rs:328-339), bit-exact: fl(v * fl(1/d))
+// is within ~2 ulp of the IEEE quotient fl(v/d), so their floors can only
+// differ when the product lies within 4 ulp of an integer; only then is the
+// IEEE quotient formed.  NaN and infinities take the same values as the
+// direct form (NaN -> 0, saturation).
+__device__ __forceinline__ int32_t disc_d(float v, float d, float inv_d) {
+    const float q = v * inv_d;
+    float f = floorf(q);
+    const float fr = q - f;
+    const float tol = fabsf(q) * 4.8e-7f;
+    if (fr < tol || fr > 1.0f - tol) f = floorf(__fdiv_rn(v, d));
+    return as_i32(f);
+}
+__device__ __forceinline__ int32_t disc(float v, const Rep& R) { return disc_d(v, R.d, R.inv_d); }
+
+// x / dh and x % dh for a replica's bag index (x < 2^32).
+__device__ __forceinline__ uint32_t div_dh(uint32_t x, const Rep& R) {
+    return (uint32_t)__umul64hi((unsigned long long)x, R.dh_magic);
+}
 
 // The query's cell range (field_2d.rs:398-418 / 484-500).  False: dist <= 0.
 __device__ __forceinline__ bool cell_range(const Rep& R, float x, float y, int32_t dd, int* mi,
                                            int* Mi, int* mj, int* Mj) {
     if (dd < 0) return false;
-    int cx = disc(x, R.d), cy = disc(y, R.d);
+    int cx = disc(x, R), cy = disc(y, R);
     int a = cx - dd, b = cx + dd, c = cy - dd, e = cy + dd;
     if (R.toroidal) {
         a = max(0, a);
@@ -146,12 +181,18 @@ struct Acc {
     int count = 0;
     uint32_t vec = 0;  // candidates including self (the reference's vec.len())
 
+    // toroidal_distance's first branch is taken for every pair when the
+    // replica guarantees it (Rep::nowrap, hoisted out of the loops by the
+    // callers): the same bits, no test
+    template <bool NOWRAP = false>
     __device__ __forceinline__ void add(const Rep& R, float sx, float sy, float4 o) {
         using M = F<STRICT>;
-        // toroidal_distance's first branch is taken for every pair when the
-        // replica guarantees it (Rep::nowrap): the same bits, no test
-        float dx = R.nowrap ? __fsub_rn(sx, o.x) : toroidal_distance(sx, o.x, R.w);
-        float dy = R.nowrap ? __fsub_rn(sy, o.y) : toroidal_distance(sy, o.y, R.h);
+        const float dx = NOWRAP ? __fsub_rn(sx, o.x) : toroidal_distance(sx, o.x, R.w);
+        const float dy = NOWRAP ? __fsub_rn(sy, o.y) : toroidal_distance(sy, o.y, R.h);
+        add_d(dx, dy, o);
+    }
+    __device__ __forceinline__ void add_d(float dx, float dy, float4 o) {
+        using M = F<STRICT>;
         count += 1;
         float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
         float q = M::add(M::mul(sq, sq), 1.0f);
@@ -159,7 +200,7 @@ struct Acc {
             xa = M::add(xa, M::div(dx, q));
             ya = M::add(ya, M::div(dy, q));
         } else {
-            float inv = __fdividef(1.0f, q);
+            const float inv = rcp_approx(q);
             xa = xa + dx * inv;
             ya = ya + dy * inv;
         }
@@ -198,7 +239,12 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
     float avx = 0.f, avy = 0.f, cox = 0.f, coy = 0.f, rax = 0.f, ray = 0.f, csx = 0.f, csy = 0.f;
     if (acc.vec > 0) {
         float xa = acc.xa, ya = acc.ya, xc = acc.xc, yc = acc.yc, xs = acc.xs, ys = acc.ys;
-        if (acc.count > 0) {
+        if (acc.count > 0 && !STRICT) {
+            const float ic = rcp_approx((float)acc.count);
+            xa *= ic; ya *= ic; xc *= ic; yc *= ic; xs *= ic; ys *= ic;
+            csx = xs * ic;  // bird.rs:91-94: a second division by count
+            csy = ys * ic;
+        } else if (acc.count > 0) {
             const float c = (float)acc.count;
             xa = M::div(xa, c); ya = M::div(ya, c);
             xc = M::div(xc, c); yc = M::div(yc, c);
@@ -220,9 +266,15 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
                                    R.seed_lo, R.seed_hi);
         const float xr = M::sub(M::mul(unit_f32(o.x), 2.0f), 1.0f);
         const float yr = M::sub(M::mul(unit_f32(o.y), 2.0f), 1.0f);
-        const float sq = M::sqrt(M::add(M::mul(xr, xr), M::mul(yr, yr)));
-        rax = M::div(M::mul(0.05f, xr), sq);
-        ray = M::div(M::mul(0.05f, yr), sq);
+        if (STRICT) {
+            const float sq = M::sqrt(M::add(M::mul(xr, xr), M::mul(yr, yr)));
+            rax = M::div(M::mul(0.05f, xr), sq);
+            ray = M::div(M::mul(0.05f, yr), sq);
+        } else {
+            const float rs = 0.05f * rsqrt_approx(xr * xr + yr * yr);
+            rax = xr * rs;
+            ray = yr * rs;
+        }
     }
     float dx = M::add(M::add(M::add(M::add(M::mul(R.coh, cox), M::mul(R.avo, avx)),
                                     M::mul(R.con, csx)),
@@ -232,10 +284,19 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
                                     M::mul(R.con, csy)),
                              M::mul(R.rnd, ray)),
                       M::mul(R.mom, me.w));
-    const float dis = M::sqrt(M::add(M::mul(dx, dx), M::mul(dy, dy)));
-    if (dis > 0.0f) {
-        dx = M::mul(M::div(dx, dis), R.jump);
-        dy = M::mul(M::div(dy, dis), R.jump);
+    if (STRICT) {
+        const float dis = M::sqrt(M::add(M::mul(dx, dx), M::mul(dy, dy)));
+        if (dis > 0.0f) {
+            dx = M::mul(M::div(dx, dis), R.jump);
+            dy = M::mul(M::div(dy, dis), R.jump);
+        }
+    } else {
+        const float d2 = dx * dx + dy * dy;
+        if (d2 > 0.0f) {
+            const float s = rsqrt_approx(d2) * R.jump;
+            dx *= s;
+            dy *= s;
+        }
     }
     const float nx = toroidal_transform(__fadd_rn(me.x, dx), R.w);
     const float ny = toroidal_transform(__fadd_rn(me.y, dy), R.w);  // bird.rs:147: y wraps with w

@@ -286,7 +286,7 @@ struct PhaseClock {
     __device__ void mark(int k) {
         if (out && threadIdx.x == 0) {
             const long long n = clock64();
-            out[k] += (unsigned long long)(n - t);
+            atomicAdd(&out[k], (unsigned long long)(n - t));
             t = n;
         }
     }
@@ -311,13 +311,16 @@ struct Smem {
     uint8_t* nsrcx;
     uint8_t* srcy;    // [maxqy][4][2] staged row runs feeding each canonical row
     uint8_t* nsrcy;
+    uint16_t* sord_cell;  // region-local bag (iq * nqy + jq) of each canonical record
 };
 
 struct StepBufs {
     const float4* prev_st;
     const uint32_t* prev_ids;
+    const uint32_t* prev_key;  // bag of each previous record (nullptr: recompute)
     float4* next_st;
     uint32_t* next_ids;
+    uint32_t* next_key;
     const uint32_t* start_prev;
     const uint32_t* start_cur;
 };
@@ -333,6 +336,8 @@ __device__ __forceinline__ void gather_bag_smem(const FusedArgs& a, const Rep& R
     const uint32_t expected = e0 - s0;
     const uint32_t cglob = R.cell_off + (uint32_t)(c.qx0 + iq) * (uint32_t)R.dh + (uint32_t)(c.qy0 + jq);
     const uint32_t sdst = S.colblk[iq] + (s0 - stt_col[0]);
+    const uint16_t lcell = (uint16_t)(iq * c.nqy + jq);
+    for (uint32_t k = 0; k < expected; ++k) S.sord_cell[sdst + k] = lcell;
     uint32_t m = 0;
     const int ncx = S.nsrcx[iq], nry = S.nsrcy[jq];
     for (int ax = 0; ax < ncx; ++ax) {
@@ -380,11 +385,17 @@ __device__ __forceinline__ void gather_bag_global(const FusedArgs& a, const Rep&
             const uint32_t cell = R.cell_off + (uint32_t)sx * (uint32_t)R.dh + (uint32_t)sy;
             const uint32_t gs = ldcg_u32(B.start_prev + cell), ge = ldcg_u32(B.start_prev + cell + 1);
             for (uint32_t q = gs; q < ge; ++q) {
-                const float4 r = ldcg_f4(B.prev_st + q);
-                const int64_t k = bag_index(R, disc(r.x, R.d), disc(r.y, R.d));
-                if (k >= 0 && R.cell_off + (uint32_t)k == cglob) {
+                uint32_t key;
+                if (B.prev_key) {
+                    key = ldcg_u32(B.prev_key + q);
+                } else {
+                    const float4 r = ldcg_f4(B.prev_st + q);
+                    const int64_t k = bag_index(R, disc(r.x, R), disc(r.y, R));
+                    key = k >= 0 ? R.cell_off + (uint32_t)k : 0xFFFFFFFFu;
+                }
+                if (key == cglob) {
                     if (m < expected) {
-                        a.g_sord_st[s0 + m] = r;
+                        a.g_sord_st[s0 + m] = ldcg_f4(B.prev_st + q);
                         a.g_sord_ids[s0 + m] = ldcg_u32(B.prev_ids + q);
                     }
                     ++m;
@@ -461,9 +472,19 @@ __device__ __forceinline__ void force_boid(const FusedArgs& a, const Rep& R, con
         me = ldcg_f4(a.g_sord_st + p);
         my_id = ldcg_u32(a.g_sord_ids + p);
     }
+    // the boid's bag: recorded by the shared-memory gather, else recomputed
+    int cx, cy;
+    if (SM) {
+        const uint32_t lc = S.sord_cell[S.colblk[X - c.qx0] + (p - sttX[0])];
+        cx = c.qx0 + (int)(lc / (uint32_t)c.nqy);
+        cy = c.qy0 + (int)(lc % (uint32_t)c.nqy);
+    } else {
+        cx = disc(me.x, R);
+        cy = disc(me.y, R);
+    }
+    const int32_t ocx = cx, ocy = cy;
     Acc<STRICT> acc;
     if (R.dd >= 0) {
-        int cx = disc(me.x, R.d), cy = disc(me.y, R.d);
         if (cx < c.X0 || cx >= c.X1 || cy < c.Y0 || cy >= c.Y1) {
             atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_OUTSIDE);  // a boid outside its own bag
             cx = min(max(cx, c.X0), c.X1 - 1);
@@ -479,11 +500,20 @@ __device__ __forceinline__ void force_boid(const FusedArgs& a, const Rep& R, con
                 const uint32_t* base_id = SM ? S.sord_ids : a.g_sord_ids;
                 if (QMODE == 0) {
                     const uint32_t s = sttc[mj - c.qy0], e = sttc[Mj + 1 - c.qy0];
-                    for (uint32_t q = s; q < e; ++q) {
-                        const uint32_t qi = (uint32_t)((int64_t)q + adj);
-                        acc.vec += 1;
-                        const uint32_t oid = SM ? base_id[qi] : ldcg_u32(base_id + qi);
-                        if (oid != my_id) acc.add(R, me.x, me.y, SM ? base_st[qi] : ldcg_f4(base_st + qi));
+                    acc.vec += e - s;
+                    if (R.nowrap) {
+                        for (uint32_t q = s; q < e; ++q) {
+                            const uint32_t qi = (uint32_t)((int64_t)q + adj);
+                            const uint32_t oid = SM ? base_id[qi] : ldcg_u32(base_id + qi);
+                            if (oid != my_id)
+                                acc.template add<true>(R, me.x, me.y, SM ? base_st[qi] : ldcg_f4(base_st + qi));
+                        }
+                    } else {
+                        for (uint32_t q = s; q < e; ++q) {
+                            const uint32_t qi = (uint32_t)((int64_t)q + adj);
+                            const uint32_t oid = SM ? base_id[qi] : ldcg_u32(base_id + qi);
+                            if (oid != my_id) acc.add(R, me.x, me.y, SM ? base_st[qi] : ldcg_f4(base_st + qi));
+                        }
                     }
                 } else {
                     for (int cj = mj; cj <= Mj; ++cj) {
@@ -509,15 +539,15 @@ __device__ __forceinline__ void force_boid(const FusedArgs& a, const Rep& R, con
     const float4 nxt = finish_bird<STRICT>(R, me, my_id, step, acc);
     B.next_st[p] = nxt;
     B.next_ids[p] = my_id;
-    const int32_t ncx = disc(nxt.x, R.d), ncy = disc(nxt.y, R.d);
+    const int32_t ncx = disc(nxt.x, R), ncy = disc(nxt.y, R);
     int64_t idx = bag_index(R, ncx, ncy);
+    if (B.next_key) B.next_key[p] = R.cell_off + (uint32_t)(idx < 0 ? 0 : idx);
     uint32_t flags = 0;
     if (idx < 0) {
         flags |= ERR_KEY_RANGE;
         idx = 0;
     }
     if (!isfinite(nxt.x) || !isfinite(nxt.y)) flags |= ERR_NONFINITE;
-    const int32_t ocx = disc(me.x, R.d), ocy = disc(me.y, R.d);
     const bool okx = move_ok(ocx, ncx, R.seam), oky = move_ok(ocy, ncy, R.seam);
     if (!(okx && oky)) flags |= ERR_REBIN_MISS | ERR_MISS_MOVE;
     if (flags) atomicOr(a.err, flags);
@@ -667,7 +697,10 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
         }
         for (uint32_t k = warp; k < c.nseg; k += FT / 32) {
             const Seg g = S.seg[k];
-            for (uint32_t e = lane; e < g.cnt; e += 32) S.stage_ids[g.soff + e] = ldcg_u32(B.prev_ids + g.glo + e);
+            for (uint32_t e = lane; e < g.cnt; e += 32) {
+                S.stage_ids[g.soff + e] = ldcg_u32(B.prev_ids + g.glo + e);
+                if (B.prev_key) S.stage_key[g.soff + e] = ldcg_u32(B.prev_key + g.glo + e);
+            }
         }
         for (int t = tid; t < c.nsx * c.nsy; t += FT) {
             const int i = t / c.nsy, j = t % c.nsy;
@@ -680,19 +713,28 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
             S.cell_lo[t] = g.soff + (s0 - g.glo);
             S.cell_cnt[t] = s1 - s0;
         }
-        uint32_t spins = 0;
-        while (!mbar_try_wait(S.mbar, *phase & 1u)) {
-            if (++spins > TMA_SPINS) {
-                atomicOr(a.err, ERR_SPIN_TIMEOUT);
-                break;
+        // one warp waits on the transaction barrier; the rest block at the
+        // CTA barrier, then observe the completed phase once
+        if (warp == 0) {
+            uint32_t spins = 0;
+            while (!mbar_try_wait(S.mbar, *phase & 1u)) {
+                if (++spins > TMA_SPINS) {
+                    atomicOr(a.err, ERR_SPIN_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        if (warp != 0) {
+            uint32_t spins = 0;
+            while (!mbar_try_wait(S.mbar, *phase & 1u) && ++spins < 64u) {
             }
         }
         *phase += 1;
-        __syncthreads();
         pc.mark(3);
         for (uint32_t e = tid; e < c.staged; e += FT) {
             const float4 r = S.stage_st[e];
-            const int64_t k = bag_index(R, disc(r.x, R.d), disc(r.y, R.d));
+            const int64_t k = bag_index(R, disc(r.x, R), disc(r.y, R));
             S.stage_key[e] = k >= 0 ? R.cell_off + (uint32_t)k : 0xFFFFFFFFu;
         }
         __syncthreads();
@@ -726,6 +768,52 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
     pc.mark(7);
 }
 
+__device__ __forceinline__ Smem smem_view(unsigned char* smem, const FusedLayout& L) {
+    Smem S;
+    S.mbar = reinterpret_cast<unsigned long long*>(smem + L.off_mbar);
+    S.stage_st = reinterpret_cast<float4*>(smem + L.off_stage_st);
+    S.sord_st = reinterpret_cast<float4*>(smem + L.off_sord_st);
+    S.stage_ids = reinterpret_cast<uint32_t*>(smem + L.off_stage_ids);
+    S.stage_key = reinterpret_cast<uint32_t*>(smem + L.off_stage_key);
+    S.sord_ids = reinterpret_cast<uint32_t*>(smem + L.off_sord_ids);
+    S.seg = reinterpret_cast<Seg*>(smem + L.off_seg);
+    S.cell_lo = reinterpret_cast<uint32_t*>(smem + L.off_cell_lo);
+    S.cell_cnt = reinterpret_cast<uint32_t*>(smem + L.off_cell_cnt);
+    S.stt = reinterpret_cast<uint32_t*>(smem + L.off_stt);
+    S.colblk = reinterpret_cast<uint32_t*>(smem + L.off_colblk);
+    S.owned = reinterpret_cast<uint32_t*>(smem + L.off_owned);
+    S.hist = reinterpret_cast<uint32_t*>(smem + L.off_hist);
+    S.srcx = smem + L.off_srcx;
+    S.nsrcx = smem + L.off_nsrcx;
+    S.srcy = smem + L.off_srcy;
+    S.nsrcy = smem + L.off_nsrcy;
+    S.sord_cell = reinterpret_cast<uint16_t*>(smem + L.off_sord_cell);
+    return S;
+}
+
+// One step of one tile per CTA (no grid-wide waits): the split form of the
+// step, followed by the histogram scan as its own launch.
+template <bool STRICT, int QMODE>
+__global__ void __launch_bounds__(FT, 4) k_tile_step(FusedArgs a, StepBufs B, uint32_t step_offset) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ TileCtx ctx;
+    const FusedLayout L = fused_layout(a.cfg);
+    const Smem S = smem_view(smem, L);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(S.mbar, 1);
+        fence_proxy_async();
+    }
+    for (int t = tid; t < L.maxhx * L.maxhy; t += FT) S.hist[t] = 0u;
+    __syncthreads();
+    const unsigned long long step = *a.step + step_offset;
+    uint32_t phase = 0;
+    PhaseClock pc;
+    pc.out = a.phase_cycles;  // all CTAs add into one set of counters
+    if (pc.out && tid == 0) pc.t = clock64();
+    process_tile<STRICT, QMODE>(a, a.tiles[blockIdx.x], ctx, S, B, step, &phase, pc);
+}
+
 template <bool STRICT, int QMODE>
 __global__ void __launch_bounds__(FT, 2) k_fused(FusedArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -750,6 +838,7 @@ __global__ void __launch_bounds__(FT, 2) k_fused(FusedArgs a) {
     S.nsrcx = smem + L.off_nsrcx;
     S.srcy = smem + L.off_srcy;
     S.nsrcy = smem + L.off_nsrcy;
+    S.sord_cell = reinterpret_cast<uint16_t*>(smem + L.off_sord_cell);
     const int tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(S.mbar, 1);
@@ -766,8 +855,10 @@ __global__ void __launch_bounds__(FT, 2) k_fused(FusedArgs a) {
         StepBufs B;
         B.prev_st = s == 0 ? a.a_in_st : a.a_st[(s - 1) & 1];
         B.prev_ids = s == 0 ? a.a_in_ids : a.a_ids[(s - 1) & 1];
+        B.prev_key = nullptr;
         B.next_st = a.a_st[s & 1];
         B.next_ids = a.a_ids[s & 1];
+        B.next_key = nullptr;
         B.start_prev = a.start_b[s & 1];
         B.start_cur = a.start_b[(s + 1) & 1];
         const unsigned long long step = base_step + s;
@@ -804,6 +895,16 @@ void* pick(bool strict, int qmode) {
     return qmode == 0 ? fused_fn<false, 0>() : fused_fn<false, 1>();
 }
 
+template <bool STRICT, int QMODE>
+void* tile_fn() {
+    return reinterpret_cast<void*>(&k_tile_step<STRICT, QMODE>);
+}
+
+void* pick_tile(bool strict, int qmode) {
+    if (strict) return qmode == 0 ? tile_fn<true, 0>() : tile_fn<true, 1>();
+    return qmode == 0 ? tile_fn<false, 0>() : tile_fn<false, 1>();
+}
+
 }  // namespace
 
 int fused_max_ctas(const FusedCfg& cfg, bool strict, int qmode, int device) {
@@ -821,6 +922,29 @@ int fused_max_ctas(const FusedCfg& cfg, bool strict, int qmode, int device) {
         return 0;
     }
     return per_sm * sms;
+}
+
+cudaError_t launch_tile_step(const FusedArgs& a, const float4* prev_st, const uint32_t* prev_ids,
+                             const uint32_t* prev_key, float4* next_st, uint32_t* next_ids,
+                             uint32_t* next_key, const uint32_t* start_prev,
+                             const uint32_t* start_cur, uint32_t step_offset, bool strict, int qmode,
+                             cudaStream_t s) {
+    if (a.ntiles == 0) return cudaSuccess;
+    const FusedLayout L = fused_layout(a.cfg);
+    void* fn = pick_tile(strict, qmode);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    if (e != cudaSuccess) return e;
+    StepBufs B;
+    B.prev_st = prev_st;
+    B.prev_ids = prev_ids;
+    B.prev_key = prev_key;
+    B.next_st = next_st;
+    B.next_ids = next_ids;
+    B.next_key = next_key;
+    B.start_prev = start_prev;
+    B.start_cur = start_cur;
+    void* args[] = {const_cast<FusedArgs*>(&a), &B, &step_offset};
+    return cudaLaunchKernel(fn, dim3(a.ntiles), dim3(FT), args, L.total, s);
 }
 
 cudaError_t launch_fused(const FusedArgs& a, bool strict, int qmode, uint32_t nctas,

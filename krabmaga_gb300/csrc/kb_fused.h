@@ -44,7 +44,7 @@ struct FusedCfg {
 struct FusedLayout {
     uint32_t off_mbar, off_stage_st, off_sord_st, off_stage_ids, off_stage_key, off_sord_ids;
     uint32_t off_seg, off_cell_lo, off_cell_cnt, off_stt, off_colblk, off_owned, off_hist;
-    uint32_t off_srcx, off_nsrcx, off_srcy, off_nsrcy;
+    uint32_t off_srcx, off_nsrcx, off_srcy, off_nsrcy, off_sord_cell;
     uint32_t total;
     int32_t maxlx, maxly, maxqx, maxqy, maxseg, maxhx, maxhy;
 };
@@ -80,6 +80,8 @@ KB_HD FusedLayout fused_layout(const FusedCfg& c) {
     o = fused_align(o, 4);
     L.off_srcy = o; o += (uint32_t)L.maxqy * 4u * 2u;   // (first, last) staged row runs per row
     L.off_nsrcy = o; o += (uint32_t)L.maxqy;
+    o = fused_align(o, 4);
+    L.off_sord_cell = o; o += c.sord_cap * 2u;          // region-local bag per record
     L.total = fused_align(o, 16);
     return L;
 }
@@ -118,5 +120,16 @@ struct FusedArgs {
 int fused_max_ctas(const FusedCfg& cfg, bool strict, int qmode, int device);
 cudaError_t launch_fused(const FusedArgs& a, bool strict, int qmode, uint32_t nctas,
                          cudaStream_t s);
+// One step, one CTA per tile (the split form): reads the previous write list
+// (prev_*, its bag keys prev_key or nullptr to recompute them) with its bag
+// offsets start_prev, writes the next one (and its keys) at the canonical
+// slots of start_cur and counts the new bags into a.hist.  The
+// step number is *a.step + step_offset.  The scan of a.hist follows as its
+// own launch.
+cudaError_t launch_tile_step(const FusedArgs& a, const float4* prev_st, const uint32_t* prev_ids,
+                             const uint32_t* prev_key, float4* next_st, uint32_t* next_ids,
+                             uint32_t* next_key, const uint32_t* start_prev,
+                             const uint32_t* start_cur, uint32_t step_offset, bool strict, int qmode,
+                             cudaStream_t s);
 
 }  // namespace kb

@@ -19,50 +19,96 @@
 namespace kb {
 namespace {
 
-template <bool STRICT, int QMODE, bool MULTI>
-__global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
-    using M = F<STRICT>;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const int r = MULTI ? rep_of_boid(a.reps, a.nrep, i) : 0;
-    const Rep R = a.reps[r];
+// Accumulate the candidates of one contiguous run [s, e) of the read
+// buffer, four at a time so their loads are in flight together.
+template <bool STRICT, bool NOWRAP>
+__device__ __forceinline__ void accumulate_run_t(const Rep& R, const float4* __restrict__ st,
+                                                 const uint32_t* __restrict__ ids, uint32_t s,
+                                                 uint32_t e, float4 me, uint32_t my_id,
+                                                 Acc<STRICT>& acc) {
+    acc.vec += e - s;
+    uint32_t q = s;
+    for (; q + 4 <= e; q += 4) {
+        uint32_t oid[4];
+        float4 o[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            oid[u] = __ldg(ids + q + u);
+            o[u] = __ldg(st + q + u);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (oid[u] != my_id) acc.template add<NOWRAP>(R, me.x, me.y, o[u]);
+    }
+    for (; q < e; ++q) {
+        const uint32_t oid = __ldg(ids + q);
+        const float4 o = __ldg(st + q);
+        if (oid != my_id) acc.template add<NOWRAP>(R, me.x, me.y, o);
+    }
+}
+template <bool STRICT>
+__device__ __forceinline__ void accumulate_run(const Rep& R, const float4* __restrict__ st,
+                                               const uint32_t* __restrict__ ids, uint32_t s,
+                                               uint32_t e, float4 me, uint32_t my_id,
+                                               Acc<STRICT>& acc) {
+    if (R.nowrap) accumulate_run_t<STRICT, true>(R, st, ids, s, e, me, my_id, acc);
+    else accumulate_run_t<STRICT, false>(R, st, ids, s, e, me, my_id, acc);
+}
+
+template <bool STRICT, int QMODE>
+__device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uint32_t i) {
     const unsigned long long step = *a.step;
-    const float4 me = a.st[i];
-    const uint32_t my_id = a.ids[i];
+    const float4 me = __ldg(a.st + i);
+    const uint32_t my_id = __ldg(a.ids + i);
 
     Acc<STRICT> acc;
     int mi, Mi, mj, Mj;
     if (cell_range(R, me.x, me.y, R.dd, &mi, &Mi, &mj, &Mj)) {
-        for (int ci = mi; ci <= Mi; ++ci) {
-            const int bx = t_transform(ci, R.max_x);
-            const uint32_t colbase = R.cell_off + (uint32_t)bx * (uint32_t)R.dh;
-            if (QMODE == 0 && R.toroidal) {
-                // clamped range: the column's bags mj..Mj are one contiguous run
-                if (mj > Mj) continue;
-                const uint32_t s = a.start[colbase + mj], e = a.start[colbase + Mj + 1];
-                for (uint32_t k = s; k < e; ++k) {
-                    acc.vec += 1;
-                    if (a.ids[k] != my_id) acc.add(R, me.x, me.y, a.st[k]);
+        if (QMODE == 0 && R.toroidal && Mi - mi < 5) {
+            // clamped range: each column's bags mj..Mj are one contiguous
+            // run; fetch every run's bounds before touching candidates
+            if (mj <= Mj) {
+                uint32_t s[5], e[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    if (mi + k <= Mi) {
+                        const uint32_t colbase = R.cell_off + (uint32_t)(mi + k) * (uint32_t)R.dh;
+                        s[k] = __ldg(a.start + colbase + mj);
+                        e[k] = __ldg(a.start + colbase + Mj + 1);
+                    }
                 }
-            } else {
+#pragma unroll
+                for (int k = 0; k < 5; ++k)
+                    if (mi + k <= Mi) accumulate_run(R, a.st, a.ids, s[k], e[k], me, my_id, acc);
+            }
+        } else {
+            for (int ci = mi; ci <= Mi; ++ci) {
+                const int bx = t_transform(ci, R.max_x);
+                const uint32_t colbase = R.cell_off + (uint32_t)bx * (uint32_t)R.dh;
+                if (QMODE == 0 && R.toroidal) {
+                    if (mj > Mj) continue;
+                    accumulate_run(R, a.st, a.ids, __ldg(a.start + colbase + mj),
+                                   __ldg(a.start + colbase + Mj + 1), me, my_id, acc);
+                    continue;
+                }
                 for (int cj = mj; cj <= Mj; ++cj) {
                     const int by = t_transform(cj, R.max_y);
                     const uint32_t c = colbase + (uint32_t)by;
-                    const uint32_t s = a.start[c], e = a.start[c + 1];
+                    const uint32_t s = __ldg(a.start + c), e = __ldg(a.start + c + 1);
                     if (s == e) continue;
-                    int check = 1;
-                    if (QMODE == 1) {
-                        check = check_circle(bx, by, R, me.x, me.y, R.radius);
-                        if (check == -1) continue;
+                    if (QMODE == 0) {
+                        accumulate_run(R, a.st, a.ids, s, e, me, my_id, acc);
+                        continue;
                     }
+                    const int check = check_circle(bx, by, R, me.x, me.y, R.radius);
+                    if (check == -1) continue;
                     for (uint32_t k = s; k < e; ++k) {
-                        const float4 o = a.st[k];
-                        if (QMODE == 1 && check == 0 &&
-                            !(distance(me.x, me.y, o.x, o.y, R.w, R.h, R.toroidal != 0) <=
-                              R.radius))
+                        const float4 o = __ldg(a.st + k);
+                        if (check == 0 &&
+                            !(distance(me.x, me.y, o.x, o.y, R.w, R.h, R.toroidal != 0) <= R.radius))
                             continue;
                         acc.vec += 1;
-                        if (a.ids[k] != my_id) acc.add(R, me.x, me.y, o);
+                        if (__ldg(a.ids + k) != my_id) acc.add(R, me.x, me.y, o);
                     }
                 }
             }
@@ -70,10 +116,10 @@ __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
     }
 
     const float4 nxt = finish_bird<STRICT>(R, me, my_id, step, acc);
-    const float nx = nxt.x, ny = nxt.y, dx = nxt.z, dy = nxt.w;
-    a.out_st[i] = make_float4(nx, ny, dx, dy);
+    const float nx = nxt.x, ny = nxt.y;
+    a.out_st[i] = nxt;
     a.out_ids[i] = my_id;
-    const int32_t ncx = disc(nx, R.d), ncy = disc(ny, R.d);
+    const int32_t ncx = disc(nx, R), ncy = disc(ny, R);
     int64_t idx = bag_index(R, ncx, ncy);
     uint32_t flags = 0;
     if (idx < 0) {
@@ -83,7 +129,7 @@ __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
     if (!isfinite(nx) || !isfinite(ny)) flags |= ERR_NONFINITE;
     // the rebin gathers a bag's arrivals from the 3x3 old bags around it
     // (plus the seam columns/rows); anything else must take the general sort
-    const int32_t ocx = disc(me.x, R.d), ocy = disc(me.y, R.d);
+    const int32_t ocx = disc(me.x, R), ocy = disc(me.y, R);
     const bool okx = move_ok(ocx, ncx, R.seam), oky = move_ok(ocy, ncy, R.seam);
     if (a.check_moves && !(okx && oky)) flags |= ERR_REBIN_MISS | ERR_MISS_MOVE;
     if (flags) atomicOr(a.err, flags);
@@ -92,9 +138,21 @@ __global__ void __launch_bounds__(256) k_flock_force(ForceArgs a) {
     atomicAdd(&a.hist[key], 1u);
 }
 
+template <bool STRICT, int QMODE, bool MULTI>
+__global__ void __launch_bounds__(256, 4) k_flock_force(ForceArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    if (MULTI) {
+        const Rep R = a.reps[rep_of_boid(a.reps, a.nrep, i)];
+        force_body<STRICT, QMODE>(a, R, i);
+    } else {
+        force_body<STRICT, QMODE>(a, a.rep0, i);
+    }
+}
+
 // ---------------------------------------------------------- scan
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_ITEMS = 16;
 constexpr unsigned long long FLAG_AGG = 1ull, FLAG_INC = 2ull;
 constexpr uint32_t SPIN_LIMIT = 1u << 20;
 
@@ -120,13 +178,15 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     uint32_t v[SCAN_ITEMS];
     if (base + SCAN_ITEMS <= n) {
         const uint4* p = reinterpret_cast<const uint4*>(in + base);
-        uint4 a = p[0], b = p[1];
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS / 4; ++k) {
+            const uint4 w = p[k];
+            v[4 * k] = w.x; v[4 * k + 1] = w.y; v[4 * k + 2] = w.z; v[4 * k + 3] = w.w;
+        }
         if (zero_in) {
             uint4* q = reinterpret_cast<uint4*>(const_cast<uint32_t*>(in + base));
-            q[0] = make_uint4(0, 0, 0, 0);
-            q[1] = make_uint4(0, 0, 0, 0);
+#pragma unroll
+            for (int k = 0; k < SCAN_ITEMS / 4; ++k) q[k] = make_uint4(0, 0, 0, 0);
         }
     } else {
 #pragma unroll
@@ -160,49 +220,64 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     const uint32_t agg = s_warp[SCAN_THREADS / 32 - 1];
     const uint32_t texcl = x - tsum + (warp > 0 ? s_warp[warp - 1] : 0u);
 
-    // decoupled look-back across tiles
-    if (warp == 0) {
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            if (lane == 0) {
-                atomicExch(&tstate[0], pack_tile(epoch, FLAG_INC, agg));
-            }
-        } else {
-            if (lane == 0) atomicExch(&tstate[tile], pack_tile(epoch, FLAG_AGG, agg));
-            int64_t pred = (int64_t)tile - 1;
-            bool done = false;
-            while (!done) {
-                const int64_t j = pred - lane;
-                unsigned long long word = pack_tile(epoch, FLAG_INC, 0u);  // lanes past tile 0
-                if (j >= 0) {
-                    uint32_t spins = 0;
-                    while (true) {
-                        word = *((volatile unsigned long long*)&tstate[j]);
-                        const bool ready = (uint32_t)(word >> 34) == (epoch & 0x3FFFFFFFu) &&
-                                           ((word >> 32) & 3ull) != 0ull;
-                        if (ready) break;
-                        if (++spins > SPIN_LIMIT) {
-                            atomicOr(err, ERR_SPIN_TIMEOUT);
-                            word = pack_tile(epoch, FLAG_INC, 0u);
-                            break;
-                        }
-                        __nanosleep(32);
-                    }
-                }
-                const bool inc = ((word >> 32) & 3ull) == FLAG_INC;
-                const uint32_t incmask = __ballot_sync(0xffffffffu, inc);
-                uint32_t val = (uint32_t)word;
-                int stop = incmask ? (__ffs(incmask) - 1) : 32;  // nearest inclusive predecessor
-                if (lane > stop) val = 0u;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-                prefix += val;
-                if (incmask) done = true;
-                else pred -= 32;
-            }
-            if (lane == 0) atomicExch(&tstate[tile], pack_tile(epoch, FLAG_INC, prefix + agg));
+    // decoupled look-back across tiles, 256 predecessors per round trip
+    __shared__ int s_jinc;
+    __shared__ uint32_t s_sum[SCAN_THREADS / 32];
+    if (tile == 0) {
+        if (tid == 0) {
+            atomicExch(&tstate[0], pack_tile(epoch, FLAG_INC, agg));
+            s_prefix = 0;
         }
-        if (lane == 0) s_prefix = prefix;
+    } else {
+        if (tid == 0) {
+            atomicExch(&tstate[tile], pack_tile(epoch, FLAG_AGG, agg));
+            s_jinc = -0x7fffffff;
+        }
+        __syncthreads();
+        uint32_t prefix = 0;
+        int64_t pred = (int64_t)tile - 1;
+        for (;;) {
+            const int64_t j = pred - tid;
+            unsigned long long word = pack_tile(epoch, FLAG_INC, 0u);  // below tile 0
+            if (j >= 0) {
+                uint32_t spins = 0;
+                while (true) {
+                    word = *((volatile unsigned long long*)&tstate[j]);
+                    if ((uint32_t)(word >> 34) == (epoch & 0x3FFFFFFFu) && ((word >> 32) & 3ull) != 0ull)
+                        break;
+                    if (++spins > SPIN_LIMIT) {
+                        atomicOr(err, ERR_SPIN_TIMEOUT);
+                        word = pack_tile(epoch, FLAG_INC, 0u);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            const bool inc = ((word >> 32) & 3ull) == FLAG_INC;
+            // the nearest inclusive predecessor in this window: the smallest tid
+            if (inc) atomicMax(&s_jinc, -(int)tid);
+            __syncthreads();
+            const int stop = -s_jinc;  // tid of the nearest inclusive word, or huge
+            uint32_t v = ((int)tid <= stop) ? (uint32_t)word : 0u;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) s_sum[warp] = v;
+            __syncthreads();
+            uint32_t tot = 0;
+#pragma unroll
+            for (int w = 0; w < SCAN_THREADS / 32; ++w) tot += s_sum[w];
+            prefix += tot;
+            const bool done = stop < SCAN_THREADS;
+            __syncthreads();
+            if (done) break;
+            if (tid == 0) s_jinc = -0x7fffffff;
+            pred -= SCAN_THREADS;
+            __syncthreads();
+        }
+        if (tid == 0) {
+            atomicExch(&tstate[tile], pack_tile(epoch, FLAG_INC, prefix + agg));
+            s_prefix = prefix;
+        }
     }
     __syncthreads();
     const uint32_t prefix = s_prefix;
@@ -215,8 +290,9 @@ __global__ void __launch_bounds__(SCAN_THREADS)
             run += v[k];
         }
         uint4* p = reinterpret_cast<uint4*>(out + base);
-        p[0] = make_uint4(o[0], o[1], o[2], o[3]);
-        p[1] = make_uint4(o[4], o[5], o[6], o[7]);
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS / 4; ++k)
+            p[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
     } else {
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; ++k) {
@@ -239,53 +315,103 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 }
 
 // ---------------------------------------------------------- rebin
+// The arrivals of bag c in write-list order from the records [s, e).
+__device__ __forceinline__ void rebin_run(const RebinArgs& a, const Rep& R, uint32_t c, uint32_t s,
+                                          uint32_t e, uint32_t& dst, uint32_t end) {
+    for (uint32_t p = s; p < e; ++p) {
+        uint32_t k;
+        if (a.key) {
+            k = __ldg(a.key + p);
+        } else {  // key from the record's own position
+            const float4 r = __ldg(a.a_st + p);
+            const int64_t b = bag_index(R, disc(r.x, R), disc(r.y, R));
+            k = b >= 0 ? R.cell_off + (uint32_t)b : 0xFFFFFFFFu;
+        }
+        if (k == c) {
+            if (dst < end) {
+                a.s_st[dst] = __ldg(a.a_st + p);
+                a.s_ids[dst] = __ldg(a.a_ids + p);
+            }
+            ++dst;
+        }
+    }
+}
+
+__device__ __forceinline__ void rebin_cell(const RebinArgs& a, const Rep& R, uint32_t c) {
+    uint32_t dst = __ldg(a.start_next + c);
+    const uint32_t end = __ldg(a.start_next + c + 1);
+    if (dst == end) return;
+    const uint32_t local = c - R.cell_off;
+    const uint32_t Xu = div_dh(local, R);
+    const int X = (int)Xu, Y = (int)(local - Xu * (uint32_t)R.dh);
+    if (X > 0 && X < R.seam && Y > 0 && Y < R.seam) {
+        // interior bag: three source columns, rows Y-1..Y+1 contiguous in each
+        uint32_t s[3], e[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t base = R.cell_off + (uint32_t)(X - 1 + k) * (uint32_t)R.dh + (uint32_t)Y;
+            s[k] = __ldg(a.start_cur + base - 1);
+            e[k] = __ldg(a.start_cur + base + 2);
+        }
+        if (a.key) {
+            // the first keys of every run in flight together
+            uint32_t kk[3][4];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    kk[k][u] = (s[k] + u < e[k]) ? __ldg(a.key + s[k] + u) : 0xFFFFFFFFu;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (kk[k][u] == c) {
+                        if (dst < end) {
+                            a.s_st[dst] = __ldg(a.a_st + s[k] + u);
+                            a.s_ids[dst] = __ldg(a.a_ids + s[k] + u);
+                        }
+                        ++dst;
+                    }
+                }
+                if (s[k] + 4 < e[k]) rebin_run(a, R, c, s[k] + 4, e[k], dst, end);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) rebin_run(a, R, c, s[k], e[k], dst, end);
+        }
+    } else {
+        int lastx = -1;
+#pragma unroll 1
+        for (int kx = 0; kx < SRC_LINES; ++kx) {
+            const int sx = src_line(kx, X, R.max_x, R.seam);
+            if (sx < 0 || sx > R.max_x || sx <= lastx) continue;
+            lastx = sx;
+            const uint32_t colbase = R.cell_off + (uint32_t)sx * (uint32_t)R.dh;
+            int lasty = -1;
+#pragma unroll 1
+            for (int ky = 0; ky < SRC_LINES; ++ky) {
+                const int sy = src_line(ky, Y, R.max_y, R.seam);
+                if (sy < 0 || sy > R.max_y || sy <= lasty) continue;
+                lasty = sy;
+                rebin_run(a, R, c, __ldg(a.start_cur + colbase + sy),
+                          __ldg(a.start_cur + colbase + sy + 1), dst, end);
+            }
+        }
+    }
+    if (dst != end) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_MATERIALIZE);
+}
+
 template <bool MULTI>
 __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c == 0 && a.step != nullptr) *a.step += 1ull;
     if (c >= a.ncells) return;
-    uint32_t dst = a.start_next[c];
-    const uint32_t end = a.start_next[c + 1];
-    if (dst == end) return;
-    const int r = MULTI ? rep_of_cell(a.reps, a.nrep, c) : 0;
-    const Rep R = a.reps[r];
-    const uint32_t local = c - R.cell_off;
-    const int X = (int)(local / (uint32_t)R.dh), Y = (int)(local % (uint32_t)R.dh);
-    int lastx = -1;
-#pragma unroll 1
-    for (int kx = 0; kx < SRC_LINES; ++kx) {
-        const int sx = src_line(kx, X, R.max_x, R.seam);
-        if (sx < 0 || sx > R.max_x || sx <= lastx) continue;
-        lastx = sx;
-        const uint32_t colbase = R.cell_off + (uint32_t)sx * (uint32_t)R.dh;
-        int lasty = -1;
-#pragma unroll 1
-        for (int ky = 0; ky < SRC_LINES; ++ky) {
-            const int sy = src_line(ky, Y, R.max_y, R.seam);
-            if (sy < 0 || sy > R.max_y || sy <= lasty) continue;
-            lasty = sy;
-            const uint32_t s = a.start_cur[colbase + sy];
-            const uint32_t e = a.start_cur[colbase + sy + 1];
-            for (uint32_t p = s; p < e; ++p) {
-                uint32_t k;
-                if (a.key) {
-                    k = a.key[p];
-                } else {  // key from the record's own position
-                    const float4 r = a.a_st[p];
-                    const int64_t b = bag_index(R, disc(r.x, R.d), disc(r.y, R.d));
-                    k = b >= 0 ? R.cell_off + (uint32_t)b : 0xFFFFFFFFu;
-                }
-                if (k == c) {
-                    if (dst < end) {
-                        a.s_st[dst] = a.a_st[p];
-                        a.s_ids[dst] = a.a_ids[p];
-                    }
-                    ++dst;
-                }
-            }
-        }
+    if (MULTI) {
+        const Rep R = a.reps[rep_of_cell(a.reps, a.nrep, c)];
+        rebin_cell(a, R, c);
+    } else {
+        rebin_cell(a, a.rep0, c);
     }
-    if (dst != end) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_MATERIALIZE);
 }
 
 // ---------------------------------------------------------- general sort
@@ -341,7 +467,7 @@ __global__ void k_query(QueryArgs a) {
     const uint64_t off = fill ? a.offsets[q] : 0;
     uint32_t cnt = 0, dig = 0;
     int mi, Mi, mj, Mj;
-    const int32_t dd = (a.dist <= 0.0f) ? -1 : disc(a.dist, R.d);
+    const int32_t dd = (a.dist <= 0.0f) ? -1 : disc(a.dist, R);
     if (cell_range(R, p.x, p.y, dd, &mi, &Mi, &mj, &Mj)) {
         for (int ci = mi; ci <= Mi; ++ci) {
             const int bx = t_transform(ci, R.max_x);
@@ -515,7 +641,7 @@ __global__ void k_repack(const PackEntry* __restrict__ plan, int32_t nplan, uint
         id = k;
         gen_uniform_boid(k, e.seed_lo, e.seed_hi, R.w, R.h, e.heading_scale, &st);
     }
-    const int64_t b = bag_index(R, disc(st.x, R.d), disc(st.y, R.d));
+    const int64_t b = bag_index(R, disc(st.x, R), disc(st.y, R));
     if (b < 0) atomicOr(err, ERR_KEY_RANGE);
     dst_st[i] = st;
     dst_ids[i] = id;

@@ -18,7 +18,7 @@ struct ScanCtl {
     uint32_t epoch;
     uint32_t _pad;
 };
-constexpr uint32_t SCAN_TILE = 2048;  // items per CTA (256 threads x 8)
+constexpr uint32_t SCAN_TILE = 4096;  // items per CTA (256 threads x 16)
 inline uint32_t scan_tiles(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
 
 // Exclusive scan of in[0..n) into out[0..n]; out[n] = total.  When zero_in,
@@ -33,6 +33,7 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
 struct ForceArgs {
     const Rep* reps;
     int32_t nrep;
+    Rep rep0;  // the single replica, read from the parameter bank when nrep == 1
     const float4* st;
     const uint32_t* ids;
     const uint32_t* start;
@@ -54,6 +55,7 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
 struct RebinArgs {
     const Rep* reps;
     int32_t nrep;
+    Rep rep0;  // the single replica when nrep == 1
     const uint32_t* start_cur;
     const uint32_t* start_next;
     const uint32_t* key;

@@ -247,10 +247,12 @@ class Field2D:
                C.c_size_t(len(q)), L.fptr(q), L.uptr(counts), L.uptr(dig))
         return counts[: len(q)], dig[: len(q)]
 
-    def set_step_options(self, fused: bool = True, tile_tx: int = 0, tile_ty: int = 0) -> None:
-        """Persistent fused step on/off and its tile shape (0 = automatic)."""
-        L.call("kb_field_set_step_options", self._h, C.c_int32(1 if fused else 0),
-               C.c_int32(tile_tx), C.c_int32(tile_ty))
+    def set_step_options(self, mode=2, tile_tx: int = 0, tile_ty: int = 0) -> None:
+        """Step path: 2 tiled split (default), 1 persistent, 0 separate kernels
+        (True/False mean 2/0); tile shape in bags (0 = automatic)."""
+        mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)
+        L.call("kb_field_set_step_options", self._h, C.c_int32(mode), C.c_int32(tile_tx),
+               C.c_int32(tile_ty))
 
     def autotune(self, params, first_step: int, steps_per_trial: int = 5, candidates=None):
         """Pick the fastest fused tile shape by timing real steps; returns

@@ -34,11 +34,13 @@ def oracle_run(rep, nsteps):
     return ids, st
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("grouping", [(0, 0), (1, 0), (1, 4), (3, 2)])
-def test_batch_replicas_match_oracle(gpu, grouping):
+def test_batch_replicas_match_oracle(gpu, grouping, mode):
     spl, graphs = grouping
     reps = small_sweep(kg.KB_ARITH_STRICT)
     b = kg.Batch(reps)
+    b.set_step_options(mode)
     b.step(0, 12, spl, graphs)
     b.step(12, 9, spl, graphs)
     for i, rep in enumerate(reps):

@@ -103,15 +103,16 @@ def test_compute_plus_lazy_update_equals_fused_steps(gpu):
     assert np.array_equal(ia, ib) and same_bits(sa, sb)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("tile", [(0, 0), (1, 1), (4, 4), (16, 8), (64, 128)])
 @pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
-def test_fused_tiles_match_oracle(gpu, tile, kind):
+def test_fused_tiles_match_oracle(gpu, tile, kind, mode):
     # every tile shape gives the oracle's trajectory bit for bit; 64x128-bag
     # tiles exceed the shared-memory capacity and run the global scratch path
     n, side = 6000, 490.0
     ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 21, 1.0)
     f = gpu_field(side, C1_D, ids0, xy0, dxy0)
-    f.set_step_options(True, *tile)
+    f.set_step_options(mode, *tile)
     o = oracle_field(side, C1_D, ids0, xy0, dxy0)
     p = kg.FlockParams(seed=5, query_mode=kind)
     step(f, p, 0, 7)
@@ -126,16 +127,18 @@ def test_fused_tiles_match_oracle(gpu, tile, kind):
         assert stats["overflow_tiles"] > 0
 
 
-def test_fused_equals_separate_kernels(gpu):
+def test_step_modes_agree(gpu):
     ids0, xy0, dxy0 = kg.gen_uniform(50000, 1400.0, 1400.0, 8, 1.0)
     p = kg.FlockParams(seed=2, arith=kg.KB_ARITH_FAST)
     out = []
-    for fused in (True, False):
+    for mode in (0, 1, 2):
         f = gpu_field(1400.0, C1_D, ids0, xy0, dxy0)
-        f.set_step_options(fused)
+        f.set_step_options(mode)
         step(f, p, 0, 40)
+        step(f, p, 40, 3)
         out.append(f.get_state())
-    assert np.array_equal(out[0][0], out[1][0]) and same_bits(out[0][1], out[1][1])
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0]) and same_bits(out[0][1], o[1])
 
 
 def test_fused_sweep_radius_two_rings(gpu):
@@ -164,7 +167,7 @@ def test_seam_geometries_match_oracle(gpu, side, d, jump, radius):
     xy0[: n // 4, 0] = np.float32(side) - (xy0[: n // 4, 0] % np.float32(1.5))
     xy0[n // 4: n // 2, 1] = xy0[n // 4: n // 2, 1] % np.float32(1.5)
     p = kg.FlockParams(seed=4, jump=jump, neighbor_radius=radius)
-    for fused in (True, False):
+    for fused in (2, 1, 0):
         f = gpu_field(side, d, ids0, xy0, dxy0)
         f.set_step_options(fused)
         o = oracle_field(side, d, ids0, xy0, dxy0)
@@ -242,22 +245,35 @@ def _order_and_neighbours(f, jump):
     return local.mean(), counts.mean()
 
 
+def _ensemble(arith, seeds, jitter_base, n, side):
+    vals = []
+    for seed in seeds:
+        ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 100 + seed, 1.0)
+        f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+        step(f, kg.FlockParams(seed=jitter_base + seed, arith=arith), 0, 200)
+        vals.append(_order_and_neighbours(f, 0.7))
+        f.close()
+    return np.array(vals)
+
+
 def test_long_run_statistics_fast_vs_strict(gpu):
-    # C1-density flocks (0.025 boids per unit^2), 200 steps, 12 seeds of
-    # 10,000 boids: the ensemble means of both statistics agree within 1%.
-    res = {kg.KB_ARITH_STRICT: [], kg.KB_ARITH_FAST: []}
-    side = float(np.sqrt(10000 / 0.025))
-    for seed in range(12):
-        ids0, xy0, dxy0 = kg.gen_uniform(10000, side, side, 100 + seed, 1.0)
-        for arith in res:
-            f = gpu_field(side, C1_D, ids0, xy0, dxy0)
-            step(f, kg.FlockParams(seed=seed, arith=arith), 0, 200)
-            res[arith].append(_order_and_neighbours(f, 0.7))
-    s = np.array(res[kg.KB_ARITH_STRICT]).mean(0)
-    q = np.array(res[kg.KB_ARITH_FAST]).mean(0)
-    print("strict (order, neighbours):", s, "fast:", q)
-    assert abs(q[0] - s[0]) / s[0] < 0.01, (q, s)
-    assert abs(q[1] - s[1]) / s[1] < 0.01, (q, s)
+    """Flocks at the C1 density (0.025 boids per unit^2), 200 steps, 32
+    initial flocks of 20,000 boids: the ensemble means of the local order
+    parameter and of the mean neighbour count under the fast arithmetic agree
+    with the strict ones within 1%.  Chaos makes the two runs independent
+    samples after a few dozen steps, so the same comparison of strict against
+    strict with another jitter seed is printed as the noise floor."""
+    n = 20000
+    side = float(np.sqrt(n / 0.025))
+    seeds = range(32)
+    strict = _ensemble(kg.KB_ARITH_STRICT, seeds, 0, n, side)
+    fast = _ensemble(kg.KB_ARITH_FAST, seeds, 0, n, side)
+    control = _ensemble(kg.KB_ARITH_STRICT, seeds, 1000, n, side)
+    s, q, c = strict.mean(0), fast.mean(0), control.mean(0)
+    se = strict.std(0, ddof=1) / np.sqrt(len(strict))
+    print("strict", s, "fast", q, "strict/other jitter", c, "standard error", se)
+    assert abs(q[0] - s[0]) / s[0] < 0.01, (q, s, c, se)
+    assert abs(q[1] - s[1]) / s[1] < 0.01, (q, s, c, se)
 
 
 def test_c2_full_size_one_step(gpu):
