@@ -204,6 +204,21 @@ kb_status kb_field_neighbor_lists(kb_field* f, int32_t kind, float dist, size_t 
 kb_status kb_field_neighbor_digest(kb_field* f, int32_t kind, float dist, size_t nq,
                                    const float* qxy, uint32_t* counts, uint32_t* digest);
 
+/* No counterpart in the reference.  kb_field_neighbor_digest for hosts that
+ * cannot allocate device memory when they query: one whose own pools hold the
+ * rest of the device's memory, or one that must not stall other streams with
+ * the device-wide synchronisation of cudaFree.  It makes no cudaMalloc,
+ * cudaFree or other allocating call: query points, counts and digests are
+ * staged in one fixed device array of KB_NOALLOC_MAX_QUERIES x 16 bytes
+ * (1 MiB) per device, shared by every call on that device.  nq above
+ * KB_NOALLOC_MAX_QUERIES returns KB_ERR_ARG.  Calls whose GPU work overlaps
+ * (two host threads, fields on the same device) race on that array.  The
+ * first call on a device sets the array up for that device
+ * (cudaGetSymbolAddress); make it before any stream capture on the device. */
+#define KB_NOALLOC_MAX_QUERIES 65536
+kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind, float dist, size_t nq,
+                                           const float* qxy, uint32_t* counts, uint32_t* digest);
+
 /* ------------------------------------------------------ batched replicas */
 /* Many independent Flockers simulations (the model-exploration workload of
  * explore_parallel!, src/explore/model_exploration.rs:354-432: one

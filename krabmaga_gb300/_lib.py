@@ -27,6 +27,7 @@ KB_QUERY_RELAX = 0
 KB_QUERY_EXACT = 1
 KB_ARITH_STRICT = 0
 KB_ARITH_FAST = 1
+KB_NOALLOC_MAX_QUERIES = 65536
 
 STATUS_NAMES = {
     0: "KB_OK", 1: "KB_ERR_ARG", 2: "KB_ERR_OOM", 3: "KB_ERR_CUDA", 4: "KB_ERR_TIMEOUT",
@@ -165,6 +166,8 @@ _SIGS = {
     "kb_field_neighbor_lists": (
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32, C.c_size_t, _SZ]),
     "kb_field_neighbor_digest": (
+        C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
+    "kb_field_neighbor_digest_noalloc": (
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
     "kb_batch_create": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(ReplicaDesc), C.POINTER(_P)]),
     "kb_batch_destroy": (C.c_int32, [_P]),

@@ -870,6 +870,24 @@ kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
 
 }  // namespace
 
+namespace kb {
+// The field's device and its read buffer as query arguments, for query
+// launches made by other translation units (kb_noalloc.cu).  Materialises the
+// read buffer; the caller has made the field's device current.
+int field_device(const kb_field* f) { return f->device; }
+kb_status field_query_view(kb_field* f, int32_t kind, float dist, QueryArgs* a, cudaStream_t* s) {
+    if (kb_status st = materialize(f)) return st;
+    a->rep = f->rep;
+    a->kind = kind;
+    a->dist = dist;
+    a->start = f->start[f->cur].p;
+    a->st = f->rst.p;
+    a->ids = f->rid.p;
+    *s = f->stream;
+    return KB_OK;
+}
+}  // namespace kb
+
 extern "C" {
 
 kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
