@@ -57,6 +57,20 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def ncu_traffic(kernel):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
+    summary of the same workload (profiles/<kernel>_c2.md, a line
+    `dram_bytes_per_launch: <int>`), or None when there is none."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_c2.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        for ln in fh:
+            if ln.startswith("dram_bytes_per_launch:"):
+                return int(ln.split(":", 1)[1].strip())
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
 
@@ -165,9 +179,9 @@ def cpu_reference(wl, steps):
 def run_sweep(args, dev):
     """Batched exploration sweep: `sweep_reps` replicas (N log-uniform over
     [1024, 65536] at density 0.025, per-replica weights/jump/radius, seed =
-    replica index), `sweep_steps` steps as CUDA graphs of 100 launches of one
-    persistent step each, tile shape from the autotuner; against running the
-    plain path replica by replica on the same GPU."""
+    replica index), `sweep_steps` steps of all replicas together, in the
+    tiled mode (tile shape from the autotuner) and the separate-kernel mode;
+    against running the plain field replica by replica on the same GPU."""
     import torch
 
     import krabmaga_gb300 as kg
@@ -176,32 +190,46 @@ def run_sweep(args, dev):
     reps = kg.sweep_replicas(args.sweep_reps)
     total = sum(r.n for r in reps)
     steps = args.sweep_steps
-    b = kg.Batch(reps, device=dev)
-    b.set_step_options(args.mode)
-    tx, ty, used, tune_ms = b.autotune(0, 4)
-    step = used
-    b.step(step, 10, 1, 0)
-    step += 10
-    b.synchronize()
-    stream = torch.cuda.ExternalStream(b.cuda_stream(), device=dev)
+
+    def batched(mode):
+        b = kg.Batch(reps, device=dev)
+        b.set_step_options(mode)
+        tx = ty = 0
+        tune_ms = None
+        step = 0
+        if mode in (1, 2):
+            tx, ty, used, tune_ms = b.autotune(0, 4)
+            step = used
+        b.step(step, 10, 1, 0)
+        step += 10
+        b.synchronize()
+        stream = torch.cuda.ExternalStream(b.cuda_stream(), device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(step, steps, 1, 100)  # one launch group per step, 100-step graphs
+        e1.record(stream)
+        b.synchronize()
+        bs = e0.elapsed_time(e1) / 1e3
+        step += steps
+        one = None
+        if mode == 1:
+            e0.record(stream)
+            b.step(step, steps, steps, 0)  # all steps in one persistent launch
+            e1.record(stream)
+            b.synchronize()
+            one = total * steps / (e0.elapsed_time(e1) / 1e3)
+        stats = b.step_stats()
+        b.close()
+        return {"mode": mode, "value": total * steps / bs, "ms_per_step": 1e3 * bs / steps,
+                "autotuned_tile": [tx, ty], "autotune_ms_per_step": tune_ms, "fused": stats,
+                "one_launch_value": one}
+
+    runs = [batched(m) for m in (2, 0)]
+    best = max(runs, key=lambda r: r["value"])
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    b.step(step, steps, 1, 100)  # one persistent launch per step, 100-launch graphs
-    e1.record(stream)
-    b.synchronize()
-    batched_s = e0.elapsed_time(e1) / 1e3
-    step += steps
-    e0.record(stream)
-    b.step(step, steps, steps, 0)  # all steps in one persistent launch
-    e1.record(stream)
-    b.synchronize()
-    one_launch_s = e0.elapsed_time(e1) / 1e3
-    stats = b.step_stats()
-    b.close()
     plain_s = 0.0
-    for r in reps:
+    for r in reps:  # the plain field's default (fastest) step path
         f = kg.Field2D(r.width, r.height, r.discretization, True, device=dev, capacity_hint=r.n)
-        f.set_step_options(args.mode)
         f.set_locations(*r.state)
         f.lazy_update()
         pc = r.params.to_c()
@@ -214,17 +242,17 @@ def run_sweep(args, dev):
         f.synchronize()
         plain_s += e0.elapsed_time(e1) / 1e3
         f.close()
-    bv = total * steps / batched_s
+    bv = best["value"]
     pv = total * steps / plain_s
     return {
         "workload": f"{args.sweep_reps} Flockers replicas, N log-uniform [1024, 65536] "
                     f"(total {total}), density 0.025, per-replica weights/jump/radius, "
                     f"{steps} steps",
         "batched_value": bv, "plain_replica_by_replica_value": pv, "speedup": bv / pv,
-        "one_launch_value": total * steps / one_launch_s, "unit": UNIT,
-        "batched_ms_per_step": 1e3 * batched_s / steps,
-        "launch": "one persistent launch per step, CUDA graphs of 100 launches",
-        "autotuned_tile": [tx, ty], "autotune_ms_per_step": tune_ms, "fused": stats,
+        "unit": UNIT, "batched_ms_per_step": best["ms_per_step"], "best_mode": best["mode"],
+        "modes": runs,
+        "launch": "mode 2: tile step + scan per step; mode 0: force + scan + rebin per step over "
+                  "all replicas; CUDA graphs of 100 steps",
         "data": "synthetic (seeded)", "l2": "working set larger than L2 (no flush)",
     }
 
@@ -344,6 +372,9 @@ def run_ours(args, wl):
 
     K = args.steps
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
+    if args.mode == 0:
+        f.kernel_times()  # drop anything recorded before the timed region
+        f.set_kernel_timing(True)
     barrier(ws)
     torch.cuda.synchronize(dev)
     with ClockSampler(dev) as clk:
@@ -358,7 +389,10 @@ def run_ours(args, wl):
     f.synchronize()  # raises if a kernel set the device error word
     barrier(ws)
     step_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
-    force_ms = step_ms
+    kernel_ms, kernel_steps = (None, 0)
+    if args.mode == 0:
+        kernel_ms, kernel_steps = f.kernel_times()
+        f.set_kernel_timing(False)
     total_s = allmax(ws, sum(step_ms) / 1e3)
     value = ws * n * K / total_s
     stats = f.step_stats()
@@ -409,9 +443,26 @@ def run_ours(args, wl):
         return
     hbm, peak_kind = peaks()
     ncells = (int(np.ceil(np.float32(side) / np.float32(D_C))) + 1) ** 2
-    step_bytes = n * 32 + ncells * 8  # state read+write per boid, bag offsets write+read
-    force_s = statistics.mean(force_ms) / 1e3
-    achieved = step_bytes / force_s / 1e9
+    # algorithmic bytes (each record, key and offset touched once)
+    step_bytes = n * 32 + ncells * 8  # whole step: state read+write per boid, bag offsets
+    force_bytes = n * 44 + ncells * 8  # record in 20, record + key out 24; offsets in, counts out
+    scan_bytes = ncells * 8            # counts in, offsets out
+    rebin_bytes = n * 44 + ncells * 8  # key + record in 24, record out 20; two offset arrays
+    kernels = None
+    if kernel_ms is not None and kernel_steps == K:
+        fm, sm, rm = (v / K for v in kernel_ms)
+        kernels = {
+            "k_flock_force": {"ms_mean": fm, "bytes": force_bytes, "gbs": force_bytes / fm / 1e6},
+            "k_scan": {"ms_mean": sm, "bytes": scan_bytes, "gbs": scan_bytes / sm / 1e6},
+            "k_rebin": {"ms_mean": rm, "bytes": rebin_bytes, "gbs": rebin_bytes / rm / 1e6},
+        }
+        kname, kbytes, kms = "k_flock_force", force_bytes, fm
+    else:  # tiled modes: the whole step is the measured unit
+        kname = {2: "k_tile_step + k_scan (two launches per step)",
+                 1: "k_fused (whole step, one launch)", 0: "whole step"}[args.mode]
+        kbytes, kms = step_bytes, statistics.mean(step_ms)
+    achieved = kbytes / kms / 1e6
+    traffic = ncu_traffic(kname) if kernels else None
     clocks = clk.summary()
 
     sweep = run_sweep(args, dev) if (args.sweep_reps > 0 and ws == 1) else None
@@ -431,15 +482,14 @@ def run_ours(args, wl):
                    "parallelism": f"replicas{ws}", "arith": args.arith, "query": "relax",
                    "l2": "flushed (512 MiB write) before every timed step",
                    "warm_l2_value": warm_value},
-        "roofline": {"bound": "hbm",
-                     "kernel": {2: "k_tile_step + k_scan (two launches per step)",
-                                1: "k_fused (whole step, one launch)",
-                                0: "k_flock_force + k_scan + k_rebin"}[args.mode],
+        "roofline": {"bound": "hbm", "kernel": kname,
                      "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
-                     "algorithmic_bytes_per_launch": step_bytes,
-                     "launch_ms_mean": statistics.mean(step_ms),
-                     "launch_ms_median": statistics.median(step_ms),
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": kbytes, "launch_ms_mean": kms,
+                     "kernels": kernels,
+                     "step_bytes": step_bytes, "step_ms_mean": statistics.mean(step_ms),
+                     "step_ms_median": statistics.median(step_ms),
+                     "step_frac": step_bytes / (statistics.mean(step_ms) / 1e3) / 1e9 / hbm,
                      "fused": stats, "autotuned": tuned},
         "cpu_baseline": cpu,
         "clocks": clocks,
@@ -469,7 +519,7 @@ def main():
     ap.add_argument("--e2e-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile", default="0x0", help="fused tile shape TXxTY in bags (0x0: automatic)")
-    ap.add_argument("--mode", type=int, default=2,
+    ap.add_argument("--mode", type=int, default=0,
                     help="step path: 2 tiled split (default), 1 persistent, 0 separate kernels")
     ap.add_argument("--profile", action="store_true", help="short plain run for ncu, no timing")
     ap.add_argument("--sweep-reps", type=int, default=512)

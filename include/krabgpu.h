@@ -159,13 +159,22 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
 kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                         uint32_t nsteps);
 /* Step implementation options (no reference counterpart; tuning only).
- * mode (the `fused` argument) for eligible fields (toroidal, square,
- * jump < discretization): 2 (default) the tiled step as two launches per
- * step (stage + rebin + force per tile, then the bag-offset scan), replayed
- * from CUDA graphs; 1 the same tiles in one persistent cooperative launch;
- * 0 the separate force / scan / rebin kernels.  tile_tx x tile_ty bags per
- * tile (0 = automatic). */
+ * mode (the `fused` argument): 0 (default) the separate force / scan / rebin
+ * kernels (a plain field replays runs of 4 steps or more from CUDA graphs);
+ * for eligible fields (toroidal, square, jump < discretization) 2 the tiled
+ * step as two launches per step (stage + rebin + force per tile, then the
+ * bag-offset scan) and 1 the same tiles in one persistent cooperative launch.
+ * tile_tx x tile_ty bags per tile (0 = automatic).  All modes give the same
+ * bits, in both arithmetic modes. */
 kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty);
+/* Per-kernel timing (no reference counterpart; measurement only).  While
+ * enabled, every separate-kernel step that is not replayed from a graph (a
+ * kb_flock_step call of fewer than 4 steps) records CUDA events around its
+ * three launches on the field's stream.  kb_field_kernel_times waits for
+ * them, returns the summed milliseconds of {force, scan, rebin} and the
+ * number of steps timed, and starts a new tally. */
+kb_status kb_field_set_kernel_timing(kb_field* f, int32_t enable);
+kb_status kb_field_kernel_times(kb_field* f, double ms[3], uint64_t* steps);
 /* Counters of the fused step: out4 = {tiles that ran through the global
  * scratch path (cumulative), tiles per step, CTAs, tx << 16 | ty}. */
 kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]);

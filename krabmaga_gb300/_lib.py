@@ -158,6 +158,8 @@ _SIGS = {
     "kb_flock_compute": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64]),
     "kb_field_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "kb_field_step_stats": (C.c_int32, [_P, _U32]),
+    "kb_field_set_kernel_timing": (C.c_int32, [_P, C.c_int32]),
+    "kb_field_kernel_times": (C.c_int32, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "kb_field_phase_clocks": (C.c_int32, [_P, C.c_int32, C.POINTER(C.c_uint64)]),
     "kb_flock_step": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_uint32]),
     "kb_field_get_state": (C.c_int32, [_P, _U32, _F, C.c_size_t, _SZ]),

@@ -75,8 +75,8 @@ class Batch:
         L.call("kb_batch_cuda_stream", self._h, C.byref(s))
         return s.value or 0
 
-    def set_step_options(self, mode=2, tile_tx: int = 0, tile_ty: int = 0) -> None:
-        """Step path: 2 tiled split (default), 1 persistent, 0 separate kernels."""
+    def set_step_options(self, mode=0, tile_tx: int = 0, tile_ty: int = 0) -> None:
+        """Step path: 0 separate kernels (default), 2 tiled split, 1 persistent."""
         mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)
         L.call("kb_batch_set_step_options", self._h, C.c_int32(mode), C.c_int32(tile_tx),
                C.c_int32(tile_ty))

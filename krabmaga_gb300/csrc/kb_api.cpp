@@ -205,7 +205,16 @@ struct kb_field {
         FusedCfg occ_cfg{};
         int occ_strict = -1, occ_qmode = -1, occ_ctas = 0;
     } fused;
-    int fused_mode = 2;  // 0 separate kernels, 1 persistent fused, 2 split tile step (default)
+    int fused_mode = 0;  // 0 separate kernels, 1 persistent fused, 2 split tile step
+    // Per-kernel timing of ungraphed separate-kernel steps: four events per
+    // step (force | scan | rebin), read and recycled by kb_field_kernel_times.
+    bool ktime = false;
+    struct KtStep {
+        cudaEvent_t ev[4];
+    };
+    std::vector<cudaEvent_t> kt_pool;
+    std::vector<KtStep> kt_pending;
+    int kt_cur = -1;  // step whose scan|rebin boundary fast_rebuild records
     // After fused steps the read buffer can stay virtual: the last write list
     // (in buffer a_last: 0 rst, 1 wst, 2 tst) plus start[1-cur] (its bag
     // offsets) and start[cur] (the read buffer's bag offsets).
@@ -216,6 +225,10 @@ struct kb_field {
 
     ~kb_field() {
         drop_graphs();
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto& k : kt_pending)
+            for (cudaEvent_t e : k.ev) cudaEventDestroy(e);
+        for (cudaEvent_t e : kt_pool) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
     void drop_graphs() {
@@ -380,6 +393,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     cudaStream_t s = f->stream;
     const int nxt = 1 - f->cur;
     KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    if (f->kt_cur >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[f->kt_cur].ev[2], s));
     RebinArgs a;
     a.reps = f->d_rep.p;
     a.nrep = nrep(f);
@@ -1390,13 +1404,44 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
 }
 
 // Enqueue nsteps steps (force + rebuild) directly on the stream.
+// Four timing events for one separate-kernel step, or -1 (timing off, the
+// general rebuild, or the stream is being captured into a graph).
+static int kt_begin(kb_field* f, bool fast) {
+    if (!f->ktime || !fast) return -1;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(f->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return -1;
+    kb_field::KtStep k;
+    for (int i = 0; i < 4; ++i) {
+        if (f->kt_pool.empty()) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreate(&e) != cudaSuccess) {
+                cudaGetLastError();
+                for (int j = 0; j < i; ++j) f->kt_pool.push_back(k.ev[j]);
+                return -1;
+            }
+            f->kt_pool.push_back(e);
+        }
+        k.ev[i] = f->kt_pool.back();
+        f->kt_pool.pop_back();
+    }
+    f->kt_pending.push_back(k);
+    return (int)f->kt_pending.size() - 1;
+}
+
 static kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps, bool fast) {
     for (uint32_t s = 0; s < nsteps; ++s) {
+        const int t = kt_begin(f, fast);
+        if (t >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[t].ev[0], f->stream));
         kb_status st = enqueue_force(f, p);
         if (st) return st;
+        if (t >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[t].ev[1], f->stream));
         f->wn = f->rn;
+        f->kt_cur = t;
         st = fast ? fast_rebuild(f, true) : general_rebuild(f, true);
+        f->kt_cur = -1;
         if (st) return st;
+        if (t >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[t].ev[3], f->stream));
         if (!fast) KB_CUDA(launch_add_u64(f->dstep.p, 1ull, f->stream));
         f->wn = 0;
     }
@@ -1477,6 +1522,35 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
         done += k;
     }
     return KB_OK;
+}
+
+kb_status kb_field_set_kernel_timing(kb_field* f, int32_t enable) {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    f->ktime = enable != 0;
+    return KB_OK;
+}
+
+kb_status kb_field_kernel_times(kb_field* f, double ms[3], uint64_t* steps) {
+    if (!f || !ms || !steps) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    ms[0] = ms[1] = ms[2] = 0.0;
+    *steps = 0;
+    kb_status st = KB_OK;
+    for (auto& k : f->kt_pending) {
+        cudaError_t e = cudaEventSynchronize(k.ev[3]);
+        float t[3] = {0.f, 0.f, 0.f};
+        for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaEventElapsedTime(&t[i], k.ev[i], k.ev[i + 1]);
+        if (e != cudaSuccess) {
+            if (!st) st = cuda_fail(e, "kernel timing events");
+            cudaGetLastError();
+        } else {
+            for (int i = 0; i < 3; ++i) ms[i] += t[i];
+            ++*steps;
+        }
+        for (cudaEvent_t ev : k.ev) f->kt_pool.push_back(ev);
+    }
+    f->kt_pending.clear();
+    return st;
 }
 
 kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,

@@ -42,12 +42,16 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
     return r;
 }
 
+// The fast arithmetic spells out every rounding too (fused multiply-adds
+// only where written as __fmaf_rn), so the compiler cannot contract the same
+// expression differently in different kernels: every step path gives the
+// same bits in fast mode as well.
 template <>
 struct F<false> {
-    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
-    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
-    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
-    static __device__ __forceinline__ float div(float a, float b) { return a * rcp_approx(b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fmul_rn(a, rcp_approx(b)); }
     static __device__ __forceinline__ float sqrt(float a) { return sqrt_approx(a); }
 };
 
@@ -194,15 +198,16 @@ struct Acc {
     __device__ __forceinline__ void add_d(float dx, float dy, float4 o) {
         using M = F<STRICT>;
         count += 1;
-        float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
-        float q = M::add(M::mul(sq, sq), 1.0f);
         if (STRICT) {
+            float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
+            float q = M::add(M::mul(sq, sq), 1.0f);
             xa = M::add(xa, M::div(dx, q));
             ya = M::add(ya, M::div(dy, q));
         } else {
-            const float inv = rcp_approx(q);
-            xa = xa + dx * inv;
-            ya = ya + dy * inv;
+            const float sq = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+            const float inv = rcp_approx(__fmaf_rn(sq, sq, 1.0f));
+            xa = __fmaf_rn(dx, inv, xa);
+            ya = __fmaf_rn(dy, inv, ya);
         }
         xc = M::add(xc, dx);
         yc = M::add(yc, dy);
@@ -241,9 +246,11 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
         float xa = acc.xa, ya = acc.ya, xc = acc.xc, yc = acc.yc, xs = acc.xs, ys = acc.ys;
         if (acc.count > 0 && !STRICT) {
             const float ic = rcp_approx((float)acc.count);
-            xa *= ic; ya *= ic; xc *= ic; yc *= ic; xs *= ic; ys *= ic;
-            csx = xs * ic;  // bird.rs:91-94: a second division by count
-            csy = ys * ic;
+            xa = __fmul_rn(xa, ic); ya = __fmul_rn(ya, ic);
+            xc = __fmul_rn(xc, ic); yc = __fmul_rn(yc, ic);
+            xs = __fmul_rn(xs, ic); ys = __fmul_rn(ys, ic);
+            csx = __fmul_rn(xs, ic);  // bird.rs:91-94: a second division by count
+            csy = __fmul_rn(ys, ic);
         } else if (acc.count > 0) {
             const float c = (float)acc.count;
             xa = M::div(xa, c); ya = M::div(ya, c);
@@ -271,19 +278,27 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
             rax = M::div(M::mul(0.05f, xr), sq);
             ray = M::div(M::mul(0.05f, yr), sq);
         } else {
-            const float rs = 0.05f * rsqrt_approx(xr * xr + yr * yr);
-            rax = xr * rs;
-            ray = yr * rs;
+            const float rs = __fmul_rn(0.05f, rsqrt_approx(__fmaf_rn(xr, xr, __fmul_rn(yr, yr))));
+            rax = __fmul_rn(xr, rs);
+            ray = __fmul_rn(yr, rs);
         }
     }
-    float dx = M::add(M::add(M::add(M::add(M::mul(R.coh, cox), M::mul(R.avo, avx)),
-                                    M::mul(R.con, csx)),
-                             M::mul(R.rnd, rax)),
-                      M::mul(R.mom, me.z));
-    float dy = M::add(M::add(M::add(M::add(M::mul(R.coh, coy), M::mul(R.avo, avy)),
-                                    M::mul(R.con, csy)),
-                             M::mul(R.rnd, ray)),
-                      M::mul(R.mom, me.w));
+    float dx, dy;
+    if (STRICT) {
+        dx = M::add(M::add(M::add(M::add(M::mul(R.coh, cox), M::mul(R.avo, avx)),
+                                  M::mul(R.con, csx)),
+                           M::mul(R.rnd, rax)),
+                    M::mul(R.mom, me.z));
+        dy = M::add(M::add(M::add(M::add(M::mul(R.coh, coy), M::mul(R.avo, avy)),
+                                  M::mul(R.con, csy)),
+                           M::mul(R.rnd, ray)),
+                    M::mul(R.mom, me.w));
+    } else {
+        dx = __fmaf_rn(R.mom, me.z, __fmaf_rn(R.rnd, rax, __fmaf_rn(R.con, csx,
+                       __fmaf_rn(R.avo, avx, __fmul_rn(R.coh, cox)))));
+        dy = __fmaf_rn(R.mom, me.w, __fmaf_rn(R.rnd, ray, __fmaf_rn(R.con, csy,
+                       __fmaf_rn(R.avo, avy, __fmul_rn(R.coh, coy)))));
+    }
     if (STRICT) {
         const float dis = M::sqrt(M::add(M::mul(dx, dx), M::mul(dy, dy)));
         if (dis > 0.0f) {
@@ -291,11 +306,11 @@ __device__ __forceinline__ float4 finish_bird(const Rep& R, float4 me, uint32_t 
             dy = M::mul(M::div(dy, dis), R.jump);
         }
     } else {
-        const float d2 = dx * dx + dy * dy;
+        const float d2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
         if (d2 > 0.0f) {
-            const float s = rsqrt_approx(d2) * R.jump;
-            dx *= s;
-            dy *= s;
+            const float s = __fmul_rn(rsqrt_approx(d2), R.jump);
+            dx = __fmul_rn(dx, s);
+            dy = __fmul_rn(dy, s);
         }
     }
     const float nx = toroidal_transform(__fadd_rn(me.x, dx), R.w);

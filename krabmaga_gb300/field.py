@@ -247,8 +247,8 @@ class Field2D:
                C.c_size_t(len(q)), L.fptr(q), L.uptr(counts), L.uptr(dig))
         return counts[: len(q)], dig[: len(q)]
 
-    def set_step_options(self, mode=2, tile_tx: int = 0, tile_ty: int = 0) -> None:
-        """Step path: 2 tiled split (default), 1 persistent, 0 separate kernels
+    def set_step_options(self, mode=0, tile_tx: int = 0, tile_ty: int = 0) -> None:
+        """Step path: 0 separate kernels (default), 2 tiled split, 1 persistent
         (True/False mean 2/0); tile shape in bags (0 = automatic)."""
         mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)
         L.call("kb_field_set_step_options", self._h, C.c_int32(mode), C.c_int32(tile_tx),
@@ -268,6 +268,18 @@ class Field2D:
         L.call("kb_field_autotune", self._h, C.byref(params.to_c()), C.c_uint64(first_step),
                C.c_uint32(steps_per_trial), cand, C.c_int32(nc), best, C.byref(ms))
         return int(best[0]), int(best[1]), int(best[2]), float(ms.value)
+
+    def set_kernel_timing(self, enable: bool) -> None:
+        """Record CUDA events around the force / scan / rebin launches of
+        ungraphed separate-kernel steps (kb_flock_step calls of < 4 steps)."""
+        L.call("kb_field_set_kernel_timing", self._h, C.c_int32(1 if enable else 0))
+
+    def kernel_times(self) -> Tuple[Tuple[float, float, float], int]:
+        """((force_ms, scan_ms, rebin_ms) summed, steps timed) since the last call."""
+        ms = (C.c_double * 3)()
+        n = C.c_uint64()
+        L.call("kb_field_kernel_times", self._h, ms, C.byref(n))
+        return (ms[0], ms[1], ms[2]), int(n.value)
 
     def step_stats(self) -> dict:
         v = np.zeros(4, np.uint32)

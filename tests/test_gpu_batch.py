@@ -34,7 +34,7 @@ def oracle_run(rep, nsteps):
     return ids, st
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("grouping", [(0, 0), (1, 0), (1, 4), (3, 2)])
 def test_batch_replicas_match_oracle(gpu, grouping, mode):
     spl, graphs = grouping
@@ -59,9 +59,13 @@ def test_batch_exact_query_matches_oracle(gpu):
         assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
 
 
-def test_batch_equals_plain_fields(gpu):
+@pytest.mark.parametrize("mode", [0, 2])
+def test_batch_equals_plain_fields(gpu, mode):
+    # fast arithmetic: the batch (either step path) and the plain field (its
+    # default path) give the same bits
     reps = small_sweep(kg.KB_ARITH_FAST)
     b = kg.Batch(reps)
+    b.set_step_options(mode)
     b.step(0, 30, 1, 10)
     for i, rep in enumerate(reps):
         f = kg.Field2D(rep.width, rep.height, rep.discretization, True)
