@@ -21,6 +21,13 @@ namespace {
 
 // Accumulate the candidates of one contiguous run [s, e) of the read
 // buffer, four at a time so their loads are in flight together.
+// Force-kernel launch shape, chosen by timing builds on GB300 (1M boids,
+// density 0.025): 2-candidate load groups and 6 resident 256-thread blocks
+// per SM (40 registers) beat deeper unrolling at lower occupancy.
+#ifndef KB_FORCE_UNROLL
+#define KB_FORCE_UNROLL 2
+#endif
+
 template <bool STRICT, bool NOWRAP>
 __device__ __forceinline__ void accumulate_run_t(const Rep& R, const float4* __restrict__ st,
                                                  const uint32_t* __restrict__ ids, uint32_t s,
@@ -28,16 +35,17 @@ __device__ __forceinline__ void accumulate_run_t(const Rep& R, const float4* __r
                                                  Acc<STRICT>& acc) {
     acc.vec += e - s;
     uint32_t q = s;
-    for (; q + 4 <= e; q += 4) {
-        uint32_t oid[4];
-        float4 o[4];
+    constexpr int U = KB_FORCE_UNROLL;  // candidates whose loads are issued together
+    for (; q + U <= e; q += U) {
+        uint32_t oid[U];
+        float4 o[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             oid[u] = __ldg(ids + q + u);
             o[u] = __ldg(st + q + u);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < U; ++u)
             if (oid[u] != my_id) acc.template add<NOWRAP>(R, me.x, me.y, o[u]);
     }
     for (; q < e; ++q) {
@@ -55,6 +63,38 @@ __device__ __forceinline__ void accumulate_run(const Rep& R, const float4* __res
     else accumulate_run_t<STRICT, false>(R, st, ids, s, e, me, my_id, acc);
 }
 
+#ifndef KB_FORCE_COL3
+#define KB_FORCE_COL3 1
+#endif
+
+// The candidate runs of up to NC columns (one contiguous run of bags per
+// column), every run's bounds loaded before any candidate.
+template <int NC, bool STRICT>
+__device__ __forceinline__ void columns_runs(const ForceArgs& a, const Rep& R, int mi, int Mi,
+                                             int mj, int Mj, float4 me, uint32_t my_id,
+                                             Acc<STRICT>& acc) {
+    uint32_t s[NC], e[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        if (mi + k <= Mi) {
+            const uint32_t colbase = R.cell_off + (uint32_t)(mi + k) * (uint32_t)R.dh;
+            s[k] = __ldg(a.start + colbase + mj);
+            e[k] = __ldg(a.start + colbase + Mj + 1);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+        if (mi + k <= Mi) accumulate_run(R, a.st, a.ids, s[k], e[k], me, my_id, acc);
+}
+// The wider ring out of line, so that it does not set the register budget of
+// the common one-ring case.
+template <bool STRICT>
+__device__ __noinline__ void columns_runs_5(const ForceArgs& a, const Rep& R, int mi, int Mi,
+                                            int mj, int Mj, float4 me, uint32_t my_id,
+                                            Acc<STRICT>& acc) {
+    columns_runs<5>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+}
+
 template <bool STRICT, int QMODE>
 __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uint32_t i) {
     const unsigned long long step = *a.step;
@@ -68,18 +108,12 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
             // clamped range: each column's bags mj..Mj are one contiguous
             // run; fetch every run's bounds before touching candidates
             if (mj <= Mj) {
-                uint32_t s[5], e[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    if (mi + k <= Mi) {
-                        const uint32_t colbase = R.cell_off + (uint32_t)(mi + k) * (uint32_t)R.dh;
-                        s[k] = __ldg(a.start + colbase + mj);
-                        e[k] = __ldg(a.start + colbase + Mj + 1);
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < 5; ++k)
-                    if (mi + k <= Mi) accumulate_run(R, a.st, a.ids, s[k], e[k], me, my_id, acc);
+#if KB_FORCE_COL3
+                if (Mi - mi < 3) columns_runs<3>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+                else columns_runs_5(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+#else
+                columns_runs<5>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+#endif
             }
         } else {
             for (int ci = mi; ci <= Mi; ++ci) {
@@ -129,22 +163,36 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
     if (!isfinite(nx) || !isfinite(ny)) flags |= ERR_NONFINITE;
     // the rebin gathers a bag's arrivals from the 3x3 old bags around it
     // (plus the seam columns/rows); anything else must take the general sort
-    const int32_t ocx = disc(me.x, R), ocy = disc(me.y, R);
-    const bool okx = move_ok(ocx, ncx, R.seam), oky = move_ok(ocy, ncy, R.seam);
-    if (a.check_moves && !(okx && oky)) flags |= ERR_REBIN_MISS | ERR_MISS_MOVE;
+    if (a.check_moves) {
+        const int32_t ocx = disc(me.x, R), ocy = disc(me.y, R);
+        if (!(move_ok(ocx, ncx, R.seam) && move_ok(ocy, ncy, R.seam)))
+            flags |= ERR_REBIN_MISS | ERR_MISS_MOVE;
+    }
     if (flags) atomicOr(a.err, flags);
     const uint32_t key = R.cell_off + (uint32_t)idx;
     a.out_key[i] = key;
     atomicAdd(&a.hist[key], 1u);
 }
 
+#ifndef KB_FORCE_THREADS
+#define KB_FORCE_THREADS 256
+#endif
+#ifndef KB_FORCE_MINB
+#define KB_FORCE_MINB 6
+#endif
+#ifndef KB_FORCE_MINB_MULTI
+#define KB_FORCE_MINB_MULTI 6
+#endif
+
 template <bool STRICT, int QMODE, bool MULTI>
-__global__ void __launch_bounds__(256, 4) k_flock_force(ForceArgs a) {
+__global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI : KB_FORCE_MINB)
+    k_flock_force(ForceArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     if (MULTI) {
-        const Rep R = a.reps[rep_of_boid(a.reps, a.nrep, i)];
-        force_body<STRICT, QMODE>(a, R, i);
+        // the replica record stays in global memory (L1-cached field loads):
+        // a register copy of it does not fit the 40-register budget
+        force_body<STRICT, QMODE>(a, a.reps[rep_of_boid(a.reps, a.nrep, i)], i);
     } else {
         force_body<STRICT, QMODE>(a, a.rep0, i);
     }
@@ -694,9 +742,9 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
 
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
-    const unsigned g = grid_for(a.n, 256);
+    const unsigned g = grid_for(a.n, KB_FORCE_THREADS);
     const bool multi = a.nrep > 1;
-#define KB_FORCE(S, Q, MU) k_flock_force<S, Q, MU><<<g, 256, 0, s>>>(a)
+#define KB_FORCE(S, Q, MU) k_flock_force<S, Q, MU><<<g, KB_FORCE_THREADS, 0, s>>>(a)
     if (strict) {
         if (qmode == 0) { if (multi) KB_FORCE(true, 0, true); else KB_FORCE(true, 0, false); }
         else { if (multi) KB_FORCE(true, 1, true); else KB_FORCE(true, 1, false); }
