@@ -301,7 +301,25 @@ kb_status grow(kb_field* f, uint32_t need) {
     return KB_OK;
 }
 
+// First segment of each replica (Rep::seg_off), before any table upload.
+void assign_segments(std::vector<Rep>& reps) {
+    uint32_t g = 0;
+    for (Rep& R : reps) {
+        R.seg_off = g;
+        g += rep_segments(R);
+    }
+}
+
+// Segments of the segment rebin over all replicas.
+uint32_t total_segments(const kb_field* f) {
+    uint64_t t = 0;
+    for (const Rep& R : f->reps) t += rep_segments(R);
+    return t > 0xFFFFFFF0ull ? 0u : (uint32_t)t;
+}
+
 kb_status upload_rep(kb_field* f) {
+    assign_segments(f->reps);
+    f->rep.seg_off = f->reps[0].seg_off;
     if (!f->is_batch) {
         f->reps[0] = f->rep;
         if (f->rep_valid && std::memcmp(&f->rep_uploaded, &f->rep, sizeof(Rep)) == 0) return KB_OK;
@@ -404,6 +422,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     a.a_st = f->wst.p;
     a.a_ids = f->wid.p;
     a.ncells = f->ncells_total;
+    a.nsegs = total_segments(f);
     a.s_st = f->rst.p;
     a.s_ids = f->rid.p;
     a.step = bump_step ? f->dstep.p : nullptr;
@@ -457,6 +476,7 @@ kb_status materialize(kb_field* f) {
     r.a_st = buf_st(f, f->a_last);
     r.a_ids = buf_ids(f, f->a_last);
     r.ncells = f->ncells_total;
+    r.nsegs = total_segments(f);
     r.s_st = buf_st(f, dst);
     r.s_ids = buf_ids(f, dst);
     r.step = nullptr;
@@ -827,6 +847,8 @@ kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uin
     f->ncells_total = ncells;
     f->cells_cap = nc;
     f->is_batch = is_batch;
+    assign_segments(f->reps);
+    f->rep = f->reps[0];
     cudaError_t e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking);
     const uint32_t nt = scan_tiles(nc) + 1;
     if (!e) e = f->d_rep.alloc(reps.size());
@@ -877,6 +899,7 @@ kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
         if (e) return cuda_fail(e, "replica table");
     }
     f->reps = reps;
+    assign_segments(f->reps);
     f->rep = f->reps[0];
     f->ncells_total = (uint32_t)total;
     f->fused.ready = false;

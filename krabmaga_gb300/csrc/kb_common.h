@@ -49,7 +49,7 @@ struct Rep {
     uint32_t origin_lo, origin_hi;  // global step at which this replica's step 0 ran
     int32_t seam;           // first line from which a one-step move can wrap to line 0
     float inv_d;            // fl(1/d), for the exact fast discretisation
-    uint32_t _pad2;
+    uint32_t seg_off;       // first 32-bag column segment of this replica (segment rebin)
     unsigned long long dh_magic;  // ceil(2^64 / dh): n / dh == umul64hi(n, dh_magic) for n < 2^32
 };
 

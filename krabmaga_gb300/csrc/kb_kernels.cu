@@ -462,6 +462,152 @@ __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
     }
 }
 
+// ---------------------------------------------------------- segment rebin
+// One warp per segment of up to 32 consecutive bags of one column (lane l
+// owns bag c0 + l).  The arrivals of those bags sit in the write list inside
+// the source runs of the neighbouring columns: rows Y0-1..Y1+1 of columns
+// X-1..X+1 (plus the seam lines at the field's edges).  The warp streams
+// those runs in ascending bag order, 32 entries at a time with coalesced key
+// loads; entries whose key falls in the segment take the next slot of their
+// bag: __match_any_sync ranks equal keys within a batch in lane (= list)
+// order, a per-bag counter in shared memory carries the rank across batches.
+// That is the per-bag insertion order of the reference's lazy_update.
+constexpr uint32_t FULL_MASK = 0xFFFFFFFFu;
+constexpr int REBIN_SEG_WARPS = 8;
+
+__device__ __forceinline__ int rep_of_seg(const Rep* reps, int nrep, uint32_t g) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&reps[mid].seg_off) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Slot of one write-list entry of a batch of 32 (key k per lane, ~0u for
+// none) in its bag of the segment, or ~0u when the key is outside the
+// segment.  Every lane of the warp calls it.
+__device__ __forceinline__ uint32_t seg_rank(uint32_t k, uint32_t c0, int nb, uint32_t lo,
+                                             uint32_t hi, uint32_t* cnt, uint32_t lane_lt,
+                                             bool& bad) {
+    const uint32_t local = k - c0;
+    const bool in = local < (uint32_t)nb;
+    if (__ballot_sync(FULL_MASK, in) == 0u) return 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(FULL_MASK, in ? local : 0xFFFFFFFFu);
+    const uint32_t rank = __popc(peers & lane_lt);
+    const uint32_t src = local & 31u;
+    const uint32_t blo = __shfl_sync(FULL_MASK, lo, src);
+    const uint32_t bhi = __shfl_sync(FULL_MASK, hi, src);
+    const uint32_t base = in ? cnt[src] : 0u;
+    __syncwarp();
+    uint32_t dst = 0xFFFFFFFFu;
+    if (in) {
+        dst = blo + base + rank;
+        if (dst >= bhi) {
+            bad = true;
+            dst = 0xFFFFFFFFu;
+        }
+        if (rank + 1u == (uint32_t)__popc(peers)) cnt[src] = base + rank + 1u;
+    }
+    __syncwarp();
+    return dst;
+}
+
+// One batch of 32 write-list entries (p, valid per lane): rank and copy.
+__device__ __forceinline__ void seg_batch(const RebinArgs& a, bool valid, uint32_t p, uint32_t c0,
+                                          int nb, uint32_t lo, uint32_t hi, uint32_t* cnt,
+                                          uint32_t lane_lt, bool& bad) {
+    const uint32_t k = valid ? __ldg(a.key + p) : 0xFFFFFFFFu;
+    const uint32_t dst = seg_rank(k, c0, nb, lo, hi, cnt, lane_lt, bad);
+    if (dst != 0xFFFFFFFFu) {
+        a.s_st[dst] = __ldg(a.a_st + p);
+        a.s_ids[dst] = __ldg(a.a_ids + p);
+    }
+}
+
+__device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, uint32_t g,
+                                              uint32_t* cnt) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nsy = ((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS;
+    const uint32_t local = g - R.seg_off;
+    const uint32_t Xu = local / nsy;
+    const int X = (int)Xu;
+    const int Y0 = (int)(local - Xu * nsy) * SEG_ROWS;
+    const int nb = min(SEG_ROWS, R.dh - Y0);
+    const int Y1 = Y0 + nb - 1;
+    const uint32_t c0 = R.cell_off + Xu * (uint32_t)R.dh + (uint32_t)Y0;
+    const bool interior = X > 0 && X < R.seam && Y0 > 0 && Y1 < R.seam;
+    // this segment's bag offsets and (interior) the bounds of its three
+    // source runs, in one round trip
+    uint32_t lo = 0, hi = 0, b = 0;
+    if ((int)lane < nb) {
+        lo = __ldg(a.start_next + c0 + lane);
+        hi = __ldg(a.start_next + c0 + lane + 1);
+    }
+    if (interior && lane < 6u) {
+        const uint32_t cb = R.cell_off + (uint32_t)(X - 1 + (int)(lane % 3u)) * (uint32_t)R.dh;
+        b = __ldg(a.start_cur + cb + (lane < 3u ? (uint32_t)(Y0 - 1) : (uint32_t)(Y1 + 2)));
+    }
+    if (__shfl_sync(FULL_MASK, lo, 0) == __shfl_sync(FULL_MASK, hi, nb - 1)) return;  // no arrivals
+    cnt[lane] = 0u;
+    __syncwarp();
+    const uint32_t lane_lt = (1u << lane) - 1u;
+    bool bad = false;
+    if (interior) {
+        // columns X-1..X+1, rows Y0-1..Y1+1, as one list of three runs
+        const uint32_t s0 = __shfl_sync(FULL_MASK, b, 0), s1 = __shfl_sync(FULL_MASK, b, 1);
+        const uint32_t s2 = __shfl_sync(FULL_MASK, b, 2), e0 = __shfl_sync(FULL_MASK, b, 3);
+        const uint32_t e1 = __shfl_sync(FULL_MASK, b, 4), e2 = __shfl_sync(FULL_MASK, b, 5);
+        const uint32_t P1 = e0 - s0, P2 = P1 + (e1 - s1), T = P2 + (e2 - s2);
+        for (uint32_t f = 0; f < T; f += 32u) {
+            const uint32_t ff = f + lane;
+            const uint32_t p = ff < P1 ? s0 + ff : (ff < P2 ? s1 + (ff - P1) : s2 + (ff - P2));
+            seg_batch(a, ff < T, p, c0, nb, lo, hi, cnt, lane_lt, bad);
+        }
+    } else {
+        // a segment at the seam or the field's edge: the source lines of
+        // src_line on both axes, run by run in ascending bag order
+        const int mlo = max(0, Y0 - 1), mhi = min(R.max_y, Y1 + 1);
+        int lastx = -1;
+#pragma unroll 1
+        for (int kx = 0; kx < SRC_LINES; ++kx) {
+            const int sx = src_line(kx, X, R.max_x, R.seam);
+            if (sx < 0 || sx > R.max_x || sx <= lastx) continue;
+            lastx = sx;
+            const uint32_t cb = R.cell_off + (uint32_t)sx * (uint32_t)R.dh;
+            int ra[3], rb[3], nr = 0;
+            if (Y1 >= R.seam && mlo > 0) { ra[nr] = 0; rb[nr] = 0; ++nr; }   // bags >= seam take row 0
+            ra[nr] = mlo; rb[nr] = mhi; ++nr;
+            if (Y0 == 0) {  // row 0 takes rows seam..seam+3
+                const int l2 = max(R.seam, mhi + 1), h2 = min(R.seam + SRC_LINES - 5, R.max_y);
+                if (l2 <= h2) { ra[nr] = l2; rb[nr] = h2; ++nr; }
+            }
+#pragma unroll 1
+            for (int r = 0; r < nr; ++r) {
+                const uint32_t s = __ldg(a.start_cur + cb + (uint32_t)ra[r]);
+                const uint32_t e = __ldg(a.start_cur + cb + (uint32_t)rb[r] + 1u);
+#pragma unroll 1
+                for (uint32_t f = s; f < e; f += 32u)
+                    seg_batch(a, f + lane < e, f + lane, c0, nb, lo, hi, cnt, lane_lt, bad);
+            }
+        }
+    }
+    if ((int)lane < nb && cnt[lane] != hi - lo) bad = true;
+    if (__any_sync(FULL_MASK, bad) && lane == 0u) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_MATERIALIZE);
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(32 * REBIN_SEG_WARPS) k_rebin_seg(RebinArgs a) {
+    __shared__ uint32_t s_cnt[REBIN_SEG_WARPS][32];
+    const uint32_t w = threadIdx.x >> 5;
+    const uint32_t g = blockIdx.x * REBIN_SEG_WARPS + w;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && a.step != nullptr) *a.step += 1ull;
+    if (g >= a.nsegs) return;  // whole warps
+    if (MULTI) rebin_segment(a, a.reps[rep_of_seg(a.reps, a.nrep, g)], g, s_cnt[w]);
+    else rebin_segment(a, a.rep0, g, s_cnt[w]);
+}
+
 // ---------------------------------------------------------- general sort
 __global__ void k_hist_list(const uint32_t* __restrict__ key, const uint8_t* __restrict__ dead,
                             uint32_t n, uint32_t* __restrict__ hist) {
@@ -757,6 +903,12 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
 }
 
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s) {
+    if (a.key != nullptr && a.nsegs > 0) {
+        const unsigned gs = grid_for(a.nsegs, REBIN_SEG_WARPS);
+        if (a.nrep > 1) k_rebin_seg<true><<<gs, 32 * REBIN_SEG_WARPS, 0, s>>>(a);
+        else k_rebin_seg<false><<<gs, 32 * REBIN_SEG_WARPS, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     const unsigned g = grid_for(a.ncells > 0 ? a.ncells : 1, 256);
     if (a.nrep > 1) k_rebin<true><<<g, 256, 0, s>>>(a);
     else k_rebin<false><<<g, 256, 0, s>>>(a);

@@ -62,11 +62,17 @@ struct RebinArgs {
     const float4* a_st;
     const uint32_t* a_ids;
     uint32_t ncells;
+    uint32_t nsegs;  // 32-bag column segments over all replicas (0: per-bag kernel only)
     float4* s_st;
     uint32_t* s_ids;
     unsigned long long* step;
     uint32_t* err;
 };
+// Bag segments of the segment rebin: SEG_ROWS consecutive bags of one column.
+constexpr int SEG_ROWS = 32;
+inline uint32_t rep_segments(const Rep& R) {
+    return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
+}
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s);
 
 // General stable counting sort of the write list by key (insertion order
