@@ -53,6 +53,14 @@ typedef int32_t kb_status;
 typedef struct kb_field kb_field;
 
 /* Field2D::new(w, h, d, toroidal), field_2d.rs:304-322. */
+/* Cell range of the neighbour queries on a toroidal field.  CLAMP is the
+ * reference (field_2d.rs:398-418, 484-500: the range is clamped to the bag
+ * matrix, so a query does not see across the seam); TORUS wraps the range
+ * (t_transform, field_2d.rs:926-932), so it does.  Non-toroidal fields
+ * always wrap, as the reference does. */
+#define KB_CELL_WRAP_CLAMP 0
+#define KB_CELL_WRAP_TORUS 1
+
 typedef struct {
     float width;
     float height;
@@ -60,6 +68,7 @@ typedef struct {
     int32_t toroidal;
     int32_t device;         /* CUDA ordinal */
     uint32_t capacity_hint; /* expected object count (storage grows as needed) */
+    int32_t cell_wrap;      /* KB_CELL_WRAP_* (0: the reference's clamped range) */
 } kb_field_desc;
 
 /* The Flockers constants (bird.rs:12-17) and query radius (bird.rs:41) as a
@@ -241,8 +250,8 @@ typedef struct {
     float height;
     float discretization;
     int32_t toroidal;
-    uint32_t nboids; /* boids this replica holds */
-    uint32_t _pad;
+    uint32_t nboids;   /* boids this replica holds */
+    int32_t cell_wrap; /* KB_CELL_WRAP_* */
     kb_flock_params params; /* query_mode and arith must be equal across a batch */
 } kb_replica_desc;
 

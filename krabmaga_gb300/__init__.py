@@ -6,6 +6,7 @@ reference's API names (Field2D, State, Schedule, simulate, Flocker).
 """
 from . import _lib
 from ._lib import KbError, lib, LIB_PATH, KB_QUERY_RELAX, KB_QUERY_EXACT, KB_ARITH_STRICT, KB_ARITH_FAST
+from ._lib import KB_CELL_WRAP_CLAMP, KB_CELL_WRAP_TORUS
 from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
@@ -16,6 +17,7 @@ __all__ = [
     "Bird", "Field2D", "Real2D", "FlockParams", "Flocker", "Schedule", "State", "simulate",
     "simulate_old", "gen_uniform", "gen_clustered", "KbError", "lib", "LIB_PATH",
     "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
+    "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
 ]
 

@@ -28,6 +28,8 @@ KB_QUERY_EXACT = 1
 KB_ARITH_STRICT = 0
 KB_ARITH_FAST = 1
 KB_NOALLOC_MAX_QUERIES = 65536
+KB_CELL_WRAP_CLAMP = 0
+KB_CELL_WRAP_TORUS = 1
 
 STATUS_NAMES = {
     0: "KB_OK", 1: "KB_ERR_ARG", 2: "KB_ERR_OOM", 3: "KB_ERR_CUDA", 4: "KB_ERR_TIMEOUT",
@@ -52,6 +54,7 @@ class FieldDesc(C.Structure):
         ("toroidal", C.c_int32),
         ("device", C.c_int32),
         ("capacity_hint", C.c_uint32),
+        ("cell_wrap", C.c_int32),
     ]
 
 
@@ -78,7 +81,7 @@ class ReplicaDesc(C.Structure):
         ("discretization", C.c_float),
         ("toroidal", C.c_int32),
         ("nboids", C.c_uint32),
-        ("_pad", C.c_uint32),
+        ("cell_wrap", C.c_int32),
         ("params", FlockParamsC),
     ]
 

@@ -28,6 +28,7 @@ class Replica:
     params: FlockParams
     state: Tuple[np.ndarray, np.ndarray, np.ndarray]  # ids, xy[n,2], dxy[n,2]
     toroidal: bool = True
+    cell_wrap: int = L.KB_CELL_WRAP_CLAMP
 
     @property
     def n(self) -> int:
@@ -40,6 +41,7 @@ class Batch:
         for d, r in zip(descs, replicas):
             d.width, d.height, d.discretization = r.width, r.height, r.discretization
             d.toroidal = 1 if r.toroidal else 0
+            d.cell_wrap = r.cell_wrap
             d.nboids = r.n
             d.params = r.params.to_c()
         h = C.c_void_p()

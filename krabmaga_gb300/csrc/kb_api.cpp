@@ -43,7 +43,8 @@ int64_t host_bag_index(const Rep& R, float x, float y) {
     return idx;
 }
 
-bool make_rep_geometry(float w, float h, float d, int toroidal, Rep* R, std::string* why) {
+bool make_rep_geometry(float w, float h, float d, int toroidal, Rep* R, std::string* why,
+                       int cell_wrap = KB_CELL_WRAP_CLAMP) {
     if (!(std::isfinite(w) && std::isfinite(h) && std::isfinite(d)) || w <= 0.f || h <= 0.f ||
         d <= 0.f) {
         *why = "width, height and discretization must be finite and positive";
@@ -54,6 +55,11 @@ bool make_rep_geometry(float w, float h, float d, int toroidal, Rep* R, std::str
     R->h = h;
     R->d = d;
     R->toroidal = toroidal ? 1 : 0;
+    if (cell_wrap != KB_CELL_WRAP_CLAMP && cell_wrap != KB_CELL_WRAP_TORUS) {
+        *why = "cell_wrap must be KB_CELL_WRAP_CLAMP or KB_CELL_WRAP_TORUS";
+        return false;
+    }
+    R->cell_wrap = (toroidal && cell_wrap == KB_CELL_WRAP_TORUS) ? 1 : 0;
     const float cw = std::ceil(w / d), ch = std::ceil(h / d);
     if (cw > 1.0e8f || ch > 1.0e8f || (double)(cw + 1.0f) * (double)(ch + 1.0f) > 2.0e9) {
         *why = "bag matrix too large (more than 2e9 bags)";
@@ -85,7 +91,8 @@ void set_rep_params(Rep* R, const kb_flock_params* p) {
     // (dd+1)*d of the boid, so toroidal_distance's |a-b| <= dim/2 test holds
     // whenever (dd+1)*d stays clear of half the side.
     const double reach = ((double)std::max(R->dd, 0) + 1.0) * (double)R->d;
-    R->nowrap = (R->toroidal && reach * 1.01 + 1e-3 < 0.5 * (double)std::min(R->w, R->h)) ? 1 : 0;
+    R->nowrap = (R->toroidal && !R->cell_wrap &&
+                 reach * 1.01 + 1e-3 < 0.5 * (double)std::min(R->w, R->h)) ? 1 : 0;
     // A move of at most |jump| wraps to line 0 only from x > w - |jump|, i.e.
     // from lines >= floor((w - |jump|)/d); one line lower covers the f32
     // rounding of x/d.  A narrow last column can put that two or three lines
@@ -516,7 +523,8 @@ bool fused_eligible(const kb_field* f, const kb_flock_params* p) {
     if (f->fused_mode == 0 || !f->layout_is_positions || f->rn == 0) return false;
     if (p->query_mode != KB_QUERY_RELAX && p->query_mode != KB_QUERY_EXACT) return false;
     for (const Rep& R : f->reps)
-        if (!R.toroidal || !fast_rebin_ok(R) || R.dd > FUSED_DD_MAX || R.dw > 65535 || R.dh > 65535)
+        if (!R.toroidal || R.cell_wrap || !fast_rebin_ok(R) || R.dd > FUSED_DD_MAX || R.dw > 65535 ||
+            R.dh > 65535)
             return false;
     return true;
 }
@@ -936,7 +944,8 @@ kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
     *out = nullptr;
     Rep R;
     std::string why;
-    if (!make_rep_geometry(desc->width, desc->height, desc->discretization, desc->toroidal, &R, &why))
+    if (!make_rep_geometry(desc->width, desc->height, desc->discretization, desc->toroidal, &R, &why,
+                           desc->cell_wrap))
         return fail(KB_ERR_ARG, why);
     return field_new(desc->device, std::vector<Rep>{R}, false, desc->capacity_hint, out);
 }
@@ -1630,7 +1639,8 @@ kb_status kb_batch_create(int32_t device, uint32_t nrep, const kb_replica_desc* 
     std::string why;
     for (uint32_t r = 0; r < nrep; ++r) {
         const kb_replica_desc& d = reps[r];
-        if (!make_rep_geometry(d.width, d.height, d.discretization, d.toroidal, &table[r], &why))
+        if (!make_rep_geometry(d.width, d.height, d.discretization, d.toroidal, &table[r], &why,
+                               d.cell_wrap))
             return fail(KB_ERR_ARG, "replica " + std::to_string(r) + ": " + why);
         if (!params_ok(&d.params, &why)) return fail(KB_ERR_ARG, "replica " + std::to_string(r) + ": " + why);
         if (d.params.query_mode != reps[0].params.query_mode || d.params.arith != reps[0].params.arith)

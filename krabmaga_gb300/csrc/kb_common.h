@@ -51,6 +51,8 @@ struct Rep {
     float inv_d;            // fl(1/d), for the exact fast discretisation
     uint32_t seg_off;       // first 32-bag column segment of this replica (segment rebin)
     unsigned long long dh_magic;  // ceil(2^64 / dh): n / dh == umul64hi(n, dh_magic) for n < 2^32
+    int32_t cell_wrap;      // toroidal fields: 0 clamp the query's cell range (the reference), 1 wrap it
+    uint32_t _pad3;
 };
 
 // ------------------------------------------------------------------ Philox

@@ -131,11 +131,16 @@ __device__ __forceinline__ bool cell_range(const Rep& R, float x, float y, int32
     if (dd < 0) return false;
     int cx = disc(x, R), cy = disc(y, R);
     int a = cx - dd, b = cx + dd, c = cy - dd, e = cy + dd;
-    if (R.toroidal) {
+    if (R.toroidal && !R.cell_wrap) {
         a = max(0, a);
         b = min(b, R.max_x - 1);
         c = max(0, c);
         e = min(e, R.max_y - 1);
+    } else if (R.toroidal) {
+        // true torus: the range wraps (t_transform); a ring as wide as the
+        // field visits every line once, in ascending order
+        if (2 * dd + 1 >= R.max_x) { a = 0; b = R.max_x - 1; }
+        if (2 * dd + 1 >= R.max_y) { c = 0; e = R.max_y - 1; }
     }
     *mi = a; *Mi = b; *mj = c; *Mj = e;
     return true;

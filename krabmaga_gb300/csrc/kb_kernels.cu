@@ -104,7 +104,8 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
     Acc<STRICT> acc;
     int mi, Mi, mj, Mj;
     if (cell_range(R, me.x, me.y, R.dd, &mi, &Mi, &mj, &Mj)) {
-        if (QMODE == 0 && R.toroidal && Mi - mi < 5) {
+        const bool clamped = R.toroidal && !R.cell_wrap;  // runs never cross the seam
+        if (QMODE == 0 && clamped && Mi - mi < 5) {
             // clamped range: each column's bags mj..Mj are one contiguous
             // run; fetch every run's bounds before touching candidates
             if (mj <= Mj) {
@@ -119,7 +120,7 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
             for (int ci = mi; ci <= Mi; ++ci) {
                 const int bx = t_transform(ci, R.max_x);
                 const uint32_t colbase = R.cell_off + (uint32_t)bx * (uint32_t)R.dh;
-                if (QMODE == 0 && R.toroidal) {
+                if (QMODE == 0 && clamped) {
                     if (mj > Mj) continue;
                     accumulate_run(R, a.st, a.ids, __ldg(a.start + colbase + mj),
                                    __ldg(a.start + colbase + Mj + 1), me, my_id, acc);

@@ -56,8 +56,10 @@ class Field2D:
     """Field2D::new(w, h, d, toroidal) -- field_2d.rs:304-322."""
 
     def __init__(self, w: float, h: float, d: float, toroidal: bool, device: int = 0,
-                 capacity_hint: int = 0):
-        desc = L.FieldDesc(w, h, d, 1 if toroidal else 0, device, capacity_hint)
+                 capacity_hint: int = 0, cell_wrap: int = L.KB_CELL_WRAP_CLAMP):
+        """cell_wrap (toroidal fields): KB_CELL_WRAP_CLAMP, the reference's
+        clamped query range, or KB_CELL_WRAP_TORUS, a range that wraps."""
+        desc = L.FieldDesc(w, h, d, 1 if toroidal else 0, device, capacity_hint, cell_wrap)
         h_ = C.c_void_p()
         L.call("kb_field_create", C.byref(desc), C.byref(h_))
         self._h = h_

@@ -37,6 +37,7 @@ _SIGS = {
     "orc_jitter_pair": (None, [C.c_uint64, C.c_uint32, C.c_uint64, _F, _F]),
     "orc_field_new": (_P, [C.c_float, C.c_float, C.c_float, C.c_int]),
     "orc_field_free": (None, [_P]),
+    "orc_field_set_cell_wrap": (None, [_P, C.c_int]),
     "orc_field_dims": (None, [_P, C.POINTER(C.c_int32)]),
     "orc_field_nagents": (C.c_size_t, [_P]),
     "orc_field_panicked": (C.c_int, [_P]),
@@ -96,8 +97,11 @@ def philox(ctr, key):
 class OracleField:
     """The oracle's Field2D (field_2d.rs:267-1014, f32-faithful)."""
 
-    def __init__(self, w, h, d, toroidal=True):
+    def __init__(self, w, h, d, toroidal=True, cell_wrap=0):
+        """cell_wrap = 1: the true-torus query range (wraps instead of clamping)."""
         self.h = lib.orc_field_new(w, h, d, 1 if toroidal else 0)
+        if cell_wrap:
+            lib.orc_field_set_cell_wrap(self.h, 1)
         dims = (C.c_int32 * 4)()
         lib.orc_field_dims(self.h, dims)
         self.dw, self.dh, self.max_x, self.max_y = (int(v) for v in dims)

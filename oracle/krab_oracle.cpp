@@ -156,6 +156,7 @@ struct Field2D {
     size_t nagents = 0;
     float width, height, disc;
     bool toroidal;
+    bool cell_wrap = false;  // toroidal only: wrap the query's cell range instead of clamping it
     int dh, dw;
     size_t density_estimation = 0;
     bool density_check = false;
@@ -235,11 +236,17 @@ struct Field2D {
         discretize(lx, ly, &cx, &cy);
         int mx = max_x(), my = max_y();
         int min_i = cx - dd, max_i = cx + dd, min_j = cy - dd, max_j = cy + dd;
-        if (toroidal) {
+        if (toroidal && !cell_wrap) {
             min_i = std::max(0, min_i);
             max_i = std::min(max_i, mx - 1);
             min_j = std::max(0, min_j);
             max_j = std::min(max_j, my - 1);
+        } else if (toroidal) {
+            // The true-torus option (not in the reference): the range wraps
+            // through t_transform; a ring as wide as the field visits every
+            // line once, in ascending order.
+            if (2 * dd + 1 >= mx) { min_i = 0; max_i = mx - 1; }
+            if (2 * dd + 1 >= my) { min_j = 0; max_j = my - 1; }
         }
         *mi = min_i; *Mi = max_i; *mj = min_j; *Mj = max_j;
         return true;
@@ -491,6 +498,7 @@ void* orc_field_new(float w, float h, float d, int toroidal) {
     return new Field2D(w, h, d, toroidal != 0);
 }
 void orc_field_free(void* f) { delete (Field2D*)f; }
+void orc_field_set_cell_wrap(void* f, int wrap) { ((Field2D*)f)->cell_wrap = wrap != 0; }
 
 void orc_field_dims(void* fp, int32_t* out4) {
     Field2D* f = (Field2D*)fp;

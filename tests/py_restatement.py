@@ -74,8 +74,9 @@ def distance(x1, y1, x2, y2, w, h, tor):
 
 
 class PyField:
-    def __init__(self, w, h, d, tor=True):
+    def __init__(self, w, h, d, tor=True, wrap=False):
         self.w, self.h, self.d, self.tor = f32(w), f32(h), f32(d), tor
+        self.wrap = bool(tor and wrap)  # true-torus query range (not in the reference)
         self.max_x = as_i32(np.ceil(f32(self.w / self.d)))
         self.max_y = as_i32(np.ceil(f32(self.h / self.d)))
         self.dw, self.dh = self.max_x + 1, self.max_y + 1
@@ -96,8 +97,13 @@ class PyField:
         dd = as_i32(np.floor(f32(f32(dist) / self.d)))
         cx, cy = self.disc(x, y)
         a, b, c, e = cx - dd, cx + dd, cy - dd, cy + dd
-        if self.tor:
+        if self.tor and not self.wrap:
             a, b, c, e = max(0, a), min(b, self.max_x - 1), max(0, c), min(e, self.max_y - 1)
+        elif self.wrap:
+            if 2 * dd + 1 >= self.max_x:
+                a, b = 0, self.max_x - 1
+            if 2 * dd + 1 >= self.max_y:
+                c, e = 0, self.max_y - 1
         return a, b, c, e
 
     def check_circle(self, bx, by, lx, ly, dis):

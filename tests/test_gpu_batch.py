@@ -93,3 +93,23 @@ def test_batch_rejects_mixed_modes(gpu):
     reps[1].params.arith = kg.KB_ARITH_STRICT
     with pytest.raises(kg.KbError):
         kg.Batch(reps)
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_batch_true_torus_replica_matches_oracle(gpu, mode):
+    # a true-torus replica beside clamped ones: the tiled path leaves the
+    # batch to the separate kernels (the tiles assume the clamped range)
+    reps = small_sweep(kg.KB_ARITH_STRICT)[:4]
+    reps[1].cell_wrap = kg.KB_CELL_WRAP_TORUS
+    b = kg.Batch(reps)
+    b.set_step_options(mode)
+    b.step(0, 15, 1, 5)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        o = oracle.OracleField(rep.width, rep.height, rep.discretization, True,
+                               cell_wrap=rep.cell_wrap)
+        o.set_many(*rep.state)
+        o.lazy_update()
+        o.flock_run(oracle.params_from(rep.params), 0, 15)
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"

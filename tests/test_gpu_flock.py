@@ -335,3 +335,35 @@ def test_device_jitter_matches_oracle_philox(gpu):
         step(f, p, t, 1)
         o.flock_run(oracle.params_from(p), t, 1)
         assert same_bits(f.get_state()[1], o.iter(1)[1])
+
+
+@pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
+@pytest.mark.parametrize("side,radius", [(300.0, 10.0), (40.0, 14.0), (30.0, 16.0)])
+def test_true_torus_option_matches_oracle(gpu, kind, side, radius):
+    # KB_CELL_WRAP_TORUS: the query's cell range wraps (the reference clamps
+    # it); trajectories and per-step neighbour lists stay bit-exact against
+    # the oracle with the same option, including rings that cover the field
+    n = int(side * side * 0.025) + 40
+    ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 17, 1.0)
+    p = kg.FlockParams(seed=6, query_mode=kind, neighbor_radius=radius, arith=kg.KB_ARITH_STRICT)
+    f = kg.Field2D(side, side, C1_D, True, capacity_hint=n, cell_wrap=kg.KB_CELL_WRAP_TORUS)
+    f.set_locations(ids0, xy0, dxy0)
+    f.lazy_update()
+    o = oracle.OracleField(side, side, C1_D, True, cell_wrap=1)
+    o.set_many(ids0, xy0, dxy0)
+    o.lazy_update()
+    for s in range(0, 24, 6):
+        step(f, p, s, 6)
+        o.flock_run(oracle.params_from(p), s, 6)
+        ids, st = f.get_state()
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), s
+        gc, gl = f.neighbor_lists(kind, radius, st[:, :2])
+        oc, ol = o.neighbor_lists(kind, radius, st[:, :2])
+        assert np.array_equal(gc, oc) and np.array_equal(gl, ol), s
+    # across the seam the wrapped range finds more than the clamped one
+    g2 = kg.Field2D(side, side, C1_D, True)
+    g2.set_locations(ids, st[:, :2].copy(), st[:, 2:].copy())
+    g2.lazy_update()
+    cc, _ = g2.neighbor_lists(kind, radius, st[:, :2])
+    assert (gc >= cc).all() and gc.sum() > cc.sum()

@@ -77,11 +77,12 @@ def test_oracle_matches_python_transcription(kind, side, d, radius, n):
         assert np.array_equal(py_st.view(np.uint32), o_st.view(np.uint32)), f"step {step}"
 
 
-def test_queries_match_python_transcription():
+@pytest.mark.parametrize("wrap", [False, True])
+def test_queries_match_python_transcription(wrap):
     ids, xy, dxy = _random_flock(300, 50.0, seed=9)
     for d in (C1_D, 1.7):
-        py = pr.PyField(50.0, 50.0, d)
-        orc = oracle.OracleField(50.0, 50.0, d, True)
+        py = pr.PyField(50.0, 50.0, d, wrap=wrap)
+        orc = oracle.OracleField(50.0, 50.0, d, True, cell_wrap=1 if wrap else 0)
         for i, p, h in zip(ids, xy, dxy):
             py.set((int(i), p[0], p[1], h[0], h[1]), p[0], p[1])
         orc.set_many(ids, xy, dxy)
@@ -90,11 +91,29 @@ def test_queries_match_python_transcription():
         rng = np.random.default_rng(5)
         for _ in range(60):
             q = (rng.random(2) * 52 - 1).astype(np.float32)
-            r = float(rng.choice([0.0, 0.3, 3.0, 10.0, 17.5]))
+            r = float(rng.choice([0.0, 0.3, 3.0, 10.0, 17.5, 30.0]))
             for kind in (0, 1):
                 want = [b[0] for b in py.query(kind, q[0], q[1], r)]
                 got, _ = orc.query(kind, float(q[0]), float(q[1]), r)
                 assert want == list(got)
+
+
+def test_true_torus_query_sees_across_the_seam():
+    # the reference's toroidal query clamps its cell range (field_2d.rs:495-500)
+    # and misses a neighbour one unit away across x = 0; the true-torus option
+    # finds it
+    ids = np.array([1, 2], np.uint32)
+    xy = np.array([[0.5, 25.0], [49.5, 25.0]], np.float32)
+    dxy = np.zeros((2, 2), np.float32)
+    found = {}
+    for wrap in (0, 1):
+        orc = oracle.OracleField(50.0, 50.0, 2.0, True, cell_wrap=wrap)
+        orc.set_many(ids, xy, dxy)
+        orc.lazy_update()
+        got, _ = orc.query(0, 0.5, 25.0, 3.0)
+        found[wrap] = sorted(int(v) for v in got)
+    assert found[0] == [1]
+    assert found[1] == [1, 2]
 
 
 def test_golden_trajectories_reproduce():
