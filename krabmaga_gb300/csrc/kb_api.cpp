@@ -390,7 +390,7 @@ kb_status check_flags(kb_field* f) {
 }
 
 kb_status ensure_aux_scan(kb_field* f, uint32_t n) {
-    const uint32_t t = scan_tiles(n) + 1;
+    const uint32_t t = scan_state_words(n);
     if (t <= f->aux_tiles) return KB_OK;
     DevBuf<unsigned long long> ts;
     cudaError_t e = ts.alloc(t);
@@ -858,7 +858,7 @@ kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uin
     assign_segments(f->reps);
     f->rep = f->reps[0];
     cudaError_t e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking);
-    const uint32_t nt = scan_tiles(nc) + 1;
+    const uint32_t nt = scan_state_words(nc);
     if (!e) e = f->d_rep.alloc(reps.size());
     if (!e) e = f->start[0].alloc((size_t)nc + 1);
     if (!e) e = f->start[1].alloc((size_t)nc + 1);

@@ -19,6 +19,43 @@
 namespace kb {
 namespace {
 
+// Programmatic dependent launch.  The step's kernels are launched so that
+// the next one may be scheduled before the previous one ends; each first
+// waits until its predecessor has finished and its writes are visible
+// (griddepcontrol.wait, before touching any memory), then lets its own
+// successor launch (griddepcontrol.launch_dependents).  Launched without the
+// attribute, the wait returns at once.
+#ifndef KB_PDL
+#define KB_PDL 1
+#endif
+__device__ __forceinline__ void pdl_enter() {
+#if KB_PDL
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                       Args... args) {
+#if KB_PDL
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+#else
+    kernel<<<grid, block, 0, s>>>(static_cast<KArgs>(args)...);
+    return cudaGetLastError();
+#endif
+}
+
 // Accumulate the candidates of one contiguous run [s, e) of the read
 // buffer, four at a time so their loads are in flight together.
 // Force-kernel launch shape, chosen by timing builds on GB300 (1M boids,
@@ -66,6 +103,9 @@ __device__ __forceinline__ void accumulate_run(const Rep& R, const float4* __res
 #ifndef KB_FORCE_COL3
 #define KB_FORCE_COL3 1
 #endif
+#ifndef KB_FORCE_FLAT
+#define KB_FORCE_FLAT 1
+#endif
 
 // The candidate runs of up to NC columns (one contiguous run of bags per
 // column), every run's bounds loaded before any candidate.
@@ -86,6 +126,42 @@ __device__ __forceinline__ void columns_runs(const ForceArgs& a, const Rep& R, i
     for (int k = 0; k < NC; ++k)
         if (mi + k <= Mi) accumulate_run(R, a.st, a.ids, s[k], e[k], me, my_id, acc);
 }
+// The three runs of a one-bag ring as one flat list: a warp then iterates
+// the longest lane's total instead of the sum of the per-column maxima.
+template <bool STRICT>
+__device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, int mi, int Mi,
+                                              int mj, int Mj, float4 me, uint32_t my_id,
+                                              Acc<STRICT>& acc) {
+    uint32_t s[3], e[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        s[k] = e[k] = 0u;
+        if (mi + k <= Mi) {
+            const uint32_t colbase = R.cell_off + (uint32_t)(mi + k) * (uint32_t)R.dh;
+            s[k] = __ldg(a.start + colbase + mj);
+            e[k] = __ldg(a.start + colbase + Mj + 1);
+        }
+    }
+    const uint32_t P1 = e[0] - s[0], P2 = P1 + (e[1] - s[1]), T = P2 + (e[2] - s[2]);
+    acc.vec += T;
+    const uint32_t d1 = s[1] - P1, d2 = s[2] - P2;  // position = f + d (mod 2^32)
+    if (R.nowrap) {
+        for (uint32_t f = 0; f < T; ++f) {
+            const uint32_t p = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
+            const uint32_t oid = __ldg(a.ids + p);
+            const float4 o = __ldg(a.st + p);
+            if (oid != my_id) acc.template add<true>(R, me.x, me.y, o);
+        }
+    } else {
+        for (uint32_t f = 0; f < T; ++f) {
+            const uint32_t p = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
+            const uint32_t oid = __ldg(a.ids + p);
+            const float4 o = __ldg(a.st + p);
+            if (oid != my_id) acc.template add<false>(R, me.x, me.y, o);
+        }
+    }
+}
+
 // The wider ring out of line, so that it does not set the register budget of
 // the common one-ring case.
 template <bool STRICT>
@@ -94,6 +170,11 @@ __device__ __noinline__ void columns_runs_5(const ForceArgs& a, const Rep& R, in
                                             Acc<STRICT>& acc) {
     columns_runs<5>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
 }
+
+template <bool STRICT>
+__device__ __forceinline__ void force_finish(const ForceArgs& a, const Rep& R, uint32_t i,
+                                             float4 me, uint32_t my_id, unsigned long long step,
+                                             const Acc<STRICT>& acc);
 
 template <bool STRICT, int QMODE>
 __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uint32_t i) {
@@ -110,7 +191,11 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
             // run; fetch every run's bounds before touching candidates
             if (mj <= Mj) {
 #if KB_FORCE_COL3
+#if KB_FORCE_FLAT
+                if (Mi - mi < 3) columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+#else
                 if (Mi - mi < 3) columns_runs<3>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+#endif
                 else columns_runs_5(a, R, mi, Mi, mj, Mj, me, my_id, acc);
 #else
                 columns_runs<5>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
@@ -150,6 +235,15 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
         }
     }
 
+    force_finish<STRICT>(a, R, i, me, my_id, step, acc);
+}
+
+// bird.rs:84-153 after the candidate sums: the next state at slot i of the
+// write list, its bag key and the arrival count of that bag.
+template <bool STRICT>
+__device__ __forceinline__ void force_finish(const ForceArgs& a, const Rep& R, uint32_t i,
+                                             float4 me, uint32_t my_id, unsigned long long step,
+                                             const Acc<STRICT>& acc) {
     const float4 nxt = finish_bird<STRICT>(R, me, my_id, step, acc);
     const float nx = nxt.x, ny = nxt.y;
     a.out_st[i] = nxt;
@@ -188,6 +282,7 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
 template <bool STRICT, int QMODE, bool MULTI>
 __global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI : KB_FORCE_MINB)
     k_flock_force(ForceArgs a) {
+    pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     if (MULTI) {
@@ -463,6 +558,129 @@ __global__ void __launch_bounds__(256) k_rebin(RebinArgs a) {
     }
 }
 
+// ---------------------------------------------------------- two-pass scan
+// For up to SCAN2_MAX_TILES tiles the offsets are a reduce-then-scan pair of
+// launches with no waiting between blocks: per-tile sums, then every tile
+// adds the sums before it (at most SCAN2_MAX_TILES / 256 loads a thread),
+// scans its items and writes them.  Larger inputs take the single-pass
+// look-back kernel above.  The sums go into the look-back state words as
+// plain 64-bit values: their flag bits stay zero, so a later look-back
+// launch on the same buffer reads them as "not published".
+constexpr int S2_ITEMS = KB_SCAN2_ITEMS;
+
+// Exclusive block scan of one value per thread (SCAN_THREADS threads).
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* s_warp, uint32_t* total) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < SCAN_THREADS / 32; ++w) {
+        const uint32_t v = s_warp[w];
+        if (w < warp) base += v;
+        tot += v;
+    }
+    *total = tot;
+    return base + incl - x;
+}
+
+template <int ITEMS>
+__device__ __forceinline__ void load_items(const uint32_t* in, uint32_t n, uint64_t base,
+                                           uint32_t (&v)[ITEMS]) {
+    if (base + ITEMS <= n) {
+        const uint4* p = reinterpret_cast<const uint4*>(in + base);
+#pragma unroll
+        for (int k = 0; k < ITEMS / 4; ++k) {
+            const uint4 w = p[k];
+            v[4 * k] = w.x; v[4 * k + 1] = w.y; v[4 * k + 2] = w.z; v[4 * k + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) v[k] = (base + k < n) ? in[base + k] : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_tile_sums(const uint32_t* __restrict__ in, uint32_t n, unsigned long long* __restrict__ sums) {
+    pdl_enter();
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN2_TILE + (uint64_t)threadIdx.x * S2_ITEMS;
+    uint32_t v[S2_ITEMS];
+    load_items<S2_ITEMS>(in, n, base, v);
+    uint32_t t = 0;
+#pragma unroll
+    for (int k = 0; k < S2_ITEMS; ++k) t += v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int w = 0; w < SCAN_THREADS / 32; ++w) s += s_warp[w];
+        sums[blockIdx.x] = (unsigned long long)s;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan_tiles(uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n,
+                 const unsigned long long* __restrict__ sums, int zero_in, uint32_t ntiles) {
+    pdl_enter();
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32], s_red[SCAN_THREADS / 32];
+    const uint32_t tile = blockIdx.x, tid = threadIdx.x;
+    // this tile's prefix: the sums of the tiles before it
+    uint32_t part = 0;
+    for (uint32_t k = tid; k < tile; k += SCAN_THREADS) part += (uint32_t)sums[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) s_red[tid >> 5] = part;
+    const uint64_t base = (uint64_t)tile * SCAN2_TILE + (uint64_t)tid * S2_ITEMS;
+    uint32_t v[S2_ITEMS];
+    load_items<S2_ITEMS>(in, n, base, v);
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int k = 0; k < S2_ITEMS; ++k) tsum += v[k];
+    uint32_t total;
+    const uint32_t texcl = block_excl_scan(tsum, s_warp, &total);  // syncs s_red too
+    uint32_t prefix = 0;
+#pragma unroll
+    for (int w = 0; w < SCAN_THREADS / 32; ++w) prefix += s_red[w];
+    uint32_t run = prefix + texcl;
+    if (base + S2_ITEMS <= n) {
+        uint32_t o[S2_ITEMS];
+#pragma unroll
+        for (int k = 0; k < S2_ITEMS; ++k) {
+            o[k] = run;
+            run += v[k];
+        }
+        uint4* p = reinterpret_cast<uint4*>(out + base);
+#pragma unroll
+        for (int k = 0; k < S2_ITEMS / 4; ++k)
+            p[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+        if (zero_in) {
+            uint4* q = reinterpret_cast<uint4*>(in + base);
+#pragma unroll
+            for (int k = 0; k < S2_ITEMS / 4; ++k) q[k] = make_uint4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < S2_ITEMS; ++k) {
+            if (base + k < n) {
+                out[base + k] = run;
+                if (zero_in) in[base + k] = 0u;
+            }
+            run += v[k];
+        }
+    }
+    if (tile == ntiles - 1 && tid == 0) out[n] = prefix + total;
+}
+
 // ---------------------------------------------------------- segment rebin
 // One warp per segment of up to 32 consecutive bags of one column (lane l
 // owns bag c0 + l).  The arrivals of those bags sit in the write list inside
@@ -598,8 +816,12 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
     if (__any_sync(FULL_MASK, bad) && lane == 0u) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_MATERIALIZE);
 }
 
+#ifndef KB_REBIN_MINB
+#define KB_REBIN_MINB 8
+#endif
 template <bool MULTI>
-__global__ void __launch_bounds__(32 * REBIN_SEG_WARPS) k_rebin_seg(RebinArgs a) {
+__global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_seg(RebinArgs a) {
+    pdl_enter();
     __shared__ uint32_t s_cnt[REBIN_SEG_WARPS][32];
     const uint32_t w = threadIdx.x >> 5;
     const uint32_t g = blockIdx.x * REBIN_SEG_WARPS + w;
@@ -883,6 +1105,14 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
     if (nt == 0) {
         return cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
     }
+    const uint32_t nt2 = (n + SCAN2_TILE - 1) / SCAN2_TILE;
+    if (nt2 <= SCAN2_MAX_TILES) {
+        // tile_state holds scan_state_words(n) >= nt2 + 1 words: one sum per tile
+        cudaError_t e = launch_pdl(k_tile_sums, nt2, SCAN_THREADS, s, in, n, tile_state);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(k_scan_tiles, nt2, SCAN_THREADS, s, const_cast<uint32_t*>(in), out, n,
+                          tile_state, zero_in ? 1 : 0, nt2);
+    }
     k_scan<<<nt, SCAN_THREADS, 0, s>>>(in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt);
     return cudaGetLastError();
 }
@@ -891,7 +1121,7 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
     if (a.n == 0) return cudaSuccess;
     const unsigned g = grid_for(a.n, KB_FORCE_THREADS);
     const bool multi = a.nrep > 1;
-#define KB_FORCE(S, Q, MU) k_flock_force<S, Q, MU><<<g, KB_FORCE_THREADS, 0, s>>>(a)
+#define KB_FORCE(S, Q, MU) return launch_pdl(k_flock_force<S, Q, MU>, g, KB_FORCE_THREADS, s, a)
     if (strict) {
         if (qmode == 0) { if (multi) KB_FORCE(true, 0, true); else KB_FORCE(true, 0, false); }
         else { if (multi) KB_FORCE(true, 1, true); else KB_FORCE(true, 1, false); }
@@ -906,9 +1136,8 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s) {
     if (a.key != nullptr && a.nsegs > 0) {
         const unsigned gs = grid_for(a.nsegs, REBIN_SEG_WARPS);
-        if (a.nrep > 1) k_rebin_seg<true><<<gs, 32 * REBIN_SEG_WARPS, 0, s>>>(a);
-        else k_rebin_seg<false><<<gs, 32 * REBIN_SEG_WARPS, 0, s>>>(a);
-        return cudaGetLastError();
+        if (a.nrep > 1) return launch_pdl(k_rebin_seg<true>, gs, 32 * REBIN_SEG_WARPS, s, a);
+        return launch_pdl(k_rebin_seg<false>, gs, 32 * REBIN_SEG_WARPS, s, a);
     }
     const unsigned g = grid_for(a.ncells > 0 ? a.ncells : 1, 256);
     if (a.nrep > 1) k_rebin<true><<<g, 256, 0, s>>>(a);

@@ -20,6 +20,17 @@ struct ScanCtl {
 };
 constexpr uint32_t SCAN_TILE = 4096;  // items per CTA (256 threads x 16)
 inline uint32_t scan_tiles(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+// Items per tile of the two-pass scan (inputs of up to SCAN2_MAX_TILES tiles).
+#ifndef KB_SCAN2_ITEMS
+#define KB_SCAN2_ITEMS 4
+#endif
+constexpr uint32_t SCAN2_TILE = 256u * KB_SCAN2_ITEMS;
+constexpr uint32_t SCAN2_MAX_TILES = 4096;
+// 64-bit state words a scan of n items needs (either form).
+inline uint32_t scan_state_words(uint32_t n) {
+    const uint32_t a = scan_tiles(n), b = (n + SCAN2_TILE - 1) / SCAN2_TILE;
+    return (a > b ? a : b) + 1u;
+}
 
 // Exclusive scan of in[0..n) into out[0..n]; out[n] = total.  When zero_in,
 // in[] is cleared as it is read (the histogram is ready for the next step).
