@@ -206,6 +206,8 @@ kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear);
 /* Wait for the handle's stream; returns KB_ERR_DEVICE_FLAG if a kernel
  * raised the error word. */
 kb_status kb_field_synchronize(kb_field* f);
+/* The same four moments for a plain field (kb_batch_moments). */
+kb_status kb_field_moments(kb_field* f, double out4[4]);
 /* The handle's CUDA stream (a cudaStream_t), for recording events or
  * ordering other work against the handle's kernels. */
 kb_status kb_field_cuda_stream(kb_field* f, void** stream);
@@ -272,6 +274,13 @@ kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps,
 /* Replica r's read buffer (ids, {x,y,dx,dy}) in its stored order. */
 kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* states, size_t cap,
                                size_t* n);
+/* Flock observables for model exploration (no reference counterpart: the
+ * reference's explore! macros read user-defined output fields of the State,
+ * model_exploration.rs:160-449).  out[4r..4r+3] = {boids, sum dx, sum dy,
+ * sum |(dx, dy)|} of replica r's current headings (last_d), reduced on the
+ * device in double: the polar order parameter is |(sum dx, sum dy)| / sum |d|,
+ * the mean speed sum |d| / boids. */
+kb_status kb_batch_moments(kb_batch* b, double* out);
 kb_status kb_batch_synchronize(kb_batch* b);
 kb_status kb_batch_cuda_stream(kb_batch* b, void** stream);
 kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty);

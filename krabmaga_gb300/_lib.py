@@ -181,6 +181,8 @@ _SIGS = {
     "kb_batch_step": (C.c_int32, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]),
     "kb_batch_get_replica": (C.c_int32, [_P, C.c_uint32, _U32, _F, C.c_size_t, _SZ]),
     "kb_batch_synchronize": (C.c_int32, [_P]),
+    "kb_batch_moments": (C.c_int32, [_P, C.POINTER(C.c_double)]),
+    "kb_field_moments": (C.c_int32, [_P, C.POINTER(C.c_double)]),
     "kb_batch_cuda_stream": (C.c_int32, [_P, C.POINTER(_P)]),
     "kb_batch_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "kb_batch_step_stats": (C.c_int32, [_P, _U32]),

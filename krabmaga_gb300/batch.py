@@ -91,6 +91,13 @@ class Batch:
     def synchronize(self) -> None:
         L.call("kb_batch_synchronize", self._h)
 
+    def moments(self) -> np.ndarray:
+        """[nrep, 4]: boids, sum dx, sum dy, sum |(dx, dy)| of each replica's
+        headings, reduced on the device in double."""
+        out = np.zeros((len(self.sizes), 4), np.float64)
+        L.call("kb_batch_moments", self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
     def get_replica(self, r: int):
         n = C.c_size_t()
         cap = self.sizes[r]

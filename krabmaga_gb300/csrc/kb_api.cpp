@@ -1871,6 +1871,33 @@ kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* st
     return check_flags(f);
 }
 
+// Moments of every replica's headings, reduced on the device.
+static kb_status field_moments(kb_field* f, double* out) {
+    DeviceGuard g(f->device);
+    kb_status st = materialize(f);
+    if (st) return st;
+    if ((st = upload_rep(f))) return st;
+    const uint32_t nr = (uint32_t)f->reps.size();
+    DevBuf<double> d;
+    cudaError_t e = d.alloc(4 * (size_t)nr);
+    if (e) return cuda_fail(e, "moments");
+    KB_CUDA(launch_moments(f->d_rep.p, nr, f->start[f->cur].p, f->rst.p, d.p, f->stream));
+    KB_CUDA(cudaMemcpyAsync(out, d.p, sizeof(double) * 4 * nr, cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return check_flags(f);
+}
+
+kb_status kb_batch_moments(kb_batch* b, double* out) {
+    if (!b || !out) return fail(KB_ERR_ARG, "null argument");
+    return field_moments(b->f, out);
+}
+
+kb_status kb_field_moments(kb_field* f, double out4[4]) {
+    if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
+    if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: use kb_batch_moments");
+    return field_moments(f, out4);
+}
+
 kb_status kb_batch_synchronize(kb_batch* b) {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     return kb_field_synchronize(b->f);

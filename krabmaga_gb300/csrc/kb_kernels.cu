@@ -1066,6 +1066,46 @@ __global__ void k_repack(const PackEntry* __restrict__ plan, int32_t nplan, uint
     dst_dead[i] = 0;
 }
 
+// Per replica (one block each): {count, sum dx, sum dy, sum |(dx, dy)|} of
+// the read buffer, in double.
+__global__ void __launch_bounds__(256) k_moments(const Rep* __restrict__ reps,
+                                                 const uint32_t* __restrict__ start,
+                                                 const float4* __restrict__ st, double* out) {
+    __shared__ double s_acc[4][8];
+    const Rep& R = reps[blockIdx.x];
+    const uint32_t lo = start[R.cell_off], hi = start[R.cell_off + R.ncells];
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        const float4 o = st[k];
+        const double dx = (double)o.z, dy = (double)o.w;
+        a0 += dx;
+        a1 += dy;
+        a2 += sqrt(dx * dx + dy * dy);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_acc[0][w] = a0;
+        s_acc[1][w] = a1;
+        s_acc[2][w] = a2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < 3; ++k)
+            for (int v = 0; v < 8; ++v) t[k] += s_acc[k][v];
+        out[4 * blockIdx.x + 0] = (double)(hi - lo);
+        out[4 * blockIdx.x + 1] = t[0];
+        out[4 * blockIdx.x + 2] = t[1];
+        out[4 * blockIdx.x + 3] = t[2];
+    }
+}
+
 __global__ void k_set_rep(Rep* dst, Rep v) { *dst = v; }
 __global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
 __global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst += v; }
@@ -1081,6 +1121,13 @@ cudaError_t launch_repack(const PackEntry* plan, int32_t nplan, uint32_t total, 
     if (total == 0 || nplan <= 0) return cudaSuccess;
     k_repack<<<grid_for(total, 256), 256, 0, s>>>(plan, nplan, total, reps, src_st, src_ids, dst_st,
                                                    dst_ids, dst_key, dst_dead, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_moments(const Rep* reps, uint32_t nrep, const uint32_t* start, const float4* st,
+                           double* out, cudaStream_t s) {
+    if (nrep == 0) return cudaSuccess;
+    k_moments<<<nrep, 256, 0, s>>>(reps, start, st, out);
     return cudaGetLastError();
 }
 

@@ -85,6 +85,9 @@ inline uint32_t rep_segments(const Rep& R) {
     return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
 }
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s);
+// out[4r..4r+3] = {boids, sum dx, sum dy, sum |(dx,dy)|} of replica r's read buffer.
+cudaError_t launch_moments(const Rep* reps, uint32_t nrep, const uint32_t* start, const float4* st,
+                           double* out, cudaStream_t s);
 
 // General stable counting sort of the write list by key (insertion order
 // kept inside each bag): histogram, scatter, per-bag canonicalisation.

@@ -1,0 +1,184 @@
+"""Model exploration on the device: the explore! / explore_parallel! macros
+(src/explore/model_exploration.rs:56-151, 354-432) for the Flockers model.
+
+Every run of every configuration becomes one replica of a single batch
+(kb_batch_*), so a whole exploration advances in the same launches; the
+outputs are flock observables reduced on the device (kb_batch_moments).
+The dataframe has the reference's columns (build_dataframe!,
+model_exploration.rs:451-520) and write_csv follows lib.rs:1781-1792.
+"""
+from __future__ import annotations
+
+import csv
+import enum
+import time
+from dataclasses import dataclass, field, replace
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .batch import Batch, Replica
+from .model import FlockParams, gen_uniform
+
+
+class ExploreMode(enum.Enum):
+    """lib.rs:481-486 (the reference's spelling)."""
+
+    Exaustive = 0  # every combination of the inputs
+    Matched = 1    # the i-th value of every input together
+
+
+def build_configurations(n_conf: int, inputs: Sequence[Sequence]) -> List[List[int]]:
+    """Index table of the exhaustive mode (lib.rs:1724-1749): row m holds, for
+    configuration i, the index into input m.  The first input varies slowest
+    and the last fastest (the cartesian product in input order)."""
+    table = []
+    rep = n_conf
+    for values in inputs:
+        size = len(values)
+        rep //= size
+        table.append([(i // rep) % size for i in range(n_conf)])
+    return table
+
+
+@dataclass
+class FlockerConfig:
+    """The non-swept part of a Flockers exploration.  Any field, or any
+    FlockParams field, may be named as an input instead."""
+
+    initial_flockers: int = 1000
+    dim: float = 200.0                      # square torus side
+    discretization: Optional[float] = None  # None: neighbor_radius / 1.5 (a 3x3 stencil)
+    heading_scale: float = 1.0              # initial headings: unit vectors (0: the reference's zero)
+    params: FlockParams = field(default_factory=FlockParams)
+    init_seed: int = 0                      # run k (in row order) starts from Philox(init_seed + k)
+
+
+_CONFIG_FIELDS = ("initial_flockers", "dim", "discretization", "heading_scale")
+_PARAM_FIELDS = ("cohesion", "avoidance", "consistency", "randomness", "momentum", "jump",
+                 "neighbor_radius")
+
+
+def _order(m: np.ndarray) -> float:
+    return float(np.hypot(m[1], m[2]) / m[3]) if m[3] > 0 else 0.0
+
+
+# Output observables: name -> function of a replica's moments row
+# {boids, sum dx, sum dy, sum |d|}.
+OUTPUTS = {
+    "order": _order,                                                # polar order parameter
+    "mean_speed": lambda m: float(m[3] / m[0]) if m[0] else 0.0,    # mean |last_d|
+    "mean_heading_x": lambda m: float(m[1] / m[0]) if m[0] else 0.0,
+    "mean_heading_y": lambda m: float(m[2] / m[0]) if m[0] else 0.0,
+    "boids": lambda m: int(m[0]),
+}
+
+
+def _apply(cfg: FlockerConfig, name: str, value) -> FlockerConfig:
+    if name in _CONFIG_FIELDS:
+        return replace(cfg, **{name: value})
+    if name in _PARAM_FIELDS:
+        return replace(cfg, params=replace(cfg.params, **{name: float(value)}))
+    raise ValueError(f"unknown input {name!r}: one of {_CONFIG_FIELDS + _PARAM_FIELDS}")
+
+
+def _replica(cfg: FlockerConfig, seed: int) -> Replica:
+    side = float(np.float32(cfg.dim))
+    d = cfg.discretization
+    if d is None:
+        d = float(np.float32(cfg.params.neighbor_radius) / np.float32(1.5))
+    params = replace(cfg.params, seed=seed)
+    state = gen_uniform(int(cfg.initial_flockers), side, side, seed, cfg.heading_scale)
+    return Replica(side, side, float(d), params, state)
+
+
+def explore(nstep: int, rep_conf: int, inputs: Dict[str, Sequence], outputs: Sequence[str],
+            mode: ExploreMode = ExploreMode.Exaustive, base: Optional[FlockerConfig] = None,
+            device: int = 0) -> List[dict]:
+    """Run every configuration rep_conf times for nstep steps, all runs as one
+    device batch, and return the dataframe rows: "Simulation" (configuration
+    index), "Run" (0-based, as explore_parallel!), the inputs, the outputs,
+    "Run Duration" (seconds of the whole batch) and "Step per sec".
+
+    With ExploreMode.Matched every input must have the same length."""
+    base = base or FlockerConfig()
+    names = list(inputs)
+    values = [list(inputs[k]) for k in names]
+    for o in outputs:
+        if o not in OUTPUTS:
+            raise ValueError(f"unknown output {o!r}: one of {sorted(OUTPUTS)}")
+    if mode == ExploreMode.Exaustive:
+        n_conf = int(np.prod([len(v) for v in values])) if values else 1
+        table = build_configurations(n_conf, values)
+        conf_values = [[values[m][table[m][i]] for m in range(len(names))] for i in range(n_conf)]
+    else:
+        lens = {len(v) for v in values}
+        if len(lens) > 1:
+            raise ValueError("ExploreMode.Matched needs inputs of equal length")
+        n_conf = lens.pop() if lens else 1
+        conf_values = [[v[i] for v in values] for i in range(n_conf)]
+    if n_conf == 0 or rep_conf <= 0:
+        return []
+    configs = []
+    for vals in conf_values:
+        cfg = base
+        for k, v in zip(names, vals):
+            cfg = _apply(cfg, k, v)
+        configs.append(cfg)
+    reps = [_replica(configs[i], base.init_seed + i * rep_conf + j)
+            for i in range(n_conf) for j in range(rep_conf)]
+    b = Batch(reps, device=device)
+    try:
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.step(0, nstep, 1, 100)
+        b.synchronize()
+        secs = time.perf_counter() - t0
+        mom = b.moments()
+    finally:
+        b.close()
+    rows = []
+    for i in range(n_conf):
+        for j in range(rep_conf):
+            row = {"Simulation": i, "Run": j}
+            row.update({k: v for k, v in zip(names, conf_values[i])})
+            m = mom[i * rep_conf + j]
+            row.update({o: OUTPUTS[o](m) for o in outputs})
+            row["Run Duration"] = secs
+            row["Step per sec"] = nstep / secs if secs > 0 else float("inf")
+            rows.append(row)
+    return rows
+
+
+def _debug(v) -> str:
+    """Rust's {:?} of the value: floats keep a fractional part ("1.0")."""
+    if isinstance(v, (bool, np.bool_)):
+        return "true" if v else "false"
+    if isinstance(v, (int, np.integer)):
+        return str(int(v))
+    if isinstance(v, (float, np.floating)):
+        s = np.format_float_positional(np.float64(v), unique=True, trim="-")
+        return s if ("." in s or "inf" in s or "nan" in s) else s + ".0"
+    return repr(v)
+
+
+def _display(v) -> str:
+    """Rust's to_string() of an f32 (shortest repr, no forced fraction)."""
+    return np.format_float_positional(np.float32(v), unique=True, trim="-")
+
+
+def write_csv(name: str, rows: Sequence[dict]) -> str:
+    """lib.rs:1781-1792: "<name>.csv", one header row (the dataframe's field
+    names), then one row per run.  Returns the path."""
+    path = f"{name}.csv"
+    with open(path, "w", newline="") as fh:
+        w = csv.writer(fh)
+        if rows:
+            keys = list(rows[0])
+            w.writerow(keys)
+            for r in rows:
+                w.writerow([str(r[k]) if k in ("Simulation", "Run")
+                            else _display(r[k]) if k in ("Run Duration", "Step per sec")
+                            else _debug(r[k]) for k in keys])
+    return path

@@ -271,6 +271,13 @@ class Field2D:
                C.c_uint32(steps_per_trial), cand, C.c_int32(nc), best, C.byref(ms))
         return int(best[0]), int(best[1]), int(best[2]), float(ms.value)
 
+    def moments(self) -> np.ndarray:
+        """[4]: boids, sum dx, sum dy, sum |(dx, dy)| of the read buffer's
+        headings, reduced on the device in double."""
+        out = np.zeros(4, np.float64)
+        L.call("kb_field_moments", self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
     def set_kernel_timing(self, enable: bool) -> None:
         """Record CUDA events around the force / scan / rebin launches of
         ungraphed separate-kernel steps (kb_flock_step calls of < 4 steps)."""

@@ -1,0 +1,83 @@
+"""The exploration adapter's host logic (no GPU): the configuration table of
+build_configurations! (lib.rs:1724-1749), the two explore modes, and the CSV
+layout of build_dataframe! / write_csv (model_exploration.rs:451-520,
+lib.rs:1781-1792)."""
+import csv
+import importlib
+import itertools
+import os
+
+import pytest
+
+import krabmaga_gb300 as kg
+ex = importlib.import_module("krabmaga_gb300.explore")  # the module (the package exports the function)
+
+
+def reference_table(n_conf, inputs):
+    # a line-by-line transcription of the macro's loops: each row gets n_conf
+    # blocks of `rep` equal indices, of which the first n_conf are used
+    table = []
+    rep = n_conf
+    for values in inputs:
+        row = []
+        size = len(values)
+        rep //= size
+        i = 0
+        for _ in range(n_conf):
+            for _ in range(rep):
+                row.append(i)
+            i = (i + 1) % size
+        table.append(row[:n_conf])
+    return table
+
+
+@pytest.mark.parametrize("sizes", [[2, 3], [3, 1, 2], [4], [2, 2, 2, 2]])
+def test_configuration_table_matches_the_macro(sizes):
+    inputs = [list(range(s)) for s in sizes]
+    n = 1
+    for s in sizes:
+        n *= s
+    got = kg.build_configurations(n, inputs)
+    assert got == reference_table(n, inputs)
+    # the first input varies slowest: the cartesian product in input order
+    combos = [tuple(got[m][i] for m in range(len(sizes))) for i in range(n)]
+    assert combos == list(itertools.product(*inputs))
+
+
+def test_unknown_names_are_rejected():
+    with pytest.raises(ValueError):
+        ex._apply(ex.FlockerConfig(), "gravity", 1.0)
+    with pytest.raises(ValueError):
+        kg.explore(10, 1, {"cohesion": [1.0]}, ["temperature"])
+
+
+def test_matched_mode_needs_equal_lengths():
+    with pytest.raises(ValueError):
+        kg.explore(10, 1, {"cohesion": [1.0, 2.0], "jump": [0.5]}, ["order"],
+                   kg.ExploreMode.Matched)
+
+
+def test_inputs_reach_the_replica():
+    cfg = ex.FlockerConfig(initial_flockers=50, dim=100.0)
+    cfg = ex._apply(cfg, "neighbor_radius", 12.0)
+    cfg = ex._apply(cfg, "initial_flockers", 70)
+    r = ex._replica(cfg, seed=5)
+    assert r.n == 70 and r.params.neighbor_radius == 12.0 and r.params.seed == 5
+    assert r.discretization == pytest.approx(8.0)
+
+
+def test_csv_layout(tmp_path):
+    rows = [{"Simulation": 0, "Run": 0, "cohesion": 1.0, "initial_flockers": 300,
+             "order": 0.25, "Run Duration": 0.5, "Step per sec": 2000.0},
+            {"Simulation": 0, "Run": 1, "cohesion": 1.0, "initial_flockers": 300,
+             "order": 0.125, "Run Duration": 0.5, "Step per sec": 2000.0}]
+    path = kg.write_csv(os.path.join(tmp_path, "exp"), rows)
+    assert path.endswith("exp.csv")
+    with open(path) as fh:
+        got = list(csv.reader(fh))
+    assert got[0] == ["Simulation", "Run", "cohesion", "initial_flockers", "order",
+                      "Run Duration", "Step per sec"]
+    # inputs/outputs as Rust's {:?} (1.0 keeps its fraction), the timings as
+    # f32 to_string() (2000 has none)
+    assert got[1] == ["0", "0", "1.0", "300", "0.25", "0.5", "2000"]
+    assert got[2][4] == "0.125"

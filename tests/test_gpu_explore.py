@@ -1,0 +1,57 @@
+"""The exploration adapter on the GPU: every row of an exhaustive exploration
+equals the same run done alone on a plain field, with the observable
+computed on the host from its final state."""
+import ctypes as C
+import importlib
+
+import numpy as np
+import pytest
+
+import krabmaga_gb300 as kg
+from krabmaga_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+ex = importlib.import_module("krabmaga_gb300.explore")
+
+
+def host_order(st):
+    d = st[:, 2:].astype(np.float64)
+    return float(np.hypot(d[:, 0].sum(), d[:, 1].sum()) / np.hypot(d[:, 0], d[:, 1]).sum())
+
+
+def test_exhaustive_rows_equal_single_runs(gpu, tmp_path):
+    base = kg.FlockerConfig(initial_flockers=400, dim=130.0, init_seed=100,
+                            params=kg.FlockParams(arith=kg.KB_ARITH_STRICT))
+    inputs = {"cohesion": [0.5, 1.5], "neighbor_radius": [8.0, 12.0]}
+    rows = kg.explore(25, 2, inputs, ["order", "mean_speed", "boids"], kg.ExploreMode.Exaustive,
+                      base)
+    assert len(rows) == 8
+    assert [(r["Simulation"], r["Run"]) for r in rows] == [(i, j) for i in range(4) for j in range(2)]
+    assert [(r["cohesion"], r["neighbor_radius"]) for r in rows[::2]] == \
+        [(0.5, 8.0), (0.5, 12.0), (1.5, 8.0), (1.5, 12.0)]
+    for k, r in enumerate(rows):
+        cfg = base
+        for name in inputs:
+            cfg = ex._apply(cfg, name, r[name])
+        rep = ex._replica(cfg, base.init_seed + k)
+        f = kg.Field2D(rep.width, rep.height, rep.discretization, True)
+        f.set_locations(*rep.state)
+        f.lazy_update()
+        L.call("kb_flock_step", f.handle, C.byref(rep.params.to_c()), C.c_uint64(0), C.c_uint32(25))
+        _, st = f.get_state()
+        assert r["boids"] == 400
+        assert r["order"] == pytest.approx(host_order(st), rel=1e-9)
+        m = f.moments()
+        assert m[0] == 400 and r["mean_speed"] == pytest.approx(m[3] / 400, rel=1e-12)
+        f.close()
+    assert rows[0]["Step per sec"] > 0
+    path = kg.write_csv(str(tmp_path / "flockers"), rows)
+    assert open(path).readline().strip() == \
+        "Simulation,Run,cohesion,neighbor_radius,order,mean_speed,boids,Run Duration,Step per sec"
+
+
+def test_matched_mode(gpu):
+    rows = kg.explore(10, 1, {"jump": [0.3, 0.9], "initial_flockers": [200, 500]}, ["boids"],
+                      kg.ExploreMode.Matched, kg.FlockerConfig(dim=100.0))
+    assert [(r["jump"], r["initial_flockers"], r["boids"]) for r in rows] == \
+        [(0.3, 200, 200), (0.9, 500, 500)]
