@@ -165,6 +165,7 @@ struct kb_field {
     bool p_loc_differs = false;
     // step temporaries
     DevBuf<uint32_t> hist, cursor, tid, tsrc, rkey, tkey;
+    bool hist_counted = false;  // a force pass has counted arrivals into hist (no scan since)
     DevBuf<float4> tst;
     DevBuf<ScanCtl> scan_ctl, aux_ctl;
     DevBuf<unsigned long long> tstate, aux_tstate;
@@ -288,6 +289,8 @@ kb_status grow(kb_field* f, uint32_t need) {
         (e = wid.alloc(c)) || (e = wkey.alloc(c)) || (e = tid.alloc(c)) || (e = tsrc.alloc(c)) ||
         (e = wdead.alloc(c)) || (e = rkey.alloc(c)) || (e = tkey.alloc(c)))
         return cuda_fail(e, "growing object storage");
+    // no removal marks outside the live write list (they are cleared as consumed)
+    KB_CUDA(cudaMemsetAsync(wdead.p, 0, c, f->stream));
     if (f->rn) {
         KB_CUDA(cudaMemcpyAsync(rst.p, f->rst.p, sizeof(float4) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
         KB_CUDA(cudaMemcpyAsync(rid.p, f->rid.p, sizeof(uint32_t) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
@@ -406,7 +409,13 @@ kb_status ensure_aux_scan(kb_field* f, uint32_t n) {
 kb_status general_rebuild(kb_field* f, bool counted) {
     cudaStream_t s = f->stream;
     const int nxt = 1 - f->cur;
-    if (!counted) KB_CUDA(launch_hist_list(f->wkey.p, f->wdead.p, f->wn, f->hist.p, s));
+    if (!counted) {
+        // a force pass may have counted the list before it was edited
+        if (f->hist_counted)
+            KB_CUDA(cudaMemsetAsync(f->hist.p, 0, sizeof(uint32_t) * f->ncells_total, s));
+        KB_CUDA(launch_hist_list(f->wkey.p, f->wdead.p, f->wn, f->hist.p, s));
+    }
+    f->hist_counted = false;  // the scan below zeroes it
     KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
     KB_CUDA(launch_scatter_list(f->wkey.p, f->wdead.p, f->wst.p, f->wid.p, f->wn, f->start[nxt].p, f->cursor.p, f->tst.p, f->tid.p, f->tsrc.p, s));
     KB_CUDA(launch_canon(f->start[nxt].p, f->ncells_total, f->tst.p, f->tid.p, f->tsrc.p, f->cursor.p, f->rst.p, f->rid.p, s));
@@ -418,6 +427,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     cudaStream_t s = f->stream;
     const int nxt = 1 - f->cur;
     KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    f->hist_counted = false;
     if (f->kt_cur >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[f->kt_cur].ev[2], s));
     RebinArgs a;
     a.reps = f->d_rep.p;
@@ -460,6 +470,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     // only names the cause, at two extra discretisations per boid.
     a.check_moves = 0;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
+    f->hist_counted = true;
     return KB_OK;
 }
 
@@ -808,6 +819,8 @@ kb_status field_lazy_update(kb_field* f) {
         if (st) return st;
         f->rn = total;
     }
+    // the removal marks are consumed: the next write list starts with none
+    if (f->w_has_dead && f->wn) KB_CUDA(cudaMemsetAsync(f->wdead.p, 0, f->wn, f->stream));
     f->wn = 0;
     f->w_from_compute = false;
     f->w_has_dead = false;

@@ -55,6 +55,7 @@ _SIGS = {
                                        C.c_size_t]),
     "orc_neighbor_digest": (None, [_P, C.c_int, C.c_float, C.c_size_t, _F, _U32, _U32]),
     "orc_flock_run": (C.c_int, [_P, C.POINTER(Params), C.c_uint64, C.c_uint32]),
+    "orc_flock_compute": (C.c_int, [_P, C.POINTER(Params), C.c_uint64]),
     "orc_flock_step_fp64": (C.c_size_t, [_P, C.POINTER(Params), C.c_uint64, _U32, _D,
                                          C.c_size_t]),
     "orc_simulate_timed": (C.c_double, [C.c_float, C.c_float, C.c_float, C.POINTER(Params),
@@ -181,6 +182,11 @@ class OracleField:
     def flock_run(self, p: Params, first_step, nsteps):
         r = lib.orc_flock_run(self.h, C.byref(p), first_step, nsteps)
         if r != 0:
+            raise IndexError("reference panics during the step")
+
+    def flock_compute(self, p: Params, step):
+        """The agent pass only (every bird into the write buffer), no lazy_update."""
+        if lib.orc_flock_compute(self.h, C.byref(p), step) != 0:
             raise IndexError("reference panics during the step")
 
     def flock_step_fp64(self, p: Params, step):

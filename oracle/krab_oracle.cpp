@@ -438,13 +438,21 @@ void read_order(const Field2D& f, std::vector<Bird>& agents) {
 // steps against the read buffer and writes into the write buffer, then
 // State::update -> lazy_update swaps them.  The caller has already done the
 // step-0 lazy_update (schedule.rs:349-351).
-bool flock_step(Field2D& f, const FlockParams& p, uint64_t step) {
+// The agent pass of one Schedule::step (schedule.rs:395-408): every agent
+// of the read buffer, in read order, writes its next state into the write
+// buffer.  The field's lazy_update follows separately.
+bool flock_compute(Field2D& f, const FlockParams& p, uint64_t step) {
     std::vector<Bird> agents, vec;
     read_order(f, agents);
     for (const Bird& a : agents) {
         Bird nb = bird_step(f, p, a, step, vec);
         if (!f.set_object_location(nb, nb.x, nb.y)) return false;
     }
+    return true;
+}
+
+bool flock_step(Field2D& f, const FlockParams& p, uint64_t step) {
+    if (!flock_compute(f, p, step)) return false;
     f.lazy_update();
     return true;
 }
@@ -648,6 +656,10 @@ void orc_neighbor_digest(void* fp, int kind, float dist, size_t nq, const float*
 // `nsteps` Schedule::step calls of the Flocker model on field f, with step
 // numbers first_step.. (parity mode: read-buffer iteration order).  The field
 // must already hold the agents in its read buffer.  0 ok, -1 reference panic.
+int orc_flock_compute(void* fp, const orc_params* pp, uint64_t step) {
+    return flock_compute(*(Field2D*)fp, to_params(pp), step) ? 0 : -1;
+}
+
 int orc_flock_run(void* fp, const orc_params* pp, uint64_t first_step, uint32_t nsteps) {
     Field2D* f = (Field2D*)fp;
     FlockParams p = to_params(pp);

@@ -367,3 +367,46 @@ def test_true_torus_option_matches_oracle(gpu, kind, side, radius):
     g2.lazy_update()
     cc, _ = g2.neighbor_lists(kind, radius, st[:, :2])
     assert (gc >= cc).all() and gc.sum() > cc.sum()
+
+
+def test_births_and_deaths_between_steps_match_oracle(gpu):
+    # A changing population, as the reference runs one: an agent that stops
+    # is not re-inserted (schedule.rs:401-407), a newborn is inserted during
+    # the step, and both show after lazy_update.  Here: the agent pass
+    # (kb_flock_compute), removals and insertions on the write buffer, then
+    # lazy_update; the oracle does the same and the read buffers must agree.
+    side = 300.0
+    ids0, xy0, dxy0 = kg.gen_uniform(2000, side, side, 21, 1.0)
+    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=8, arith=kg.KB_ARITH_STRICT)
+    rng = np.random.default_rng(4)
+    next_id, alive = 2000, 2000
+    for s in range(8):
+        L.call("kb_flock_compute", f.handle, C.byref(p.to_c()), C.c_uint64(s))
+        o.flock_compute(oracle.params_from(p), s)
+        wids, wst, _ = o.iter(0)  # the write buffer after the agent pass
+        for k in rng.choice(len(wids), size=25, replace=False):
+            loc = kg.Real2D(float(wst[k, 0]), float(wst[k, 1]))
+            f.remove_object_location(kg.Bird(int(wids[k]), loc), loc)
+            o.remove(int(wids[k]), float(wst[k, 0]), float(wst[k, 1]))
+        nb = 15 + 5 * s
+        bid = np.arange(next_id, next_id + nb, dtype=np.uint32)
+        bxy = (rng.random((nb, 2)) * side).astype(np.float32)
+        bdxy = (rng.standard_normal((nb, 2)) * 0.5).astype(np.float32)
+        next_id += nb
+        alive += nb - 25
+        f.set_locations(bid, bxy, bdxy)
+        o.set_many(bid, bxy, bdxy)
+        f.lazy_update()
+        o.lazy_update()
+        ids, st = f.get_state()
+        oids, ost, _ = o.iter(1)
+        assert len(ids) == alive
+        assert np.array_equal(ids, oids) and same_bits(st, ost), s
+    # whole steps continue from the edited population
+    step(f, p, 8, 5)
+    o.flock_run(oracle.params_from(p), 8, 5)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
