@@ -166,6 +166,12 @@ struct kb_field {
     // step temporaries
     DevBuf<uint32_t> hist, cursor, tid, tsrc, rkey, tkey;
     bool hist_counted = false;  // a force pass has counted arrivals into hist (no scan since)
+    // Several replicas: block tables of the force and segment-rebin kernels
+    // ({replica, first boid} / {replica, first segment}), no block spanning
+    // two replicas; rebuilt with the replica table.
+    DevBuf<uint2> blk_force, blk_seg;
+    std::vector<uint2> blk_force_h, blk_seg_h;
+    uint32_t nblk_force = 0, nblk_seg = 0;
     DevBuf<float4> tst;
     DevBuf<ScanCtl> scan_ctl, aux_ctl;
     DevBuf<unsigned long long> tstate, aux_tstate;
@@ -320,6 +326,38 @@ void assign_segments(std::vector<Rep>& reps) {
     }
 }
 
+// The per-replica block tables of a packed field (see kb_field::blk_force).
+kb_status build_rep_blocks(kb_field* f) {
+    f->nblk_force = f->nblk_seg = 0;
+    if (f->reps.size() < 2) return KB_OK;
+    auto& bf = f->blk_force_h;
+    auto& bs = f->blk_seg_h;
+    bf.clear();
+    bs.clear();
+    for (uint32_t r = 0; r < (uint32_t)f->reps.size(); ++r) {
+        const Rep& R = f->reps[r];
+        for (uint64_t i = 0; i < R.nboids; i += FORCE_THREADS) bf.push_back(make_uint2(r, R.boid_off + (uint32_t)i));
+        const uint32_t ns = rep_segments(R);
+        for (uint32_t g = 0; g < ns; g += REBIN_SEG_WARPS) bs.push_back(make_uint2(r, R.seg_off + g));
+    }
+    if (bf.size() > f->blk_force.n) {
+        cudaError_t e = f->blk_force.alloc(std::max<size_t>(bf.size(), 2 * f->blk_force.n));
+        if (e) return cuda_fail(e, "replica block table");
+    }
+    if (bs.size() > f->blk_seg.n) {
+        cudaError_t e = f->blk_seg.alloc(std::max<size_t>(bs.size(), 2 * f->blk_seg.n));
+        if (e) return cuda_fail(e, "replica block table");
+    }
+    if (!bf.empty())
+        KB_CUDA(cudaMemcpyAsync(f->blk_force.p, bf.data(), sizeof(uint2) * bf.size(), cudaMemcpyHostToDevice, f->stream));
+    if (!bs.empty())
+        KB_CUDA(cudaMemcpyAsync(f->blk_seg.p, bs.data(), sizeof(uint2) * bs.size(), cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    f->nblk_force = (uint32_t)bf.size();
+    f->nblk_seg = (uint32_t)bs.size();
+    return KB_OK;
+}
+
 // Segments of the segment rebin over all replicas.
 uint32_t total_segments(const kb_field* f) {
     uint64_t t = 0;
@@ -339,6 +377,7 @@ kb_status upload_rep(kb_field* f) {
     } else {
         KB_CUDA(cudaMemcpyAsync(f->d_rep.p, f->reps.data(), sizeof(Rep) * f->reps.size(), cudaMemcpyHostToDevice, f->stream));
         KB_CUDA(cudaStreamSynchronize(f->stream));
+        if (kb_status st = build_rep_blocks(f)) return st;
     }
     return KB_OK;
 }
@@ -440,6 +479,8 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     a.a_ids = f->wid.p;
     a.ncells = f->ncells_total;
     a.nsegs = total_segments(f);
+    a.sblk = f->nblk_seg ? f->blk_seg.p : nullptr;
+    a.nsblk = f->nblk_seg;
     a.s_st = f->rst.p;
     a.s_ids = f->rid.p;
     a.step = bump_step ? f->dstep.p : nullptr;
@@ -469,6 +510,8 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     // exactly its counted arrivals) reports any miss.  The per-boid move check
     // only names the cause, at two extra discretisations per boid.
     a.check_moves = 0;
+    a.blk = f->nblk_force ? f->blk_force.p : nullptr;
+    a.nblk = f->nblk_force;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
     f->hist_counted = true;
     return KB_OK;
@@ -495,6 +538,8 @@ kb_status materialize(kb_field* f) {
     r.a_ids = buf_ids(f, f->a_last);
     r.ncells = f->ncells_total;
     r.nsegs = total_segments(f);
+    r.sblk = f->nblk_seg ? f->blk_seg.p : nullptr;
+    r.nsblk = f->nblk_seg;
     r.s_st = buf_st(f, dst);
     r.s_ids = buf_ids(f, dst);
     r.step = nullptr;
@@ -898,6 +943,10 @@ kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uin
         delete f;
         return cuda_fail(e, "creating field");
     }
+    if (kb_status st = build_rep_blocks(f)) {
+        delete f;
+        return st;
+    }
     if (capacity) {
         kb_status st = grow(f, capacity);
         if (st) {
@@ -927,7 +976,7 @@ kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
     f->drop_graphs();
     KB_CUDA(cudaMemcpyAsync(f->d_rep.p, f->reps.data(), sizeof(Rep) * reps.size(), cudaMemcpyHostToDevice, f->stream));
     KB_CUDA(cudaStreamSynchronize(f->stream));
-    return KB_OK;
+    return build_rep_blocks(f);
 }
 
 }  // namespace

@@ -272,6 +272,7 @@ __device__ __forceinline__ void force_finish(const ForceArgs& a, const Rep& R, u
 #ifndef KB_FORCE_THREADS
 #define KB_FORCE_THREADS 256
 #endif
+static_assert(KB_FORCE_THREADS == FORCE_THREADS, "the host block tables assume this block size");
 #ifndef KB_FORCE_MINB
 #define KB_FORCE_MINB 6
 #endif
@@ -279,19 +280,32 @@ __device__ __forceinline__ void force_finish(const ForceArgs& a, const Rep& R, u
 #define KB_FORCE_MINB_MULTI 6
 #endif
 
+// A replica record into shared memory, one word per thread (blockDim >= words).
+__device__ __forceinline__ void load_rep_shared(Rep* dst, const Rep* src) {
+    constexpr int WORDS = sizeof(Rep) / 4;
+    static_assert(sizeof(Rep) % 4 == 0 && WORDS <= 256, "replica record words");
+    if (threadIdx.x < WORDS)
+        reinterpret_cast<uint32_t*>(dst)[threadIdx.x] = __ldg(reinterpret_cast<const uint32_t*>(src) + threadIdx.x);
+}
+
 template <bool STRICT, int QMODE, bool MULTI>
 __global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI : KB_FORCE_MINB)
     k_flock_force(ForceArgs a) {
     pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
     if (MULTI) {
-        // the replica record stays in global memory (L1-cached field loads):
-        // a register copy of it does not fit the 40-register budget
-        force_body<STRICT, QMODE>(a, a.reps[rep_of_boid(a.reps, a.nrep, i)], i);
-    } else {
-        force_body<STRICT, QMODE>(a, a.rep0, i);
+        // one replica per block: its record is read once into shared memory
+        __shared__ Rep sR;
+        const uint2 e = a.blk[blockIdx.x];
+        load_rep_shared(&sR, a.reps + e.x);
+        __syncthreads();
+        const uint32_t k = e.y + threadIdx.x;
+        if (k >= sR.boid_off + sR.nboids) return;
+        force_body<STRICT, QMODE>(a, sR, k);
+        return;
     }
+    if (i >= a.n) return;
+    force_body<STRICT, QMODE>(a, a.rep0, i);
 }
 
 // ---------------------------------------------------------- scan
@@ -692,7 +706,10 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 // order, a per-bag counter in shared memory carries the rank across batches.
 // That is the per-bag insertion order of the reference's lazy_update.
 constexpr uint32_t FULL_MASK = 0xFFFFFFFFu;
-constexpr int REBIN_SEG_WARPS = 8;
+
+__device__ __forceinline__ uint32_t rep_segments_dev(const Rep& R) {
+    return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
+}
 
 __device__ __forceinline__ int rep_of_seg(const Rep* reps, int nrep, uint32_t g) {
     int lo = 0, hi = nrep - 1;
@@ -824,11 +841,21 @@ __global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_s
     pdl_enter();
     __shared__ uint32_t s_cnt[REBIN_SEG_WARPS][32];
     const uint32_t w = threadIdx.x >> 5;
-    const uint32_t g = blockIdx.x * REBIN_SEG_WARPS + w;
     if (blockIdx.x == 0 && threadIdx.x == 0 && a.step != nullptr) *a.step += 1ull;
+    if (MULTI) {
+        // one replica per block: its record is read once into shared memory
+        __shared__ Rep sR;
+        const uint2 e = a.sblk[blockIdx.x];
+        load_rep_shared(&sR, a.reps + e.x);
+        __syncthreads();
+        const uint32_t g = e.y + w;
+        if (g >= sR.seg_off + rep_segments_dev(sR)) return;  // whole warps
+        rebin_segment(a, sR, g, s_cnt[w]);
+        return;
+    }
+    const uint32_t g = blockIdx.x * REBIN_SEG_WARPS + w;
     if (g >= a.nsegs) return;  // whole warps
-    if (MULTI) rebin_segment(a, a.reps[rep_of_seg(a.reps, a.nrep, g)], g, s_cnt[w]);
-    else rebin_segment(a, a.rep0, g, s_cnt[w]);
+    rebin_segment(a, a.rep0, g, s_cnt[w]);
 }
 
 // ---------------------------------------------------------- general sort
@@ -1166,8 +1193,9 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
 
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
-    const unsigned g = grid_for(a.n, KB_FORCE_THREADS);
     const bool multi = a.nrep > 1;
+    if (multi && a.blk == nullptr) return cudaErrorInvalidValue;
+    const unsigned g = multi ? a.nblk : grid_for(a.n, KB_FORCE_THREADS);
 #define KB_FORCE(S, Q, MU) return launch_pdl(k_flock_force<S, Q, MU>, g, KB_FORCE_THREADS, s, a)
     if (strict) {
         if (qmode == 0) { if (multi) KB_FORCE(true, 0, true); else KB_FORCE(true, 0, false); }
@@ -1181,9 +1209,9 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
 }
 
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s) {
-    if (a.key != nullptr && a.nsegs > 0) {
+    if (a.key != nullptr && a.nsegs > 0 && (a.nrep == 1 || a.sblk != nullptr)) {
+        if (a.nrep > 1) return launch_pdl(k_rebin_seg<true>, a.nsblk, 32 * REBIN_SEG_WARPS, s, a);
         const unsigned gs = grid_for(a.nsegs, REBIN_SEG_WARPS);
-        if (a.nrep > 1) return launch_pdl(k_rebin_seg<true>, gs, 32 * REBIN_SEG_WARPS, s, a);
         return launch_pdl(k_rebin_seg<false>, gs, 32 * REBIN_SEG_WARPS, s, a);
     }
     const unsigned g = grid_for(a.ncells > 0 ? a.ncells : 1, 256);

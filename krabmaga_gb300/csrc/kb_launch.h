@@ -56,7 +56,12 @@ struct ForceArgs {
     uint32_t* hist;
     uint32_t* err;
     int32_t check_moves;  // flag moves the stencil-gather rebin cannot follow
+    // several replicas: one block per entry {replica, first boid}; no block
+    // spans two replicas (built by the host with the replica table)
+    const uint2* blk;
+    uint32_t nblk;
 };
+constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
 
 // Stencil-gather rebin: builds the canonical read buffer of the next step
@@ -74,6 +79,10 @@ struct RebinArgs {
     const uint32_t* a_ids;
     uint32_t ncells;
     uint32_t nsegs;  // 32-bag column segments over all replicas (0: per-bag kernel only)
+    // several replicas: one block per entry {replica, first segment}, up to
+    // REBIN_SEG_WARPS segments of that replica
+    const uint2* sblk;
+    uint32_t nsblk;
     float4* s_st;
     uint32_t* s_ids;
     unsigned long long* step;
@@ -81,6 +90,7 @@ struct RebinArgs {
 };
 // Bag segments of the segment rebin: SEG_ROWS consecutive bags of one column.
 constexpr int SEG_ROWS = 32;
+constexpr int REBIN_SEG_WARPS = 8;  // segments (warps) per block
 inline uint32_t rep_segments(const Rep& R) {
     return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
 }
