@@ -4,6 +4,8 @@ The reference's own tests (tests/engine/field_2d.rs:31-246) against the GPU
 field, and the field's queries against the oracle on random fields: the
 returned lists must equal the oracle's bit for bit, in the same visiting order.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -11,6 +13,7 @@ import krabmaga_gb300 as kg
 import oracle
 from conftest import C1_D
 from krabmaga_gb300 import Bird, Real2D
+from krabmaga_gb300 import _lib as L
 
 pytestmark = pytest.mark.gpu
 
@@ -197,3 +200,30 @@ def test_write_buffer_semantics_match_oracle(gpu):
         gi, gs = g.get_state()
         oi, os_, _ = o.iter(1)
         assert np.array_equal(gi, oi) and np.array_equal(gs, os_)
+
+
+def test_empty_single_and_growing_fields(gpu):
+    p = kg.FlockParams(seed=1, arith=kg.KB_ARITH_STRICT)
+    pc = p.to_c()
+    # no boids at all: steps run and leave nothing
+    f = kg.Field2D(50.0, 50.0, C1_D, True)
+    f.lazy_update()
+    L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(0), C.c_uint32(5))
+    ids, st = f.get_state()
+    assert len(ids) == 0 and f.nagents == 0
+    assert len(f.get_neighbors_within_relax_distance(Real2D(25.0, 25.0), 10.0)) == 0
+    # one boid (its only candidate is itself) and a field grown from no
+    # capacity to 5,000 boids, against the oracle
+    for n in (1, 5000):
+        ids0, xy0, dxy0 = kg.gen_uniform(n, 200.0, 200.0, 3, 1.0)
+        g = kg.Field2D(200.0, 200.0, C1_D, True, capacity_hint=0)
+        g.set_locations(ids0, xy0, dxy0)
+        g.lazy_update()
+        o = oracle.OracleField(200.0, 200.0, C1_D, True)
+        o.set_many(ids0, xy0, dxy0)
+        o.lazy_update()
+        L.call("kb_flock_step", g.handle, C.byref(pc), C.c_uint64(0), C.c_uint32(12))
+        o.flock_run(oracle.params_from(p), 0, 12)
+        gi, gs = g.get_state()
+        oi, os_, _ = o.iter(1)
+        assert np.array_equal(gi, oi) and np.array_equal(gs.view(np.uint32), os_.view(np.uint32))
