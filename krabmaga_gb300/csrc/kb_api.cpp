@@ -468,7 +468,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
     f->hist_counted = false;
     if (f->kt_cur >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[f->kt_cur].ev[2], s));
-    RebinArgs a;
+    RebinArgs a{};
     a.reps = f->d_rep.p;
     a.nrep = nrep(f);
     a.rep0 = f->reps[0];
@@ -491,7 +491,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
 }
 
 kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
-    ForceArgs a;
+    ForceArgs a{};
     a.reps = f->d_rep.p;
     a.nrep = nrep(f);
     a.rep0 = f->reps[0];
@@ -527,7 +527,7 @@ kb_status materialize(kb_field* f) {
     if (!f->virt) return KB_OK;
     int dst = 0;
     if (f->a_last == 0) dst = 1;  // the write list sits in rst: gather into wst, then swap roles
-    RebinArgs r;
+    RebinArgs r{};
     r.reps = f->d_rep.p;
     r.nrep = nrep(f);
     r.rep0 = f->reps[0];
@@ -1137,7 +1137,7 @@ static kb_status query_points(kb_field* f, int kind, float dist, size_t nq, cons
     if (!e && digest) e = ddig.alloc(n);
     if (e) return cuda_fail(e, "query buffers");
     KB_CUDA(cudaMemcpyAsync(dq.p, qxy, sizeof(float2) * n, cudaMemcpyHostToDevice, f->stream));
-    QueryArgs a;
+    QueryArgs a{};
     a.rep = f->rep;
     a.kind = kind;
     a.dist = dist;

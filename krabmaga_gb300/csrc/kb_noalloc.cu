@@ -116,7 +116,7 @@ extern "C" kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind,
     if (pin.err != cudaSuccess) return cuda_fail(pin.err, "selecting the field's device");
     unsigned char* scratch = nullptr;
     if (kb_status st = scratch_for_device(field_device(f), &scratch)) return st;
-    QueryArgs a;
+    QueryArgs a{};
     cudaStream_t s = nullptr;
     if (kb_status st = field_query_view(f, kind, dist, &a, &s)) return st;
     if (nq == 0) return KB_OK;
