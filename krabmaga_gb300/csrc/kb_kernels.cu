@@ -100,13 +100,6 @@ __device__ __forceinline__ void accumulate_run(const Rep& R, const float4* __res
     else accumulate_run_t<STRICT, false>(R, st, ids, s, e, me, my_id, acc);
 }
 
-#ifndef KB_FORCE_COL3
-#define KB_FORCE_COL3 1
-#endif
-#ifndef KB_FORCE_FLAT
-#define KB_FORCE_FLAT 1
-#endif
-
 // The candidate runs of up to NC columns (one contiguous run of bags per
 // column), every run's bounds loaded before any candidate.
 template <int NC, bool STRICT>
@@ -190,16 +183,10 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
             // clamped range: each column's bags mj..Mj are one contiguous
             // run; fetch every run's bounds before touching candidates
             if (mj <= Mj) {
-#if KB_FORCE_COL3
-#if KB_FORCE_FLAT
+                // a one-bag ring (the common case) as one flat list; the wider
+                // two-bag ring out of line
                 if (Mi - mi < 3) columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc);
-#else
-                if (Mi - mi < 3) columns_runs<3>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
-#endif
                 else columns_runs_5(a, R, mi, Mi, mj, Mj, me, my_id, acc);
-#else
-                columns_runs<5>(a, R, mi, Mi, mj, Mj, me, my_id, acc);
-#endif
             }
         } else {
             for (int ci = mi; ci <= Mi; ++ci) {
@@ -836,6 +823,7 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
 #ifndef KB_REBIN_MINB
 #define KB_REBIN_MINB 8
 #endif
+
 template <bool MULTI>
 __global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_seg(RebinArgs a) {
     pdl_enter();
