@@ -98,12 +98,18 @@ constexpr uint32_t STREAM_JITTER = 0u;   // ctr = (id, step lo, step hi, 0)
 constexpr uint32_t STREAM_INIT = 1u;     // ctr = (id, attempt, 0, 1)
 
 // ------------------------------------------------------- reference helpers
-// Rust `f as i32`: saturating, NaN -> 0.
+// Rust `f as i32`: truncation, saturating, NaN -> 0.  On the device that is
+// the conversion instruction itself (cvt.rzi.s32.f32 saturates and maps NaN
+// to 0); on the host the checks are spelled out.
 KB_HD int32_t as_i32(float v) {
+#ifdef __CUDA_ARCH__
+    return __float2int_rz(v);
+#else
     if (!(v == v)) return 0;
     if (v >= 2147483647.0f) return 2147483647;
     if (v <= -2147483648.0f) return (-2147483647 - 1);
     return (int32_t)v;
+#endif
 }
 
 // field_2d.rs:926-932

@@ -119,7 +119,6 @@ __device__ __forceinline__ int32_t disc_d(float v, float d, float inv_d) {
     return as_i32(f);
 }
 __device__ __forceinline__ int32_t disc(float v, const Rep& R) { return disc_d(v, R.d, R.inv_d); }
-
 // x / dh and x % dh for a replica's bag index (x < 2^32).
 __device__ __forceinline__ uint32_t div_dh(uint32_t x, const Rep& R) {
     return (uint32_t)__umul64hi((unsigned long long)x, R.dh_magic);

@@ -227,3 +227,26 @@ def test_empty_single_and_growing_fields(gpu):
         gi, gs = g.get_state()
         oi, os_, _ = o.iter(1)
         assert np.array_equal(gi, oi) and np.array_equal(gs.view(np.uint32), os_.view(np.uint32))
+
+
+def test_query_radius_edge_values_match_oracle(gpu):
+    # the device's float -> i32 conversion must act as Rust's `as i32`
+    # (truncate, saturate, NaN -> 0) in floor(dist / d): a NaN radius gives a
+    # one-bag range (dd = 0) in both, a huge one the whole matrix
+    side, d = 60.0, 2.5
+    rng = np.random.default_rng(8)
+    ids = np.arange(500, dtype=np.uint32)
+    xy = (rng.random((500, 2)) * side).astype(np.float32)
+    dxy = np.zeros((500, 2), np.float32)
+    g = kg.Field2D(side, side, d, True)
+    g.set_locations(ids, xy, dxy)
+    g.lazy_update()
+    o = oracle.OracleField(side, side, d, True)
+    o.set_many(ids, xy, dxy)
+    o.lazy_update()
+    q = xy[:40]
+    for r in (float("nan"), 1.0e6, 2.5, 2.4999998):
+        for kind in (kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT):
+            gc, gl = g.neighbor_lists(kind, r, q)
+            oc, ol = o.neighbor_lists(kind, r, q)
+            assert np.array_equal(gc, oc) and np.array_equal(gl, ol), (r, kind)
