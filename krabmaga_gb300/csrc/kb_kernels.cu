@@ -309,6 +309,7 @@ __device__ __forceinline__ unsigned long long pack_tile(uint32_t epoch, unsigned
 __global__ void __launch_bounds__(SCAN_THREADS)
     k_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n, ScanCtl* ctl,
            unsigned long long* tstate, uint32_t* err, int zero_in, uint32_t ntiles) {
+    pdl_enter();
     __shared__ uint32_t s_tile, s_epoch, s_prefix;
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1175,8 +1176,7 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
         return launch_pdl(k_scan_tiles, nt2, SCAN_THREADS, s, const_cast<uint32_t*>(in), out, n,
                           tile_state, zero_in ? 1 : 0, nt2);
     }
-    k_scan<<<nt, SCAN_THREADS, 0, s>>>(in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt);
-    return cudaGetLastError();
+    return launch_pdl(k_scan, nt, SCAN_THREADS, s, in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt);
 }
 
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s) {

@@ -25,7 +25,10 @@ inline uint32_t scan_tiles(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE;
 #define KB_SCAN2_ITEMS 4
 #endif
 constexpr uint32_t SCAN2_TILE = 256u * KB_SCAN2_ITEMS;
-constexpr uint32_t SCAN2_MAX_TILES = 4096;
+#ifndef KB_SCAN2_MAX
+#define KB_SCAN2_MAX 4096
+#endif
+constexpr uint32_t SCAN2_MAX_TILES = KB_SCAN2_MAX;
 // 64-bit state words a scan of n items needs (either form).
 inline uint32_t scan_state_words(uint32_t n) {
     const uint32_t a = scan_tiles(n), b = (n + SCAN2_TILE - 1) / SCAN2_TILE;
