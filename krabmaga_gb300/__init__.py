@@ -10,7 +10,8 @@ from ._lib import KB_CELL_WRAP_CLAMP, KB_CELL_WRAP_TORUS
 from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
-from .explore import ExploreMode, FlockerConfig, build_configurations, explore, write_csv
+from .explore import (ExploreMode, FlockerConfig, build_configurations, explore, random_search,
+                      write_csv)
 from .model import (FlockParams, Flocker, Schedule, State, gen_clustered, gen_uniform, simulate,
                     simulate_old)
 
@@ -20,7 +21,8 @@ __all__ = [
     "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
     "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
-    "ExploreMode", "FlockerConfig", "build_configurations", "explore", "write_csv",
+    "ExploreMode", "FlockerConfig", "build_configurations", "explore", "random_search",
+    "write_csv",
 ]
 
 

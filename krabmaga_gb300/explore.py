@@ -6,6 +6,7 @@ Every run of every configuration becomes one replica of a single batch
 outputs are flock observables reduced on the device (kb_batch_moments).
 The dataframe has the reference's columns (build_dataframe!,
 model_exploration.rs:451-520) and write_csv follows lib.rs:1781-1792.
+random_search drives the same batches (random_search.rs).
 """
 from __future__ import annotations
 
@@ -13,7 +14,7 @@ import csv
 import enum
 import time
 from dataclasses import dataclass, field, replace
-from typing import Dict, List, Optional, Sequence
+from typing import Callable, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -182,3 +183,50 @@ def write_csv(name: str, rows: Sequence[dict]) -> str:
                             else _display(r[k]) if k in ("Run Duration", "Step per sec")
                             else _debug(r[k]) for k in keys])
     return path
+
+
+def _observables(m: np.ndarray) -> dict:
+    return {name: fn(m) for name, fn in OUTPUTS.items()}
+
+
+def random_search(init: FlockerConfig, n_iter: int, target: float,
+                  cost_function: Callable[[dict], float],
+                  gen_sample: Callable[[FlockerConfig, np.random.Generator], FlockerConfig],
+                  batch_size: int, step: int, reps: int, seed: int = 0,
+                  device: int = 0) -> Tuple[FlockerConfig, float, List[float]]:
+    """random_search! (src/explore/random_search.rs:1-80) on the device.
+
+    Each iteration draws batch_size samples from the best configuration so
+    far (gen_sample(best, rng)), runs every sample reps times for step steps
+    (all batch_size * reps runs as one device batch), averages
+    cost_function over a sample's runs (it receives the run's observables,
+    the OUTPUTS of explore), and keeps the lowest; the search stops once the
+    best cost is <= target.  Returns (best configuration, its cost, the best
+    cost after every iteration).  Run k of the whole search starts from
+    Philox(init.init_seed + k), so a search is reproducible."""
+    rng = np.random.default_rng(seed)
+    best, min_cost = init, float(np.finfo(np.float32).max)
+    history: List[float] = []
+    run = 0
+    for _ in range(int(n_iter)):
+        samples = [gen_sample(best, rng) for _ in range(int(batch_size))]
+        reps_list = []
+        for smp in samples:
+            for _ in range(int(reps)):
+                reps_list.append(_replica(smp, init.init_seed + run))
+                run += 1
+        b = Batch(reps_list, device=device)
+        try:
+            b.step(0, int(step), 1, 100)
+            mom = b.moments()
+        finally:
+            b.close()
+        costs = [float(np.mean([cost_function(_observables(mom[i * reps + r])) for r in range(reps)]))
+                 for i in range(len(samples))]
+        k = int(np.argmin(costs))
+        if costs[k] < min_cost:
+            best, min_cost = samples[k], costs[k]
+        history.append(min_cost)
+        if min_cost <= target:
+            break
+    return best, min_cost, history

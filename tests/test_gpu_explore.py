@@ -55,3 +55,49 @@ def test_matched_mode(gpu):
                       kg.ExploreMode.Matched, kg.FlockerConfig(dim=100.0))
     assert [(r["jump"], r["initial_flockers"], r["boids"]) for r in rows] == \
         [(0.3, 200, 200), (0.9, 500, 500)]
+
+
+def test_random_search_keeps_the_best_and_stops_at_target(gpu):
+    base = kg.FlockerConfig(initial_flockers=300, dim=110.0, init_seed=7,
+                            params=kg.FlockParams(arith=kg.KB_ARITH_STRICT))
+
+    def gen(best, rng):
+        return ex._apply(ex._apply(best, "cohesion", float(rng.uniform(0.2, 2.0))),
+                         "jump", float(rng.uniform(0.3, 1.0)))
+
+    def cost(obs):  # seek a disordered flock
+        return obs["order"]
+
+    best, c, hist = kg.random_search(base, 4, -1.0, cost, gen, batch_size=3, step=15, reps=2,
+                                     seed=3)
+    assert len(hist) == 4 and all(b >= a for a, b in zip(hist[1:], hist[:-1]))
+    assert c == hist[-1]
+    # the reported cost is the mean over its runs, recomputed alone here
+    # recompute every sample of the search, in the same order, one run at a time
+    rng = np.random.default_rng(3)
+    b_cur, b_cost, run = base, float(np.finfo(np.float32).max), 0
+    for it in range(4):
+        batch = [gen(b_cur, rng) for _ in range(3)]
+        costs = []
+        for smp in batch:
+            vals = []
+            for r in range(2):
+                rep = ex._replica(smp, base.init_seed + run)
+                run += 1
+                f = kg.Field2D(rep.width, rep.height, rep.discretization, True)
+                f.set_locations(*rep.state)
+                f.lazy_update()
+                L.call("kb_flock_step", f.handle, C.byref(rep.params.to_c()), C.c_uint64(0),
+                       C.c_uint32(15))
+                _, st = f.get_state()
+                vals.append(host_order(st))
+                f.close()
+            costs.append(float(np.mean(vals)))
+        k = int(np.argmin(costs))
+        if costs[k] < b_cost:
+            b_cur, b_cost = batch[k], costs[k]
+        assert hist[it] == pytest.approx(b_cost, rel=1e-9)
+    assert best == b_cur
+    # a target that the first iteration already meets stops the search
+    _, c2, hist2 = kg.random_search(base, 5, 10.0, cost, gen, batch_size=2, step=5, reps=1)
+    assert len(hist2) == 1 and c2 <= 10.0
