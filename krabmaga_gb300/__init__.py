@@ -10,8 +10,8 @@ from ._lib import KB_CELL_WRAP_CLAMP, KB_CELL_WRAP_TORUS
 from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
-from .explore import (ExploreMode, FlockerConfig, build_configurations, explore, random_search,
-                      write_csv)
+from .explore import (ExploreMode, FlockerConfig, build_configurations, evolutionary_search,
+                      explore, random_search, write_csv)
 from .model import (FlockParams, Flocker, Schedule, State, gen_clustered, gen_uniform, simulate,
                     simulate_old)
 
@@ -22,7 +22,7 @@ __all__ = [
     "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
     "ExploreMode", "FlockerConfig", "build_configurations", "explore", "random_search",
-    "write_csv",
+    "evolutionary_search", "write_csv",
 ]
 
 

@@ -6,7 +6,8 @@ Every run of every configuration becomes one replica of a single batch
 outputs are flock observables reduced on the device (kb_batch_moments).
 The dataframe has the reference's columns (build_dataframe!,
 model_exploration.rs:451-520) and write_csv follows lib.rs:1781-1792.
-random_search drives the same batches (random_search.rs).
+random_search and evolutionary_search drive the same batches
+(random_search.rs, genetic.rs).
 """
 from __future__ import annotations
 
@@ -230,3 +231,64 @@ def random_search(init: FlockerConfig, n_iter: int, target: float,
         if min_cost <= target:
             break
     return best, min_cost, history
+
+
+def evolutionary_search(init_population: Callable[[], List],
+                        make_config: Callable[[object, int], FlockerConfig],
+                        fitness: Callable[[List[dict]], float],
+                        selection: Callable[[List[Tuple[object, float]]], None],
+                        mutation: Callable[[object], object],
+                        crossover: Callable[[List], None],
+                        cmp: Callable[[float, float], bool],
+                        desired_fitness: float, generation_num: int, step: int, reps: int = 1,
+                        init_seed: int = 0, device: int = 0) -> List[dict]:
+    """explore_ga_parallel! (src/explore/genetic.rs:626-826) on the device.
+
+    Every generation runs each individual reps times for step steps, all of
+    them as one device batch; make_config(individual, r) builds run r of an
+    individual (the reference's new_with_parameters).  fitness gets the runs'
+    observables (the OUTPUTS of explore), cmp(a, b) says that fitness a is
+    better than b.  The search stops after generation_num generations (0: no
+    limit) or in the first generation where an individual reaches
+    desired_fitness; otherwise selection(pop_fitness) filters the
+    (individual, fitness) list in place, crossover(population) edits the
+    survivors in place and mutation(individual) returns each new individual.
+    Returns one row per evaluated individual: generation, index, fitness,
+    individual and its last run's observables ("state"), as BufferGA."""
+    population = list(init_population())
+    rows: List[dict] = []
+    generation, run = 0, 0
+    while population:
+        if generation_num != 0 and generation == generation_num:
+            break
+        generation += 1
+        reps_list = []
+        for ind in population:
+            for r in range(int(reps)):
+                reps_list.append(_replica(make_config(ind, r), init_seed + run))
+                run += 1
+        b = Batch(reps_list, device=device)
+        try:
+            b.step(0, int(step), 1, 100)
+            mom = b.moments()
+        finally:
+            b.close()
+        pop_fitness = []
+        reached = False
+        for i, ind in enumerate(population):
+            obs = [_observables(mom[i * reps + r]) for r in range(int(reps))]
+            fit = float(fitness(obs))
+            rows.append({"generation": generation, "index": i, "fitness": fit, "individual": ind,
+                         "state": repr(obs[-1])})
+            pop_fitness.append((ind, fit))
+            if cmp(fit, desired_fitness):
+                reached = True
+        if reached:
+            break
+        selection(pop_fitness)
+        if len(pop_fitness) < 1:
+            break
+        population = [ind for ind, _ in pop_fitness]
+        crossover(population)
+        population = [mutation(ind) for ind in population]
+    return rows

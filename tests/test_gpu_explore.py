@@ -101,3 +101,56 @@ def test_random_search_keeps_the_best_and_stops_at_target(gpu):
     # a target that the first iteration already meets stops the search
     _, c2, hist2 = kg.random_search(base, 5, 10.0, cost, gen, batch_size=2, step=5, reps=1)
     assert len(hist2) == 1 and c2 <= 10.0
+
+
+def test_evolutionary_search_rows_equal_single_runs(gpu):
+    base = kg.FlockerConfig(initial_flockers=250, dim=100.0, init_seed=40,
+                            params=kg.FlockParams(arith=kg.KB_ARITH_STRICT))
+    rng = np.random.default_rng(9)
+
+    def init_population():
+        return [f"{c:.3f};{j:.3f}" for c, j in zip(rng.uniform(0.3, 1.8, 4), rng.uniform(0.3, 1.0, 4))]
+
+    def make_config(ind, r):
+        c, j = (float(v) for v in ind.split(";"))
+        return ex._apply(ex._apply(base, "cohesion", c), "jump", j)
+
+    def fitness(obs):
+        return float(np.mean([o["order"] for o in obs]))
+
+    def selection(pop):
+        pop.sort(key=lambda t: -t[1])
+        del pop[2:]
+
+    def crossover(population):
+        a, b = population[0].split(";"), population[1].split(";")
+        population.extend([f"{a[0]};{b[1]}", f"{b[0]};{a[1]}"])
+
+    def mutation(ind):
+        c, j = (float(v) for v in ind.split(";"))
+        return f"{min(2.0, c * 1.05):.3f};{j:.3f}"
+
+    rows = kg.evolutionary_search(init_population, make_config, fitness, selection, mutation,
+                                  crossover, lambda a, b: a > b, 2.0, 3, step=12, reps=2,
+                                  init_seed=base.init_seed)
+    assert [r["generation"] for r in rows] == [1] * 4 + [2] * 4 + [3] * 4
+    # every row's fitness equals its runs done one at a time
+    run = 0
+    for r in rows:
+        vals = []
+        for k in range(2):
+            rep = ex._replica(make_config(r["individual"], k), base.init_seed + run)
+            run += 1
+            f = kg.Field2D(rep.width, rep.height, rep.discretization, True)
+            f.set_locations(*rep.state)
+            f.lazy_update()
+            L.call("kb_flock_step", f.handle, C.byref(rep.params.to_c()), C.c_uint64(0),
+                   C.c_uint32(12))
+            _, st = f.get_state()
+            vals.append(host_order(st))
+            f.close()
+        assert r["fitness"] == pytest.approx(float(np.mean(vals)), rel=1e-9)
+    # a desired fitness reached in the first generation stops the search there
+    rows2 = kg.evolutionary_search(init_population, make_config, fitness, selection, mutation,
+                                   crossover, lambda a, b: a > b, -1.0, 5, step=5, reps=1)
+    assert {r["generation"] for r in rows2} == {1}
