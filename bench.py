@@ -7,7 +7,7 @@ Schedule::step of the whole flock: the agent pass (every Bird::step) and the
 field's lazy_update, on inputs resident in HBM.  L2 is flushed (a 512 MiB
 write) before every timed step; the JSON line says so.
 
-  python bench.py [--steps K] [--warmup W] [--workload c2|c1|c3] [--impl ours|reference]
+  python bench.py [--steps K] [--warmup W] [--workload flock1m|flock1k|clustered4m] [--impl ours|reference]
 
 --impl reference times the reference-equivalent CPU path (the oracle's
 priority-queue schedule, one host core: the reference's sequential path is
@@ -36,12 +36,12 @@ sys.path.insert(0, ROOT)
 D_C = float(np.float32(10.0) / np.float32(1.5))
 WORKLOADS = {
     # name: (n, side, seed, generator, sim steps of the workload)
-    "c1": dict(n=1000, side=200.0, seed=42, gen="uniform", steps=200,
+    "flock1k": dict(n=1000, side=200.0, seed=42, gen="uniform", steps=200,
                desc="Flockers 1,000 boids, torus 200x200"),
-    "c2": dict(n=1 << 20, side=float(np.float32(np.sqrt((1 << 20) / 0.025))), seed=7,
+    "flock1m": dict(n=1 << 20, side=float(np.float32(np.sqrt((1 << 20) / 0.025))), seed=7,
                gen="uniform", steps=1000,
                desc="Flockers 1,048,576 boids, density 0.025 (torus side 6476.34)"),
-    "c3": dict(n=1 << 22, side=12952.0, seed=11, gen="clustered", steps=500,
+    "clustered4m": dict(n=1 << 22, side=12952.0, seed=11, gen="clustered", steps=500,
                desc="Flockers 4,194,304 boids in 256 Gaussian clusters (sigma 40), torus 12952"),
 }
 METRIC = "boid-updates/s (1M boids, 1 GB300)"
@@ -59,9 +59,9 @@ def peaks():
 
 def ncu_traffic(kernel):
     """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
-    summary of the same workload (profiles/<kernel>_c2.md, a line
+    summary of the same workload (profiles/<kernel>_flock1m.md, a line
     `dram_bytes_per_launch: <int>`), or None when there is none."""
-    p = os.path.join(ROOT, "profiles", f"{kernel}_c2.md")
+    p = os.path.join(ROOT, "profiles", f"{kernel}_flock1m.md")
     if not os.path.exists(p):
         return None
     with open(p) as fh:
@@ -524,7 +524,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="flock1m", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arith", default="fast", choices=["fast", "strict"])
     ap.add_argument("--cpu-steps", type=int, default=10)

@@ -122,13 +122,13 @@ def explore(nstep: int, rep_conf: int, inputs: Dict[str, Sequence], outputs: Seq
         conf_values = [[v[i] for v in values] for i in range(n_conf)]
     if n_conf == 0 or rep_conf <= 0:
         return []
-    configs = []
+    conf_list = []
     for vals in conf_values:
         cfg = base
         for k, v in zip(names, vals):
             cfg = _apply(cfg, k, v)
-        configs.append(cfg)
-    reps = [_replica(configs[i], base.init_seed + i * rep_conf + j)
+        conf_list.append(cfg)
+    reps = [_replica(conf_list[i], base.init_seed + i * rep_conf + j)
             for i in range(n_conf) for j in range(rep_conf)]
     b = Batch(reps, device=device)
     try:

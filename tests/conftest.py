@@ -21,9 +21,9 @@ if not (os.path.exists(LIB) and os.path.exists(ORACLE)):
 
     __graft_entry__.build()
 
-# The C1 workload: 1,000 boids on a 200x200 torus, d = 10/1.5 in f32, r = 10.
-C1_SIDE = 200.0
-C1_D = float(np.float32(10.0) / np.float32(1.5))
+# The 1,000-boid flock: a 200x200 torus, bags of d = 10/1.5 in f32, radius 10.
+SIDE_1K = 200.0
+FLOCK_D = float(np.float32(10.0) / np.float32(1.5))
 
 
 def pytest_configure(config):

@@ -1,10 +1,10 @@
-"""Generates the committed C1 fixtures from the oracle.
+"""Generates the committed 1,000-boid fixtures from the oracle.
 
-C1: 1,000 boids on a 200x200 torus, discretization 10/1.5 (f32), radius 10,
+The flock: 1,000 boids on a 200x200 torus, discretization 10/1.5 (f32), radius 10,
 all weights 1.0, jump 0.7, uniform positions and unit headings from
 Philox(seed 42), jitter from Philox(seed 42).  Checkpoints of the whole read
 buffer (stored order) after 1, 10 and 200 steps, for the relaxed query
-(the spec path) and the exact query (the in-tree Bird).
+(the reference Flockers query path) and the exact query (the in-tree Bird).
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -49,5 +49,5 @@ def make(kind: int, name: str) -> None:
 
 
 if __name__ == "__main__":
-    make(0, "c1_relax_strict.npz")
-    make(1, "c1_exact_strict.npz")
+    make(0, "flock1k_relax_strict.npz")
+    make(1, "flock1k_exact_strict.npz")

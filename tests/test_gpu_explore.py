@@ -99,8 +99,8 @@ def test_random_search_keeps_the_best_and_stops_at_target(gpu):
         assert hist[it] == pytest.approx(b_cost, rel=1e-9)
     assert best == b_cur
     # a target that the first iteration already meets stops the search
-    _, c2, hist2 = kg.random_search(base, 5, 10.0, cost, gen, batch_size=2, step=5, reps=1)
-    assert len(hist2) == 1 and c2 <= 10.0
+    _, cost2, hist2 = kg.random_search(base, 5, 10.0, cost, gen, batch_size=2, step=5, reps=1)
+    assert len(hist2) == 1 and cost2 <= 10.0
 
 
 def test_evolutionary_search_rows_equal_single_runs(gpu):

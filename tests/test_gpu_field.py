@@ -11,7 +11,7 @@ import pytest
 
 import krabmaga_gb300 as kg
 import oracle
-from conftest import C1_D
+from conftest import FLOCK_D
 from krabmaga_gb300 import Bird, Real2D
 from krabmaga_gb300 import _lib as L
 
@@ -126,7 +126,7 @@ def test_out_of_matrix_location_is_an_error(gpu):
 
 def _random_fields():
     rng = np.random.default_rng(11)
-    for side, d, n, tor in [(50.0, C1_D, 400, True), (50.0, 1.7, 900, True),
+    for side, d, n, tor in [(50.0, FLOCK_D, 400, True), (50.0, 1.7, 900, True),
                             (30.0, 2.0, 300, False), (10.0, 0.5, 60, True)]:
         ids = rng.permutation(n).astype(np.uint32)
         xy = (rng.random((n, 2), dtype=np.float32) * np.float32(side)).astype(np.float32)
@@ -206,7 +206,7 @@ def test_empty_single_and_growing_fields(gpu):
     p = kg.FlockParams(seed=1, arith=kg.KB_ARITH_STRICT)
     pc = p.to_c()
     # no boids at all: steps run and leave nothing
-    f = kg.Field2D(50.0, 50.0, C1_D, True)
+    f = kg.Field2D(50.0, 50.0, FLOCK_D, True)
     f.lazy_update()
     L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(0), C.c_uint32(5))
     ids, st = f.get_state()
@@ -216,10 +216,10 @@ def test_empty_single_and_growing_fields(gpu):
     # capacity to 5,000 boids, against the oracle
     for n in (1, 5000):
         ids0, xy0, dxy0 = kg.gen_uniform(n, 200.0, 200.0, 3, 1.0)
-        g = kg.Field2D(200.0, 200.0, C1_D, True, capacity_hint=0)
+        g = kg.Field2D(200.0, 200.0, FLOCK_D, True, capacity_hint=0)
         g.set_locations(ids0, xy0, dxy0)
         g.lazy_update()
-        o = oracle.OracleField(200.0, 200.0, C1_D, True)
+        o = oracle.OracleField(200.0, 200.0, FLOCK_D, True)
         o.set_many(ids0, xy0, dxy0)
         o.lazy_update()
         L.call("kb_flock_step", g.handle, C.byref(pc), C.c_uint64(0), C.c_uint32(12))

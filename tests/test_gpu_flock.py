@@ -19,12 +19,12 @@ import pytest
 
 import krabmaga_gb300 as kg
 import oracle
-from conftest import C1_D, C1_SIDE
+from conftest import FLOCK_D, SIDE_1K
 from krabmaga_gb300 import _lib as L
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-TOL_REL_DOMAIN = 1e-5  # spec tolerance for one step vs FP64
+TOL_REL_DOMAIN = 1e-5  # the stated tolerance of one step against FP64, relative to the side
 
 
 def gpu_field(side, d, ids, xy, dxy, tor=True):
@@ -49,10 +49,10 @@ def same_bits(a, b):
     return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-@pytest.mark.parametrize("name", ["c1_relax_strict.npz", "c1_exact_strict.npz"])
-def test_c1_matches_golden_fixtures(gpu, name):
+@pytest.mark.parametrize("name", ["flock1k_relax_strict.npz", "flock1k_exact_strict.npz"])
+def test_1k_flock_matches_golden_fixtures(gpu, name):
     g = np.load(os.path.join(GOLDEN, name))
-    f = gpu_field(C1_SIDE, C1_D, g["ids0"], g["xy0"], g["dxy0"])
+    f = gpu_field(SIDE_1K, FLOCK_D, g["ids0"], g["xy0"], g["dxy0"])
     p = kg.FlockParams(seed=int(g["seed"]), query_mode=int(g["kind"]), arith=kg.KB_ARITH_STRICT)
     ids, st = f.get_state()
     counts, lists = f.neighbor_lists(int(g["kind"]), 10.0, st[:, :2])
@@ -67,10 +67,10 @@ def test_c1_matches_golden_fixtures(gpu, name):
 
 
 @pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
-def test_c1_neighbour_sets_bit_exact_every_step(gpu, kind):
-    ids0, xy0, dxy0 = kg.gen_uniform(1000, C1_SIDE, C1_SIDE, 42, 1.0)
-    f = gpu_field(C1_SIDE, C1_D, ids0, xy0, dxy0)
-    o = oracle_field(C1_SIDE, C1_D, ids0, xy0, dxy0)
+def test_1k_flock_neighbour_sets_bit_exact_every_step(gpu, kind):
+    ids0, xy0, dxy0 = kg.gen_uniform(1000, SIDE_1K, SIDE_1K, 42, 1.0)
+    f = gpu_field(SIDE_1K, FLOCK_D, ids0, xy0, dxy0)
+    o = oracle_field(SIDE_1K, FLOCK_D, ids0, xy0, dxy0)
     p = kg.FlockParams(seed=42, query_mode=kind, arith=kg.KB_ARITH_STRICT)
     op = oracle.params_from(p)
     for t in range(200):
@@ -87,9 +87,9 @@ def test_c1_neighbour_sets_bit_exact_every_step(gpu, kind):
 def test_compute_plus_lazy_update_equals_fused_steps(gpu):
     ids0, xy0, dxy0 = kg.gen_uniform(3000, 300.0, 300.0, 3, 1.0)
     p = kg.FlockParams(seed=9)
-    a = gpu_field(300.0, C1_D, ids0, xy0, dxy0)
-    b = gpu_field(300.0, C1_D, ids0, xy0, dxy0)
-    state = kg.Flocker((300.0, 300.0), 3000, C1_D, params=p)
+    a = gpu_field(300.0, FLOCK_D, ids0, xy0, dxy0)
+    b = gpu_field(300.0, FLOCK_D, ids0, xy0, dxy0)
+    state = kg.Flocker((300.0, 300.0), 3000, FLOCK_D, params=p)
     state.field1.close()
     state.field1 = a  # already initialised and past its step-0 update
     sched = kg.Schedule()
@@ -111,9 +111,9 @@ def test_fused_tiles_match_oracle(gpu, tile, kind, mode):
     # tiles exceed the shared-memory capacity and run the global scratch path
     n, side = 6000, 490.0
     ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 21, 1.0)
-    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+    f = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
     f.set_step_options(mode, *tile)
-    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    o = oracle_field(side, FLOCK_D, ids0, xy0, dxy0)
     p = kg.FlockParams(seed=5, query_mode=kind)
     step(f, p, 0, 7)
     step(f, p, 7, 6)
@@ -132,7 +132,7 @@ def test_step_modes_agree(gpu):
     p = kg.FlockParams(seed=2, arith=kg.KB_ARITH_FAST)
     out = []
     for mode in (0, 1, 2):
-        f = gpu_field(1400.0, C1_D, ids0, xy0, dxy0)
+        f = gpu_field(1400.0, FLOCK_D, ids0, xy0, dxy0)
         f.set_step_options(mode)
         step(f, p, 0, 40)
         step(f, p, 40, 3)
@@ -145,8 +145,8 @@ def test_fused_sweep_radius_two_rings(gpu):
     # radius 14 with bags of 10/1.5 gives a query ring of two bags
     ids0, xy0, dxy0 = kg.gen_uniform(3000, 350.0, 350.0, 13, 1.0)
     p = kg.FlockParams(seed=3, neighbor_radius=14.0, jump=0.9, cohesion=0.6, avoidance=1.4)
-    f = gpu_field(350.0, C1_D, ids0, xy0, dxy0)
-    o = oracle_field(350.0, C1_D, ids0, xy0, dxy0)
+    f = gpu_field(350.0, FLOCK_D, ids0, xy0, dxy0)
+    o = oracle_field(350.0, FLOCK_D, ids0, xy0, dxy0)
     step(f, p, 0, 20)
     o.flock_run(oracle.params_from(p), 0, 20)
     ids, st = f.get_state()
@@ -156,7 +156,7 @@ def test_fused_sweep_radius_two_rings(gpu):
 
 @pytest.mark.parametrize("side,d,jump,radius", [
     (284.82, 2.005, 0.795, 5.012),   # last column 0.12 wide: wraps from three lines in
-    (200.0, C1_D, 0.7, 10.0),        # side/d an exact integer: the x = w line exists
+    (200.0, FLOCK_D, 0.7, 10.0),        # side/d an exact integer: the x = w line exists
     (101.3, 4.99, 0.98, 12.0),       # ring of two bags, last column 1.5 wide
     (60.05, 6.0, 0.6, 6.5),          # small field, last column 0.05 wide
 ])
@@ -199,7 +199,7 @@ def test_steps_are_deterministic(gpu):
     ids0, xy0, dxy0 = kg.gen_uniform(20000, 900.0, 900.0, 5, 1.0)
     outs = []
     for _ in range(2):
-        f = gpu_field(900.0, C1_D, ids0, xy0, dxy0)
+        f = gpu_field(900.0, FLOCK_D, ids0, xy0, dxy0)
         step(f, kg.FlockParams(seed=3, arith=kg.KB_ARITH_FAST), 0, 50)
         outs.append(f.get_state())
     assert np.array_equal(outs[0][0], outs[1][0]) and same_bits(outs[0][1], outs[1][1])
@@ -225,8 +225,8 @@ def _fp64_one_step(side, d, ids0, xy0, dxy0, kind, arith):
 @pytest.mark.parametrize("arith", [kg.KB_ARITH_STRICT, kg.KB_ARITH_FAST])
 @pytest.mark.parametrize("kind", [kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT])
 def test_one_step_within_fp64_tolerance(gpu, arith, kind):
-    ids0, xy0, dxy0 = kg.gen_uniform(1000, C1_SIDE, C1_SIDE, 42, 1.0)
-    err = _fp64_one_step(C1_SIDE, C1_D, ids0, xy0, dxy0, kind, arith)
+    ids0, xy0, dxy0 = kg.gen_uniform(1000, SIDE_1K, SIDE_1K, 42, 1.0)
+    err = _fp64_one_step(SIDE_1K, FLOCK_D, ids0, xy0, dxy0, kind, arith)
     assert err <= TOL_REL_DOMAIN, err
 
 
@@ -249,7 +249,7 @@ def _ensemble(arith, seeds, jitter_base, n, side):
     vals = []
     for seed in seeds:
         ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 100 + seed, 1.0)
-        f = gpu_field(side, C1_D, ids0, xy0, dxy0)
+        f = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
         step(f, kg.FlockParams(seed=jitter_base + seed, arith=arith), 0, 200)
         vals.append(_order_and_neighbours(f, 0.7))
         f.close()
@@ -257,7 +257,7 @@ def _ensemble(arith, seeds, jitter_base, n, side):
 
 
 def test_long_run_statistics_fast_vs_strict(gpu):
-    """Flocks at the C1 density (0.025 boids per unit^2), 200 steps, 32
+    """Flocks at density 0.025 boids per unit^2, 200 steps, 32
     initial flocks of 20,000 boids: the ensemble means of the local order
     parameter and of the mean neighbour count under the fast arithmetic agree
     with the strict ones within 1%.  Chaos makes the two runs independent
@@ -276,14 +276,14 @@ def test_long_run_statistics_fast_vs_strict(gpu):
     assert abs(q[1] - s[1]) / s[1] < 0.01, (q, s, c, se)
 
 
-def test_c2_full_size_one_step(gpu):
+def test_1m_flock_full_size_one_step(gpu):
     """1,048,576 boids at density 0.025: neighbour digests of every boid and
     the one-step state (strict) equal the oracle's."""
     n = 1 << 20
     side = float(np.float32(np.sqrt(n / 0.025)))
     ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 7, 1.0)
-    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
-    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    f = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    o = oracle_field(side, FLOCK_D, ids0, xy0, dxy0)
     ids, st = f.get_state()
     oids, ost, _ = o.iter(1)
     assert np.array_equal(ids, oids) and same_bits(st, ost)
@@ -299,15 +299,15 @@ def test_c2_full_size_one_step(gpu):
     assert f.device_flags() == 0
 
 
-def test_c3_clustered_digests(gpu):
+def test_4m_clustered_quarter_size_digests(gpu):
     """Clustered stress (256 Gaussian clusters, sigma 40) at a quarter of the
     4,194,304-boid size: after 3 strict steps the state equals the oracle's
     and so do the neighbour digests of a sample of boids."""
     n = 1 << 20
     side = 12952.0 / 2
     ids0, xy0, dxy0 = kg.gen_clustered(n, side, side, 256, 40.0, 0.3, 11)
-    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
-    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    f = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    o = oracle_field(side, FLOCK_D, ids0, xy0, dxy0)
     p = kg.FlockParams(seed=11)
     step(f, p, 0, 3)
     o.flock_run(oracle.params_from(p), 0, 3)
@@ -328,8 +328,8 @@ def test_device_jitter_matches_oracle_philox(gpu):
     ids = np.array([12345], np.uint32)
     xy = np.array([[50.0, 50.0]], np.float32)
     dxy = np.array([[0.0, 0.0]], np.float32)
-    f = gpu_field(side, C1_D, ids, xy, dxy)
-    o = oracle_field(side, C1_D, ids, xy, dxy)
+    f = gpu_field(side, FLOCK_D, ids, xy, dxy)
+    o = oracle_field(side, FLOCK_D, ids, xy, dxy)
     p = kg.FlockParams(seed=(7 << 32) | 99, momentum=0.0)
     for t in range(5):
         step(f, p, t, 1)
@@ -346,10 +346,10 @@ def test_true_torus_option_matches_oracle(gpu, kind, side, radius):
     n = int(side * side * 0.025) + 40
     ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 17, 1.0)
     p = kg.FlockParams(seed=6, query_mode=kind, neighbor_radius=radius, arith=kg.KB_ARITH_STRICT)
-    f = kg.Field2D(side, side, C1_D, True, capacity_hint=n, cell_wrap=kg.KB_CELL_WRAP_TORUS)
+    f = kg.Field2D(side, side, FLOCK_D, True, capacity_hint=n, cell_wrap=kg.KB_CELL_WRAP_TORUS)
     f.set_locations(ids0, xy0, dxy0)
     f.lazy_update()
-    o = oracle.OracleField(side, side, C1_D, True, cell_wrap=1)
+    o = oracle.OracleField(side, side, FLOCK_D, True, cell_wrap=1)
     o.set_many(ids0, xy0, dxy0)
     o.lazy_update()
     for s in range(0, 24, 6):
@@ -362,7 +362,7 @@ def test_true_torus_option_matches_oracle(gpu, kind, side, radius):
         oc, ol = o.neighbor_lists(kind, radius, st[:, :2])
         assert np.array_equal(gc, oc) and np.array_equal(gl, ol), s
     # across the seam the wrapped range finds more than the clamped one
-    g2 = kg.Field2D(side, side, C1_D, True)
+    g2 = kg.Field2D(side, side, FLOCK_D, True)
     g2.set_locations(ids, st[:, :2].copy(), st[:, 2:].copy())
     g2.lazy_update()
     cc, _ = g2.neighbor_lists(kind, radius, st[:, :2])
@@ -377,8 +377,8 @@ def test_births_and_deaths_between_steps_match_oracle(gpu):
     # lazy_update; the oracle does the same and the read buffers must agree.
     side = 300.0
     ids0, xy0, dxy0 = kg.gen_uniform(2000, side, side, 21, 1.0)
-    f = gpu_field(side, C1_D, ids0, xy0, dxy0)
-    o = oracle_field(side, C1_D, ids0, xy0, dxy0)
+    f = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    o = oracle_field(side, FLOCK_D, ids0, xy0, dxy0)
     p = kg.FlockParams(seed=8, arith=kg.KB_ARITH_STRICT)
     rng = np.random.default_rng(4)
     next_id, alive = 2000, 2000

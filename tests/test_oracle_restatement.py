@@ -13,7 +13,7 @@ import pytest
 
 import oracle
 import py_restatement as pr
-from conftest import C1_D, C1_SIDE
+from conftest import FLOCK_D, SIDE_1K
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -50,8 +50,8 @@ def _random_flock(n, side, seed):
 
 
 @pytest.mark.parametrize("kind,side,d,radius,n", [
-    (0, 40.0, C1_D, 10.0, 80),     # relaxed query, 3x3 stencil
-    (1, 40.0, C1_D, 10.0, 80),     # exact query (check_circle)
+    (0, 40.0, FLOCK_D, 10.0, 80),     # relaxed query, 3x3 stencil
+    (1, 40.0, FLOCK_D, 10.0, 80),     # exact query (check_circle)
     (1, 10.0, 0.5, 10.0, 12),      # the reference test geometry (state.rs:11-14)
     (0, 30.0, 2.0, 5.0, 120),      # dd = 2
 ])
@@ -80,7 +80,7 @@ def test_oracle_matches_python_transcription(kind, side, d, radius, n):
 @pytest.mark.parametrize("wrap", [False, True])
 def test_queries_match_python_transcription(wrap):
     ids, xy, dxy = _random_flock(300, 50.0, seed=9)
-    for d in (C1_D, 1.7):
+    for d in (FLOCK_D, 1.7):
         py = pr.PyField(50.0, 50.0, d, wrap=wrap)
         orc = oracle.OracleField(50.0, 50.0, d, True, cell_wrap=1 if wrap else 0)
         for i, p, h in zip(ids, xy, dxy):
@@ -117,9 +117,9 @@ def test_true_torus_query_sees_across_the_seam():
 
 
 def test_golden_trajectories_reproduce():
-    """The committed C1 fixtures (generated by tests/golden/make_golden.py)."""
-    g = np.load(os.path.join(GOLDEN, "c1_relax_strict.npz"))
-    orc = oracle.OracleField(C1_SIDE, C1_SIDE, C1_D, True)
+    """The committed 1,000-boid fixtures (generated by tests/golden/make_golden.py)."""
+    g = np.load(os.path.join(GOLDEN, "flock1k_relax_strict.npz"))
+    orc = oracle.OracleField(SIDE_1K, SIDE_1K, FLOCK_D, True)
     orc.set_many(g["ids0"], g["xy0"], g["dxy0"])
     orc.lazy_update()
     p = oracle.params(seed=int(g["seed"]), query_mode=0)
