@@ -379,7 +379,7 @@ def run_ours(args, wl):
             for k in range(K):
                 flush.fill_(k & 0xFF)  # evict L2 between timed steps
                 ev[k][0].record(stream)
-                one_step(step_no)  # one persistent launch: the whole step
+                one_step(step_no)  # the whole step (its launches, chained)
                 ev[k][1].record(stream)
                 step_no += 1
         torch.cuda.synchronize(dev)

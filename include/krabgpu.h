@@ -243,9 +243,10 @@ kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind, float dist
 /* Many independent Flockers simulations (the model-exploration workload of
  * explore_parallel!, src/explore/model_exploration.rs:354-432: one
  * simulate_explore! per configuration, lines 160-190) packed into one
- * device field and stepped by one persistent launch per step (or per
- * steps_per_launch steps), each replica with its own geometry and
- * parameters. */
+ * device field, each replica with its own geometry and parameters, and
+ * stepped together: by default the force, offsets and rebin kernels run once
+ * per step over all replicas (one replica per block); the tiled step paths
+ * (kb_batch_set_step_options) group steps into launches and graphs. */
 typedef struct kb_batch kb_batch;
 typedef struct {
     float width;
@@ -266,9 +267,10 @@ kb_status kb_batch_set_replica(kb_batch* b, uint32_t r, size_t n, const uint32_t
                                const float* xy, const float* dxy);
 /* Pack every replica into the read buffer (the step-0 lazy_update). */
 kb_status kb_batch_commit(kb_batch* b);
-/* nsteps steps of every replica; steps_per_launch persistent steps per kernel
- * launch (0 = all in one); graph_launches > 1 captures that many launches
- * into one CUDA graph and replays it. */
+/* nsteps steps of every replica.  The launch grouping applies to the tiled
+ * step paths: steps_per_launch persistent steps per kernel launch (0 = all
+ * in one) and graph_launches > 1 launches captured into one CUDA graph and
+ * replayed; the default path ignores both (four launches per step). */
 kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps,
                         uint32_t steps_per_launch, uint32_t graph_launches);
 /* Replica r's read buffer (ids, {x,y,dx,dy}) in its stored order. */

@@ -1,10 +1,12 @@
-"""Batched replicas: many independent Flockers simulations in one launch.
+"""Batched replicas: many independent Flockers simulations in the same launches.
 
 The GPU form of explore_parallel! (src/explore/model_exploration.rs:354-432),
 which runs one simulate_explore! (lines 160-190) per configuration x
 repetition on rayon threads: here every replica lives in one packed device
-field and all of them advance together, one persistent launch per step (or
-per ``steps_per_launch`` steps), optionally replayed from CUDA graphs.
+field and all of them advance together.  The default step path runs the
+force, offsets and rebin kernels once per step over all replicas (each block
+belongs to one replica); the tiled paths (set_step_options(2) or (1)) take
+``steps_per_launch`` / ``graph_launches`` for their launch grouping.
 """
 from __future__ import annotations
 
