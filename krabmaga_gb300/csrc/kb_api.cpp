@@ -166,6 +166,10 @@ struct kb_field {
     // step temporaries
     DevBuf<uint32_t> hist, cursor, tid, tsrc, rkey, tkey;
     bool hist_counted = false;  // a force pass has counted arrivals into hist (no scan since)
+    // Every replica's ids are distinct in the read buffer (checked on the
+    // device after each general rebuild; the step paths keep the id multiset)
+    bool ids_unique = false;
+    DevBuf<unsigned long long> dup_tab;
     // Several replicas: block tables of the force and segment-rebin kernels
     // ({replica, first boid} / {replica, first segment}), no block spanning
     // two replicas; rebuilt with the replica table.
@@ -512,6 +516,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     a.check_moves = 0;
     a.blk = f->nblk_force ? f->blk_force.p : nullptr;
     a.nblk = f->nblk_force;
+    a.self_by_slot = f->ids_unique ? 1 : 0;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
     f->hist_counted = true;
     return KB_OK;
@@ -844,6 +849,38 @@ kb_status tiled_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
     return split_steps_graphed(f, p, nsteps, 100);
 }
 
+// ids_unique changes what the captured force launches do: drop the graphs.
+void set_ids_unique(kb_field* f, bool u) {
+    if (f->ids_unique != u) f->drop_graphs();
+    f->ids_unique = u;
+}
+
+// Whether the read buffer's ids are distinct within each replica.
+kb_status check_unique_ids(kb_field* f) {
+    if (f->rn == 0) {
+        set_ids_unique(f, true);
+        return KB_OK;
+    }
+    uint64_t cap = 1024;
+    while (cap < 2ull * f->rn) cap <<= 1;
+    if (cap > 0x80000000ull) {
+        set_ids_unique(f, false);
+        return KB_OK;
+    }
+    if (f->dup_tab.n < cap) {
+        cudaError_t e = f->dup_tab.alloc(cap);
+        if (e) return cuda_fail(e, "id check table");
+    }
+    if (kb_status st = upload_rep(f)) return st;
+    KB_CUDA(cudaMemsetAsync(f->small.p, 0, sizeof(uint32_t), f->stream));
+    KB_CUDA(launch_dup_check(f->d_rep.p, nrep(f), f->rid.p, f->rn, f->dup_tab.p, (uint32_t)cap,
+                             f->small.p, f->stream));
+    uint32_t dup = 0;
+    if (kb_status st = read_u32(f, f->small.p, &dup)) return st;
+    set_ids_unique(f, dup == 0);
+    return KB_OK;
+}
+
 kb_status field_lazy_update(kb_field* f) {
     kb_status st = flush_pending(f);
     if (st) return st;
@@ -863,6 +900,8 @@ kb_status field_lazy_update(kb_field* f) {
         st = read_u32(f, f->start[f->cur].p + f->ncells_total, &total);
         if (st) return st;
         f->rn = total;
+        // the id multiset may have changed
+        if ((st = check_unique_ids(f))) return st;
     }
     // the removal marks are consumed: the next write list starts with none
     if (f->w_has_dead && f->wn) KB_CUDA(cudaMemsetAsync(f->wdead.p, 0, f->wn, f->stream));
@@ -2104,6 +2143,7 @@ kb_status srv_repack(kb_server* S, std::vector<SrvReq*>& act) {
     f->virt = false;
     if ((st = general_rebuild(f, false))) return st;
     f->rn = (uint32_t)boids;
+    set_ids_unique(f, true);  // every request's boids are ids 0..n-1
     f->wn = 0;
     f->layout_is_positions = true;
     for (SrvReq* q : act) q->fresh = false;

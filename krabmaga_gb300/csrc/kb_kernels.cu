@@ -122,9 +122,11 @@ __device__ __forceinline__ void columns_runs(const ForceArgs& a, const Rep& R, i
 // The three runs of a one-bag ring as one flat list: a warp then iterates
 // the longest lane's total instead of the sum of the per-column maxima.
 template <bool STRICT>
+// my_slot: the boid's own read-buffer slot when ids are unique (a candidate
+// is the boid itself exactly there), else ~0u and ids are compared.
 __device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, int mi, int Mi,
                                               int mj, int Mj, float4 me, uint32_t my_id,
-                                              Acc<STRICT>& acc) {
+                                              Acc<STRICT>& acc, uint32_t my_slot) {
     uint32_t s[3], e[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -138,7 +140,13 @@ __device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, 
     const uint32_t P1 = e[0] - s[0], P2 = P1 + (e[1] - s[1]), T = P2 + (e[2] - s[2]);
     acc.vec += T;
     const uint32_t d1 = s[1] - P1, d2 = s[2] - P2;  // position = f + d (mod 2^32)
-    if (R.nowrap) {
+    if (R.nowrap && my_slot != 0xFFFFFFFFu) {
+        for (uint32_t f = 0; f < T; ++f) {
+            const uint32_t p = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
+            const float4 o = __ldg(a.st + p);
+            if (p != my_slot) acc.template add<true>(R, me.x, me.y, o);
+        }
+    } else if (R.nowrap) {
         for (uint32_t f = 0; f < T; ++f) {
             const uint32_t p = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
             const uint32_t oid = __ldg(a.ids + p);
@@ -185,7 +193,8 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
             if (mj <= Mj) {
                 // a one-bag ring (the common case) as one flat list; the wider
                 // two-bag ring out of line
-                if (Mi - mi < 3) columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc);
+                if (Mi - mi < 3)
+                    columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc, a.self_by_slot ? i : 0xFFFFFFFFu);
                 else columns_runs_5(a, R, mi, Mi, mj, Mj, me, my_id, acc);
             }
         } else {
@@ -1122,6 +1131,27 @@ __global__ void __launch_bounds__(256) k_moments(const Rep* __restrict__ reps,
     }
 }
 
+// One thread per read-buffer slot: insert (replica, id) into an open-
+// addressing table; a key that is already there is a repeat.
+__global__ void k_dup_check(const Rep* __restrict__ reps, int32_t nrep, const uint32_t* __restrict__ ids,
+                            uint32_t n, unsigned long long* table, uint32_t cap, uint32_t* dup) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t r = nrep > 1 ? (uint32_t)rep_of_boid(reps, nrep, k) : 0u;
+    const unsigned long long key = ((unsigned long long)r << 32) | ids[k];
+    uint32_t h = id_mix(ids[k] ^ (r * 0x9E3779B9u)) & (cap - 1u);
+    for (uint32_t probe = 0; probe < cap; ++probe) {  // the table is at most half full
+        const unsigned long long prev = atomicCAS(table + h, ~0ull, key);
+        if (prev == ~0ull) return;
+        if (prev == key) {
+            *dup = 1u;
+            return;
+        }
+        h = (h + 1u) & (cap - 1u);
+    }
+    *dup = 1u;  // no free slot found (cannot happen at half occupancy): be conservative
+}
+
 __global__ void k_set_rep(Rep* dst, Rep v) { *dst = v; }
 __global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
 __global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst += v; }
@@ -1144,6 +1174,15 @@ cudaError_t launch_moments(const Rep* reps, uint32_t nrep, const uint32_t* start
                            double* out, cudaStream_t s) {
     if (nrep == 0) return cudaSuccess;
     k_moments<<<nrep, 256, 0, s>>>(reps, start, st, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dup_check(const Rep* reps, int32_t nrep, const uint32_t* ids, uint32_t n,
+                             unsigned long long* table, uint32_t cap, uint32_t* dup,
+                             cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(table, 0xFF, sizeof(unsigned long long) * cap, s);
+    if (e != cudaSuccess || n == 0) return e;
+    k_dup_check<<<grid_for(n, 256), 256, 0, s>>>(reps, nrep, ids, n, table, cap, dup);
     return cudaGetLastError();
 }
 

@@ -63,6 +63,9 @@ struct ForceArgs {
     // spans two replicas (built by the host with the replica table)
     const uint2* blk;
     uint32_t nblk;
+    // ids are unique within every replica: a candidate is the boid itself
+    // exactly when it is the boid's own slot, so no id is loaded per candidate
+    int32_t self_by_slot;
 };
 constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
@@ -98,6 +101,12 @@ inline uint32_t rep_segments(const Rep& R) {
     return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
 }
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s);
+// Whether any (replica, id) pair repeats in the read buffer (n boids, nrep
+// replicas by boid_off): an open-addressing table of cap (a power of two,
+// >= 2n) 64-bit words, cleared here; *dup is set to 1 on a repeat.
+cudaError_t launch_dup_check(const Rep* reps, int32_t nrep, const uint32_t* ids, uint32_t n,
+                             unsigned long long* table, uint32_t cap, uint32_t* dup,
+                             cudaStream_t s);
 // out[4r..4r+3] = {boids, sum dx, sum dy, sum |(dx,dy)|} of replica r's read buffer.
 cudaError_t launch_moments(const Rep* reps, uint32_t nrep, const uint32_t* start, const float4* st,
                            double* out, cudaStream_t s);

@@ -410,3 +410,34 @@ def test_births_and_deaths_between_steps_match_oracle(gpu):
     ids, st = f.get_state()
     oids, ost, _ = o.iter(1)
     assert np.array_equal(ids, oids) and same_bits(st, ost)
+
+
+def test_duplicate_ids_exclude_each_other_as_the_reference_does(gpu):
+    # Bird::step skips every candidate whose id equals its own (bird.rs:50),
+    # so boids sharing an id ignore each other.  With unique ids the force
+    # pass excludes the boid's own slot instead; with repeats it must compare
+    # ids, and the trajectories still equal the oracle's.
+    ids0, xy0, dxy0 = kg.gen_uniform(3000, 350.0, 350.0, 5, 1.0)
+    ids0 = ids0.copy()
+    ids0[1::7] = ids0[0::7][: len(ids0[1::7])]
+    assert len(np.unique(ids0)) < len(ids0)
+    p = kg.FlockParams(seed=3, arith=kg.KB_ARITH_STRICT)
+    for kind in (kg.KB_QUERY_RELAX, kg.KB_QUERY_EXACT):
+        p.query_mode = kind
+        f = gpu_field(350.0, FLOCK_D, ids0, xy0, dxy0)
+        o = oracle_field(350.0, FLOCK_D, ids0, xy0, dxy0)
+        step(f, p, 0, 20)
+        o.flock_run(oracle.params_from(p), 0, 20)
+        ids, st = f.get_state()
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), kind
+        # removing the repeats (a new population through lazy_update) goes
+        # back to the slot test, still equal to the oracle
+        keep = np.unique(ids, return_index=True)[1]
+        g = gpu_field(350.0, FLOCK_D, ids[keep], st[keep, :2].copy(), st[keep, 2:].copy())
+        q = oracle_field(350.0, FLOCK_D, ids[keep], st[keep, :2].copy(), st[keep, 2:].copy())
+        step(g, p, 20, 10)
+        q.flock_run(oracle.params_from(p), 20, 10)
+        gi, gs = g.get_state()
+        qi, qs, _ = q.iter(1)
+        assert np.array_equal(gi, qi) and same_bits(gs, qs), kind
