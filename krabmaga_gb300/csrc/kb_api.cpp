@@ -1094,29 +1094,39 @@ kb_status kb_field_set_object_location(kb_field* f, uint32_t id, const float pos
 kb_status kb_field_set_locations(kb_field* f, size_t n, const uint32_t* ids, const float* xy,
                                  const float* dxy) {
     if (!f || (n && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
-    const size_t old = f->p_id.size();
-    f->p_st.reserve(old + n);
-    f->p_id.reserve(old + n);
-    f->p_key.reserve(old + n);
-    for (size_t i = 0; i < n; ++i) {
+    if (n == 0) return KB_OK;
+    if ((uint64_t)f->wn + f->p_id.size() + n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many objects");
+    DeviceGuard g(f->device);
+    // earlier single writes first (insertion order), then this batch packed
+    // on the device straight behind them
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    if (f->virt && (st = materialize(f))) return st;
+    if ((st = grow(f, f->wn + (uint32_t)n))) return st;
+    const uint32_t m = (uint32_t)n;
+    // staging in the scratch records buffer: xy in its first 8n bytes, dxy after
+    float2* sxy = reinterpret_cast<float2*>(f->tst.p);
+    float2* sdxy = sxy + m;
+    KB_CUDA(cudaMemcpyAsync(sxy, xy, sizeof(float2) * m, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemcpyAsync(sdxy, dxy, sizeof(float2) * m, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemcpyAsync(f->wid.p + f->wn, ids, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemsetAsync(f->small.p, 0xFF, sizeof(uint32_t), f->stream));
+    KB_CUDA(launch_pack_locations(f->rep, sxy, sdxy, m, f->wst.p + f->wn, f->wkey.p + f->wn,
+                                  f->wdead.p + f->wn, f->small.p, f->stream));
+    uint32_t bad = 0;
+    if ((st = read_u32(f, f->small.p, &bad))) return st;
+    if (bad != 0xFFFFFFFFu) {  // the write list is left as it was
+        const size_t i = bad;
         if (!(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) &&
-              std::isfinite(dxy[2 * i]) && std::isfinite(dxy[2 * i + 1]))) {
-            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
+              std::isfinite(dxy[2 * i]) && std::isfinite(dxy[2 * i + 1])))
             return fail(KB_ERR_ARG, "non-finite position or heading");
-        }
-        int64_t idx = host_bag_index(f->rep, xy[2 * i], xy[2 * i + 1]);
-        if (idx < 0) {
-            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
-            char buf[128];
-            std::snprintf(buf, sizeof buf, "object %zu: location outside the bag matrix (the reference panics)", i);
-            return fail(KB_ERR_RANGE, buf);
-        }
-        f->p_st.push_back(make_float4(xy[2 * i], xy[2 * i + 1], dxy[2 * i], dxy[2 * i + 1]));
-        f->p_id.push_back(ids[i]);
-        f->p_key.push_back((uint32_t)idx);
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "object %zu: location outside the bag matrix (the reference panics)", i);
+        return fail(KB_ERR_RANGE, buf);
     }
+    f->wn += m;
     if (!f->density_check) f->nagents += n;
-    if (n) f->w_from_compute = false;
+    f->w_from_compute = false;
     return KB_OK;
 }
 

@@ -1152,6 +1152,22 @@ __global__ void k_dup_check(const Rep* __restrict__ reps, int32_t nrep, const ui
     *dup = 1u;  // no free slot found (cannot happen at half occupancy): be conservative
 }
 
+__global__ void k_pack_locations(Rep R, const float2* __restrict__ xy, const float2* __restrict__ dxy,
+                                 uint32_t n, float4* __restrict__ out_st, uint32_t* __restrict__ out_key,
+                                 uint8_t* __restrict__ out_dead, uint32_t* bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 p = xy[i], d = dxy[i];
+    const int64_t idx = bag_index(R, disc(p.x, R), disc(p.y, R));
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(d.x) && isfinite(d.y)) || idx < 0) {
+        atomicMin(bad, i);
+        return;
+    }
+    out_st[i] = make_float4(p.x, p.y, d.x, d.y);
+    out_key[i] = R.cell_off + (uint32_t)idx;
+    out_dead[i] = 0;
+}
+
 __global__ void k_set_rep(Rep* dst, Rep v) { *dst = v; }
 __global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
 __global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst += v; }
@@ -1183,6 +1199,14 @@ cudaError_t launch_dup_check(const Rep* reps, int32_t nrep, const uint32_t* ids,
     cudaError_t e = cudaMemsetAsync(table, 0xFF, sizeof(unsigned long long) * cap, s);
     if (e != cudaSuccess || n == 0) return e;
     k_dup_check<<<grid_for(n, 256), 256, 0, s>>>(reps, nrep, ids, n, table, cap, dup);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_locations(const Rep& rep, const float2* xy, const float2* dxy, uint32_t n,
+                                  float4* out_st, uint32_t* out_key, uint8_t* out_dead,
+                                  uint32_t* bad, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_pack_locations<<<grid_for(n, 256), 256, 0, s>>>(rep, xy, dxy, n, out_st, out_key, out_dead, bad);
     return cudaGetLastError();
 }
 

@@ -111,6 +111,14 @@ cudaError_t launch_dup_check(const Rep* reps, int32_t nrep, const uint32_t* ids,
 cudaError_t launch_moments(const Rep* reps, uint32_t nrep, const uint32_t* start, const float4* st,
                            double* out, cudaStream_t s);
 
+// Bulk set_object_location on the device: n objects at their own positions
+// (xy and dxy as float2 arrays) appended to the write list as records, bag
+// keys and live marks; *bad takes the smallest index of an object with a
+// non-finite value or a location outside the bag matrix (~0u when none).
+cudaError_t launch_pack_locations(const Rep& rep, const float2* xy, const float2* dxy, uint32_t n,
+                                  float4* out_st, uint32_t* out_key, uint8_t* out_dead,
+                                  uint32_t* bad, cudaStream_t s);
+
 // General stable counting sort of the write list by key (insertion order
 // kept inside each bag): histogram, scatter, per-bag canonicalisation.
 cudaError_t launch_hist_list(const uint32_t* key, const uint8_t* dead, uint32_t n, uint32_t* hist,
