@@ -250,3 +250,27 @@ def test_query_radius_edge_values_match_oracle(gpu):
             gc, gl = g.neighbor_lists(kind, r, q)
             oc, ol = o.neighbor_lists(kind, r, q)
             assert np.array_equal(gc, oc) and np.array_equal(gl, ol), (r, kind)
+
+
+def test_bulk_set_rejects_bad_objects_and_keeps_the_write_buffer(gpu):
+    f = kg.Field2D(50.0, 50.0, 2.0, True)
+    f.set_object_location(Bird(1, Real2D(3.0, 4.0)), Real2D(3.0, 4.0))
+    ids = np.arange(10, 20, dtype=np.uint32)
+    xy = np.full((10, 2), 10.0, np.float32)
+    dxy = np.zeros((10, 2), np.float32)
+    xy[6] = (-5.0, 10.0)  # outside the bag matrix: the reference panics
+    with pytest.raises(kg.KbError) as e:
+        f.set_locations(ids, xy, dxy)
+    assert e.value.status == L.KB_ERR_RANGE and "object 6" in str(e.value)
+    xy[6] = (10.0, 10.0)
+    dxy[3] = (float("nan"), 0.0)
+    with pytest.raises(kg.KbError) as e:
+        f.set_locations(ids, xy, dxy)
+    assert e.value.status == L.KB_ERR_ARG
+    # the refused batches left nothing behind; a good one follows the earlier write
+    dxy[3] = (0.0, 0.0)
+    f.set_locations(ids, xy, dxy)
+    f.lazy_update()
+    got, st = f.get_state()
+    assert list(got) == [1] + list(range(10, 20))
+    assert f.nagents == 11
