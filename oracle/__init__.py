@@ -55,6 +55,9 @@ _SIGS = {
                                        C.c_size_t]),
     "orc_neighbor_digest": (None, [_P, C.c_int, C.c_float, C.c_size_t, _F, _U32, _U32]),
     "orc_flock_run": (C.c_int, [_P, C.POINTER(Params), C.c_uint64, C.c_uint32]),
+    "orc_simulate_timed_threads": (C.c_double, [C.c_float, C.c_float, C.c_float, C.POINTER(Params),
+                                                 C.c_size_t, _U32, _F, _F, C.c_uint32, C.c_uint32,
+                                                 C.POINTER(_P)]),
     "orc_flock_compute": (C.c_int, [_P, C.POINTER(Params), C.c_uint64]),
     "orc_flock_step_fp64": (C.c_size_t, [_P, C.POINTER(Params), C.c_uint64, _U32, _D,
                                          C.c_size_t]),
@@ -196,6 +199,25 @@ class OracleField:
         lib.orc_flock_step_fp64(self.h, C.byref(p), step, _u(ids),
                                 out.ctypes.data_as(_D), n)
         return ids[:n], out[:n]
+
+
+def simulate_timed_threads(w, h, d, p: Params, ids, xy, dxy, nsteps, threads, keep_field=False):
+    """The same run with the agent pass on `threads` host threads (results
+    equal to the sequential run); returns (seconds, OracleField or None)."""
+    ids = np.ascontiguousarray(ids, np.uint32)
+    xy = np.ascontiguousarray(xy, np.float32)
+    dxy = np.ascontiguousarray(dxy, np.float32)
+    out = C.c_void_p()
+    secs = lib.orc_simulate_timed_threads(w, h, d, C.byref(p), len(ids), _u(ids), _f(xy), _f(dxy),
+                                          nsteps, threads, C.byref(out) if keep_field else None)
+    f = None
+    if keep_field:
+        f = OracleField.__new__(OracleField)
+        f.h = out.value
+        dims = (C.c_int32 * 4)()
+        lib.orc_field_dims(f.h, dims)
+        f.dw, f.dh, f.max_x, f.max_y = (int(v) for v in dims)
+    return secs, f
 
 
 def simulate_timed(w, h, d, p: Params, ids, xy, dxy, nsteps, keep_field=False):

@@ -34,6 +34,7 @@
 #include <cstdint>
 #include <cstring>
 #include <queue>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -720,6 +721,51 @@ double orc_simulate_timed(float w, float h, float d, const orc_params* pp, size_
             pq.push(Event{e.time + 1.0f, e.ordering, seq++, nb});
         }
         f->lazy_update();  // schedule.rs:410-412
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    if (out_field) *out_field = f;
+    else delete f;
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// The same run with the agent pass spread over `threads` host threads
+// (not the reference: its sequential schedule runs one agent at a time, and
+// its parallel build serialises agents on one mutex, schedule.rs:187).  Every
+// agent reads the read buffer only, so the threads compute the next states
+// of consecutive agent ranges into one array; the insertion into the write
+// buffer stays sequential, in agent order, so the result equals the
+// sequential run's bit for bit.  Agents run in read-buffer order (the
+// oracle's parity order) rather than through the priority queue.
+double orc_simulate_timed_threads(float w, float h, float d, const orc_params* pp, size_t n,
+                                  const uint32_t* ids, const float* xy, const float* dxy,
+                                  uint32_t nsteps, uint32_t threads, void** out_field) {
+    FlockParams p = to_params(pp);
+    Field2D* f = new Field2D(w, h, d, true);
+    for (size_t i = 0; i < n; ++i) {
+        Bird b{ids[i], xy[2 * i], xy[2 * i + 1], dxy[2 * i], dxy[2 * i + 1]};
+        f->set_object_location(b, b.x, b.y);
+    }
+    if (threads == 0) threads = 1;
+    auto t0 = std::chrono::steady_clock::now();
+    f->lazy_update();
+    std::vector<Bird> agents, next;
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        read_order(*f, agents);
+        next.resize(agents.size());
+        const size_t m = agents.size();
+        const size_t chunk = (m + threads - 1) / threads;
+        std::vector<std::thread> pool;
+        for (uint32_t t = 0; t < threads; ++t) {
+            const size_t lo = t * chunk, hi = std::min(m, lo + chunk);
+            if (lo >= hi) break;
+            pool.emplace_back([&, lo, hi]() {
+                std::vector<Bird> vec;
+                for (size_t k = lo; k < hi; ++k) next[k] = bird_step(*f, p, agents[k], s, vec);
+            });
+        }
+        for (auto& th : pool) th.join();
+        for (const Bird& nb : next) f->set_object_location(nb, nb.x, nb.y);
+        f->lazy_update();
     }
     auto t1 = std::chrono::steady_clock::now();
     if (out_field) *out_field = f;

@@ -130,3 +130,19 @@ def test_golden_trajectories_reproduce():
         ids, st, _ = orc.iter(1)
         assert np.array_equal(ids, g[f"ids_{step}"])
         assert np.array_equal(st.view(np.uint32), g[f"st_{step}"].view(np.uint32))
+
+
+def test_threaded_timing_run_equals_the_sequential_steps():
+    # the all-cores timing run of the oracle (the agent pass on host threads,
+    # insertion in agent order) gives the parity run's state bit for bit
+    ids, xy, dxy = _random_flock(2000, 300.0, seed=4)
+    p = oracle.params(seed=5, query_mode=0)
+    _, f = oracle.simulate_timed_threads(300.0, 300.0, FLOCK_D, p, ids, xy, dxy, 6, 4,
+                                         keep_field=True)
+    o = oracle.OracleField(300.0, 300.0, FLOCK_D, True)
+    o.set_many(ids, xy, dxy)
+    o.lazy_update()
+    o.flock_run(p, 0, 6)
+    a_ids, a_st, _ = f.iter(1)
+    b_ids, b_st, _ = o.iter(1)
+    assert np.array_equal(a_ids, b_ids) and np.array_equal(a_st.view(np.uint32), b_st.view(np.uint32))
