@@ -283,6 +283,23 @@ kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* st
  * device in double: the polar order parameter is |(sum dx, sum dy)| / sum |d|,
  * the mean speed sum |d| / boids. */
 kb_status kb_batch_moments(kb_batch* b, double* out);
+/* Add a replica to a committed batch (no reference counterpart: the
+ * reference's sweep runs each configuration as its own simulation,
+ * model_exploration.rs:56-151).  The new replica gets the last index
+ * (*index); its nboids objects (ids, xy, dxy as in kb_batch_set_replica) are
+ * placed like set_object_location + lazy_update (field_2d.rs:905-921), and
+ * its step numbering starts at origin_step: a later kb_batch_step with
+ * first_step = origin_step + k advances it exactly like step k of a batch of
+ * it alone.  The other replicas keep their records in their canonical order,
+ * so their next steps are unchanged.  The objects are checked on the host
+ * first: a non-finite value (KB_ERR_ARG) or a location outside the new
+ * replica's bag matrix (KB_ERR_RANGE) leaves the batch as it was. */
+kb_status kb_batch_add_replica(kb_batch* b, const kb_replica_desc* d, const uint32_t* ids,
+                               const float* xy, const float* dxy, uint64_t origin_step,
+                               uint32_t* index);
+/* Remove replica r from a committed batch; replicas after r move down one
+ * index.  A batch keeps at least one replica (KB_ERR_STATE). */
+kb_status kb_batch_remove_replica(kb_batch* b, uint32_t r);
 kb_status kb_batch_synchronize(kb_batch* b);
 kb_status kb_batch_cuda_stream(kb_batch* b, void** stream);
 kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty);

@@ -182,6 +182,9 @@ _SIGS = {
     "kb_batch_get_replica": (C.c_int32, [_P, C.c_uint32, _U32, _F, C.c_size_t, _SZ]),
     "kb_batch_synchronize": (C.c_int32, [_P]),
     "kb_batch_moments": (C.c_int32, [_P, C.POINTER(C.c_double)]),
+    "kb_batch_add_replica": (C.c_int32, [_P, C.POINTER(ReplicaDesc), _U32, _F, _F, C.c_uint64,
+                                         C.POINTER(C.c_uint32)]),
+    "kb_batch_remove_replica": (C.c_int32, [_P, C.c_uint32]),
     "kb_field_moments": (C.c_int32, [_P, C.POINTER(C.c_double)]),
     "kb_batch_cuda_stream": (C.c_int32, [_P, C.POINTER(_P)]),
     "kb_batch_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),

@@ -37,15 +37,19 @@ class Replica:
         return len(self.state[0])
 
 
+def _fill_desc(d: L.ReplicaDesc, r: Replica) -> None:
+    d.width, d.height, d.discretization = r.width, r.height, r.discretization
+    d.toroidal = 1 if r.toroidal else 0
+    d.cell_wrap = r.cell_wrap
+    d.nboids = r.n
+    d.params = r.params.to_c()
+
+
 class Batch:
     def __init__(self, replicas: Sequence[Replica], device: int = 0):
         descs = (L.ReplicaDesc * len(replicas))()
         for d, r in zip(descs, replicas):
-            d.width, d.height, d.discretization = r.width, r.height, r.discretization
-            d.toroidal = 1 if r.toroidal else 0
-            d.cell_wrap = r.cell_wrap
-            d.nboids = r.n
-            d.params = r.params.to_c()
+            _fill_desc(d, r)
         h = C.c_void_p()
         L.call("kb_batch_create", C.c_int32(device), C.c_uint32(len(replicas)), descs, C.byref(h))
         self._h = h
@@ -99,6 +103,27 @@ class Batch:
         out = np.zeros((len(self.sizes), 4), np.float64)
         L.call("kb_batch_moments", self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
+
+    def add_replica(self, replica: Replica, origin_step: int) -> int:
+        """Append a replica to the running batch; its step 0 is the batch's
+        step ``origin_step``.  Returns its index."""
+        d = L.ReplicaDesc()
+        _fill_desc(d, replica)
+        ids = np.ascontiguousarray(replica.state[0], np.uint32)
+        xy = np.ascontiguousarray(replica.state[1], np.float32)
+        dxy = np.ascontiguousarray(replica.state[2], np.float32)
+        idx = C.c_uint32()
+        L.call("kb_batch_add_replica", self._h, C.byref(d), L.uptr(ids), L.fptr(xy), L.fptr(dxy),
+               C.c_uint64(origin_step), C.byref(idx))
+        self.sizes.append(replica.n)
+        self.nrep += 1
+        return int(idx.value)
+
+    def remove_replica(self, r: int) -> None:
+        """Drop replica r; later replicas move down one index."""
+        L.call("kb_batch_remove_replica", self._h, C.c_uint32(r))
+        del self.sizes[r]
+        self.nrep -= 1
 
     def get_replica(self, r: int):
         n = C.c_size_t()

@@ -997,6 +997,37 @@ kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uin
     return KB_OK;
 }
 
+// Bag arrays for at least `need` bags (contents are not kept: the caller
+// rebuilds the offsets with a general sort).
+kb_status grow_cells(kb_field* f, uint64_t need) {
+    if (need <= f->cells_cap) return KB_OK;
+    if (need > 0xF0000000ull) return fail(KB_ERR_ARG, "bag matrix too large");
+    const uint32_t nc = (uint32_t)std::min<uint64_t>(0xF0000000ull, std::max<uint64_t>(need, 2ull * f->cells_cap));
+    const uint32_t nt = scan_state_words(nc);
+    DevBuf<uint32_t> s0, s1, hist, cursor;
+    DevBuf<unsigned long long> ts;
+    cudaError_t e;
+    if ((e = s0.alloc((size_t)nc + 1)) || (e = s1.alloc((size_t)nc + 1)) || (e = hist.alloc(nc)) ||
+        (e = cursor.alloc(nc)) || (e = ts.alloc(nt)))
+        return cuda_fail(e, "growing the bag arrays");
+    KB_CUDA(cudaMemsetAsync(s0.p, 0, sizeof(uint32_t) * ((size_t)nc + 1), f->stream));
+    KB_CUDA(cudaMemsetAsync(s1.p, 0, sizeof(uint32_t) * ((size_t)nc + 1), f->stream));
+    KB_CUDA(cudaMemsetAsync(hist.p, 0, sizeof(uint32_t) * nc, f->stream));
+    KB_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(uint32_t) * nc, f->stream));
+    KB_CUDA(cudaMemsetAsync(ts.p, 0, sizeof(unsigned long long) * nt, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    f->start[0].swap(s0);
+    f->start[1].swap(s1);
+    f->hist.swap(hist);
+    f->cursor.swap(cursor);
+    f->tstate.swap(ts);
+    f->cells_cap = nc;
+    f->hist_counted = false;
+    f->fused.ready = false;
+    f->drop_graphs();
+    return KB_OK;
+}
+
 // Replace the replica table of a capacity-sized field (the contents are
 // rebuilt by the caller).
 kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
@@ -2007,6 +2038,138 @@ kb_status kb_field_moments(kb_field* f, double out4[4]) {
     if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
     if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: use kb_batch_moments");
     return field_moments(f, out4);
+}
+
+// Rebuild a committed batch with a new replica table: slot i of `reps`
+// takes the canonical records of old replica src[i] (src[i] >= 0) or, for
+// src[i] < 0, the n host objects given (a new replica's initial state).
+static kb_status batch_repack(kb_batch* b, std::vector<Rep> reps, const std::vector<int64_t>& src,
+                              size_t n_new, const uint32_t* ids, const float* xy, const float* dxy) {
+    kb_field* f = b->f;
+    DeviceGuard g(f->device);
+    kb_status st = materialize(f);
+    if (st) return st;
+    const std::vector<Rep> old = f->reps;
+    std::vector<PackEntry> plan;
+    uint64_t cells = 0, boids = 0, host_off = 0;
+    bool have_host = false;
+    for (size_t i = 0; i < reps.size(); ++i) {
+        Rep& R = reps[i];
+        R.cell_off = (uint32_t)cells;
+        R.boid_off = (uint32_t)boids;
+        if (src[i] >= 0) {
+            PackEntry e{};
+            e.dst_off = (uint32_t)boids;
+            e.n = R.nboids;
+            e.rep = (uint32_t)i;
+            e.src_off = old[(size_t)src[i]].boid_off;
+            e.kind = 0u;
+            if (e.n) plan.push_back(e);
+        } else {
+            have_host = true;
+            host_off = boids;
+        }
+        cells += R.ncells;
+        boids += R.nboids;
+    }
+    if (cells > 0xF0000000ull || boids > 0xF0000000ull) return fail(KB_ERR_ARG, "batch too large");
+    if ((st = grow(f, (uint32_t)std::max<uint64_t>(boids, 1)))) return st;
+    if ((st = grow_cells(f, cells))) return st;
+    DevBuf<PackEntry> dplan;
+    if (!plan.empty()) {
+        cudaError_t e = dplan.alloc(plan.size());
+        if (e) return cuda_fail(e, "repack plan");
+        KB_CUDA(cudaMemcpyAsync(dplan.p, plan.data(), sizeof(PackEntry) * plan.size(), cudaMemcpyHostToDevice, f->stream));
+    }
+    // the read buffer (rst) is the copy source; the write list the target
+    if ((st = field_set_reps(f, reps))) return st;
+    if (!plan.empty())
+        KB_CUDA(launch_repack(dplan.p, (int32_t)plan.size(), (uint32_t)boids, f->d_rep.p, f->rst.p,
+                              f->rid.p, f->wst.p, f->wid.p, f->wkey.p, f->wdead.p, f->err.p, f->stream));
+    if (have_host && n_new) {
+        const Rep& R = f->reps[std::find(src.begin(), src.end(), (int64_t)-1) - src.begin()];
+        const uint32_t m = (uint32_t)n_new, at = (uint32_t)host_off;
+        float2* sxy = reinterpret_cast<float2*>(f->tst.p);
+        KB_CUDA(cudaMemcpyAsync(sxy, xy, sizeof(float2) * m, cudaMemcpyHostToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(sxy + m, dxy, sizeof(float2) * m, cudaMemcpyHostToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(f->wid.p + at, ids, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, f->stream));
+        KB_CUDA(cudaMemsetAsync(f->small.p, 0xFF, sizeof(uint32_t), f->stream));
+        KB_CUDA(launch_pack_locations(R, sxy, sxy + m, m, f->wst.p + at, f->wkey.p + at, f->wdead.p + at,
+                                      f->small.p, f->stream));
+        uint32_t bad = 0;
+        if ((st = read_u32(f, f->small.p, &bad))) return st;
+        if (bad != 0xFFFFFFFFu)
+            return fail(KB_ERR_RANGE, "new replica: object " + std::to_string(bad) +
+                                          " outside its bag matrix on the device");
+    }
+    f->wn = (uint32_t)boids;
+    f->w_from_compute = false;
+    f->w_has_dead = false;
+    f->virt = false;
+    f->p_st.clear(); f->p_id.clear(); f->p_key.clear();
+    if ((st = general_rebuild(f, false))) return st;
+    f->rn = (uint32_t)boids;
+    f->wn = 0;
+    f->layout_is_positions = true;
+    if ((st = check_unique_ids(f))) return st;
+    b->have.assign(reps.size(), 1);
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second.exec);
+    b->graphs.clear();
+    return check_flags(f);
+}
+
+kb_status kb_batch_remove_replica(kb_batch* b, uint32_t r) {
+    if (!b) return fail(KB_ERR_ARG, "null argument");
+    kb_field* f = b->f;
+    if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
+    if (f->reps.size() < 2) return fail(KB_ERR_STATE, "a batch keeps at least one replica");
+    if (f->wn || !f->p_id.empty() || std::find(b->have.begin(), b->have.end(), 0) != b->have.end())
+        return fail(KB_ERR_STATE, "batch not committed");
+    std::vector<Rep> reps;
+    std::vector<int64_t> src;
+    for (uint32_t i = 0; i < f->reps.size(); ++i)
+        if (i != r) {
+            reps.push_back(f->reps[i]);
+            src.push_back(i);
+        }
+    return batch_repack(b, reps, src, 0, nullptr, nullptr, nullptr);
+}
+
+kb_status kb_batch_add_replica(kb_batch* b, const kb_replica_desc* d, const uint32_t* ids,
+                               const float* xy, const float* dxy, uint64_t origin_step,
+                               uint32_t* index) {
+    if (!b || !d || !index || (d->nboids && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
+    kb_field* f = b->f;
+    if (f->wn || !f->p_id.empty() || std::find(b->have.begin(), b->have.end(), 0) != b->have.end())
+        return fail(KB_ERR_STATE, "batch not committed");
+    Rep R;
+    std::string why;
+    if (!make_rep_geometry(d->width, d->height, d->discretization, d->toroidal, &R, &why, d->cell_wrap))
+        return fail(KB_ERR_ARG, why);
+    if (!params_ok(&d->params, &why)) return fail(KB_ERR_ARG, why);
+    if (d->params.query_mode != b->common.query_mode || d->params.arith != b->common.arith)
+        return fail(KB_ERR_ARG, "all replicas of a batch share query_mode and arith");
+    set_rep_params(&R, &d->params);
+    R.nboids = d->nboids;
+    // checked here so that a refused replica leaves the batch as it was
+    for (uint32_t i = 0; i < d->nboids; ++i) {
+        if (!(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) && std::isfinite(dxy[2 * i]) &&
+              std::isfinite(dxy[2 * i + 1])))
+            return fail(KB_ERR_ARG, "object " + std::to_string(i) + ": non-finite position or heading");
+        if (host_bag_index(R, xy[2 * i], xy[2 * i + 1]) < 0)
+            return fail(KB_ERR_RANGE, "object " + std::to_string(i) + ": location outside the replica's bag matrix");
+    }
+    R.origin_lo = (uint32_t)origin_step;
+    R.origin_hi = (uint32_t)(origin_step >> 32);
+    std::vector<Rep> reps = f->reps;
+    std::vector<int64_t> src;
+    for (uint32_t i = 0; i < reps.size(); ++i) src.push_back(i);
+    reps.push_back(R);
+    src.push_back(-1);
+    kb_status st = batch_repack(b, reps, src, d->nboids, ids, xy, dxy);
+    if (st) return st;
+    *index = (uint32_t)(reps.size() - 1);
+    return KB_OK;
 }
 
 kb_status kb_batch_synchronize(kb_batch* b) {

@@ -113,3 +113,64 @@ def test_batch_true_torus_replica_matches_oracle(gpu, mode):
         o.flock_run(oracle.params_from(rep.params), 0, 15)
         oids, ost, _ = o.iter(1)
         assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_batch_add_and_remove_replicas_match_oracle(gpu, mode):
+    # replicas join and leave a running batch: each one still equals the
+    # oracle run of it alone over the steps it took part in (strict bits)
+    reps = small_sweep(kg.KB_ARITH_STRICT)
+    b = kg.Batch(reps[:4])
+    b.set_step_options(mode)
+    live = [(reps[i], 0) for i in range(4)]  # (replica, batch step of its step 0)
+    b.step(0, 10, 1, 5)
+    b.remove_replica(1)
+    del live[1]
+    assert b.add_replica(reps[5], 10) == 3    # grows the bag arrays
+    live.append((reps[5], 10))
+    b.step(10, 10, 1, 5)
+    assert b.add_replica(reps[6], 20) == 4
+    live.append((reps[6], 20))
+    b.remove_replica(0)
+    del live[0]
+    b.step(20, 5, 1, 5)
+    assert b.nrep == len(live) == 4
+    m = b.moments()
+    for i, (rep, origin) in enumerate(live):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 25 - origin)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+        assert m[i, 0] == rep.n
+
+
+def test_batch_add_replica_errors_leave_the_batch_unchanged(gpu):
+    reps = small_sweep(kg.KB_ARITH_STRICT)[:3]
+    b = kg.Batch(reps[:2])
+    b.step(0, 4)
+    bad = kg.Replica(reps[2].width, reps[2].height, reps[2].discretization, reps[2].params,
+                     (reps[2].state[0], reps[2].state[1].copy(), reps[2].state[2]))
+    bad.state[1][7] = (reps[2].width * 3, 1.0)        # outside the bag matrix
+    with pytest.raises(L.KbError) as err:
+        b.add_replica(bad, 4)
+    assert err.value.status == L.KB_ERR_RANGE and "object 7" in str(err.value)
+    bad.state[1][7] = (np.nan, 1.0)
+    with pytest.raises(L.KbError) as err:
+        b.add_replica(bad, 4)
+    assert err.value.status == L.KB_ERR_ARG
+    fast = kg.Replica(reps[2].width, reps[2].height, reps[2].discretization,
+                      kg.FlockParams(arith=kg.KB_ARITH_FAST), reps[2].state)
+    with pytest.raises(L.KbError):
+        b.add_replica(fast, 4)
+    with pytest.raises(L.KbError) as err:
+        b.remove_replica(2)
+    assert err.value.status == L.KB_ERR_ARG
+    assert b.nrep == 2
+    b.step(4, 6)
+    for i, rep in enumerate(reps[:2]):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 10)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+    b.remove_replica(0)
+    with pytest.raises(L.KbError) as err:
+        b.remove_replica(0)                          # the last replica stays
+    assert err.value.status == L.KB_ERR_STATE
