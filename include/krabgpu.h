@@ -113,6 +113,14 @@ kb_status kb_field_set_locations(kb_field* f, size_t n, const uint32_t* ids, con
                                  const float* dxy);
 /* remove_object_location(object, loc) -- field_2d.rs:885-898 (write buffer). */
 kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float loc[2]);
+/* Bulk removal by id (no single reference counterpart): every object of the
+ * write buffer whose id is in ids[0..n) is removed, wherever its bag; for
+ * each such object that is remove_object_location at its write location
+ * (field_2d.rs:885-898).  An agent that leaves the schedule after
+ * kb_flock_compute wrote it (Schedule::dequeue, schedule.rs:329-343, or
+ * Agent::is_stopped, schedule.rs:401) is dropped this way: the reference
+ * writes nothing for it.  *removed (may be NULL) = objects removed. */
+kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t* removed);
 /* Field::lazy_update -- field_2d.rs:905-921: the write buffer becomes the
  * read buffer and a new empty write buffer starts. */
 kb_status kb_field_lazy_update(kb_field* f);
@@ -161,6 +169,17 @@ kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, u
  * buffer, writes every bird's next state into the (empty) write buffer.
  * `step` keys the jitter stream. */
 kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step);
+/* Bird::step (bird.rs:39-154) for n agents that the caller holds rather
+ * than the read buffer: agents that join the schedule at this step
+ * (schedule_repeating / schedule_once at a later time, schedule.rs:283-303)
+ * or skipped earlier steps.  Agent j = {ids[j], states[4j..4j+3] = x, y,
+ * last_d.x, last_d.y} reads its neighbours from the read buffer, skips
+ * candidates with its own id (bird.rs:50) and is written into the write
+ * buffer after what is already there, in the given order (the order in
+ * which the schedule pops them).  May follow kb_flock_compute for the same
+ * step.  The next lazy_update takes the general rebuild. */
+kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_t step, size_t n,
+                                  const uint32_t* ids, const float* states);
 /* nsteps full steps: compute + lazy_update each (schedule.rs:395-412), with
  * step numbers first_step ... first_step+nsteps-1.  The read buffer must
  * hold the flock and the write buffer must be empty (call lazy_update after

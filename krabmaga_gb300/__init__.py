@@ -12,11 +12,12 @@ from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
 from .explore import (ExploreMode, FlockerConfig, build_configurations, evolutionary_search,
                       explore, random_search, write_csv)
-from .model import (FlockParams, Flocker, Schedule, State, gen_clustered, gen_uniform, simulate,
-                    simulate_old)
+from .model import (Agent, AgentImpl, FlockParams, Flocker, Schedule, State, gen_clustered,
+                    gen_uniform, simulate, simulate_old)
 
 __all__ = [
     "Bird", "Field2D", "Real2D", "FlockParams", "Flocker", "Schedule", "State", "simulate",
+    "Agent", "AgentImpl",
     "simulate_old", "gen_uniform", "gen_clustered", "KbError", "lib", "LIB_PATH",
     "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
     "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS",

@@ -145,6 +145,7 @@ _SIGS = {
     "kb_field_set_object_location": (C.c_int32, [_P, C.c_uint32, _F, _F, _F]),
     "kb_field_set_locations": (C.c_int32, [_P, C.c_size_t, _U32, _F, _F]),
     "kb_field_remove_object_location": (C.c_int32, [_P, C.c_uint32, _F]),
+    "kb_field_remove_ids": (C.c_int32, [_P, C.c_size_t, _U32, _SZ]),
     "kb_field_lazy_update": (C.c_int32, [_P]),
     "kb_field_num_agents": (C.c_int32, [_P, _SZ]),
     "kb_field_num_objects": (C.c_int32, [_P, _SZ]),
@@ -159,6 +160,8 @@ _SIGS = {
     "kb_field_get_random_empty_bag": (C.c_int32, [_P, C.c_uint64, _F, C.POINTER(C.c_int32)]),
     "kb_field_iter_objects": (C.c_int32, [_P, C.c_int32, _F, _U32, _F, C.c_size_t, _SZ]),
     "kb_flock_compute": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64]),
+    "kb_flock_compute_agents": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_size_t,
+                                            _U32, _F]),
     "kb_field_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "kb_field_step_stats": (C.c_int32, [_P, _U32]),
     "kb_field_set_kernel_timing": (C.c_int32, [_P, C.c_int32]),

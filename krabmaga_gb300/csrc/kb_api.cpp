@@ -1581,6 +1581,83 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
     return KB_OK;
 }
 
+kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_t step, size_t n,
+                                  const uint32_t* ids, const float* states) {
+    if (!f || !p || (n && (!ids || !states))) return fail(KB_ERR_ARG, "null argument");
+    if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: agents join a batch with kb_batch_add_replica");
+    std::string why;
+    if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
+    for (size_t j = 0; j < n; ++j)
+        for (int c = 0; c < 4; ++c)
+            if (!std::isfinite(states[4 * j + c]))
+                return fail(KB_ERR_ARG, "agent " + std::to_string(j) + ": non-finite position or heading");
+    if (n == 0) return KB_OK;
+    DeviceGuard g(f->device);
+    // objects set from the host earlier come first in the write buffer
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    if ((st = materialize(f))) return st;
+    if ((uint64_t)f->wn + n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "object count exceeds 2^32-16");
+    const uint32_t m = (uint32_t)n;
+    if ((st = grow(f, std::max(f->rn, f->wn + m)))) return st;
+    set_rep_params(&f->rep, p);
+    if ((st = upload_rep(f))) return st;
+    KB_CUDA(launch_set_u64(f->dstep.p, step, f->stream));
+    f->dstep_host = step;
+    // the agents are staged in the sort temporaries (free until lazy_update)
+    KB_CUDA(cudaMemcpyAsync(f->tst.p, states, sizeof(float4) * m, cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemcpyAsync(f->tid.p, ids, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, f->stream));
+    ForceArgs a{};
+    a.reps = f->d_rep.p;
+    a.nrep = 1;
+    a.rep0 = f->reps[0];
+    a.st = f->rst.p;
+    a.ids = f->rid.p;
+    a.start = f->start[f->cur].p;
+    a.n = f->rn;
+    a.step = f->dstep.p;
+    a.out_st = f->wst.p + f->wn;
+    a.out_ids = f->wid.p + f->wn;
+    a.out_key = f->wkey.p + f->wn;
+    a.hist = f->hist.p;
+    a.err = f->err.p;
+    KB_CUDA(launch_flock_agents(a, f->tst.p, f->tid.p, m, p->arith == KB_ARITH_STRICT, p->query_mode,
+                                f->stream));
+    f->hist_counted = true;
+    f->wn += m;
+    f->w_from_compute = false;  // the write list is no longer one pass over the read buffer
+    if (!f->density_check) f->nagents += m;
+    return KB_OK;
+}
+
+kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t* removed) {
+    if (!f || (n && !ids)) return fail(KB_ERR_ARG, "null argument");
+    if (removed) *removed = 0;
+    if (n == 0) return KB_OK;
+    if (n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many ids");
+    DeviceGuard g(f->device);
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    if (f->wn == 0) return KB_OK;
+    std::vector<uint32_t> sorted(ids, ids + n);
+    std::sort(sorted.begin(), sorted.end());
+    sorted.erase(std::unique(sorted.begin(), sorted.end()), sorted.end());
+    DevBuf<uint32_t> d;
+    cudaError_t e = d.alloc(sorted.size());
+    if (e) return cuda_fail(e, "id list");
+    KB_CUDA(cudaMemcpyAsync(d.p, sorted.data(), sizeof(uint32_t) * sorted.size(), cudaMemcpyHostToDevice, f->stream));
+    KB_CUDA(cudaMemsetAsync(f->small.p, 0, sizeof(uint32_t), f->stream));
+    KB_CUDA(launch_remove_ids(f->wid.p, f->wdead.p, f->wn, d.p, (uint32_t)sorted.size(), f->small.p, f->stream));
+    uint32_t cnt = 0;
+    if ((st = read_u32(f, f->small.p, &cnt))) return st;  // synchronises: d may be freed
+    if (cnt) {
+        f->w_has_dead = true;
+        if (!f->density_check) f->nagents -= cnt;
+    }
+    if (removed) *removed = cnt;
+    return KB_OK;
+}
+
 // Enqueue nsteps steps (force + rebuild) directly on the stream.
 // Four timing events for one separate-kernel step, or -1 (timing off, the
 // general rebuild, or the stream is being captured into a graph).

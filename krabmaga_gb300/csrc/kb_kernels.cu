@@ -177,13 +177,13 @@ __device__ __forceinline__ void force_finish(const ForceArgs& a, const Rep& R, u
                                              float4 me, uint32_t my_id, unsigned long long step,
                                              const Acc<STRICT>& acc);
 
+// The candidate sums of one agent at `me` against the read buffer (the
+// query of bird.rs:41 and the loop of bird.rs:48-82).  my_slot: the agent's
+// own read-buffer slot when self is recognised by slot, else ~0u.
 template <bool STRICT, int QMODE>
-__device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uint32_t i) {
-    const unsigned long long step = *a.step;
-    const float4 me = __ldg(a.st + i);
-    const uint32_t my_id = __ldg(a.ids + i);
-
-    Acc<STRICT> acc;
+__device__ __forceinline__ void gather_candidates(const ForceArgs& a, const Rep& R, float4 me,
+                                                  uint32_t my_id, uint32_t my_slot,
+                                                  Acc<STRICT>& acc) {
     int mi, Mi, mj, Mj;
     if (cell_range(R, me.x, me.y, R.dd, &mi, &Mi, &mj, &Mj)) {
         const bool clamped = R.toroidal && !R.cell_wrap;  // runs never cross the seam
@@ -194,7 +194,7 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
                 // a one-bag ring (the common case) as one flat list; the wider
                 // two-bag ring out of line
                 if (Mi - mi < 3)
-                    columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc, a.self_by_slot ? i : 0xFFFFFFFFu);
+                    columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc, my_slot);
                 else columns_runs_5(a, R, mi, Mi, mj, Mj, me, my_id, acc);
             }
         } else {
@@ -230,7 +230,15 @@ __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uin
             }
         }
     }
+}
 
+template <bool STRICT, int QMODE>
+__device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uint32_t i) {
+    const unsigned long long step = *a.step;
+    const float4 me = __ldg(a.st + i);
+    const uint32_t my_id = __ldg(a.ids + i);
+    Acc<STRICT> acc;
+    gather_candidates<STRICT, QMODE>(a, R, me, my_id, a.self_by_slot ? i : 0xFFFFFFFFu, acc);
     force_finish<STRICT>(a, R, i, me, my_id, step, acc);
 }
 
@@ -302,6 +310,42 @@ __global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI 
     }
     if (i >= a.n) return;
     force_body<STRICT, QMODE>(a, a.rep0, i);
+}
+
+// Bird::step for agents given by the caller rather than read from the read
+// buffer (agents that join the schedule, schedule.rs:283-303): agent j reads
+// its neighbours from the read buffer, skips candidates with its own id
+// (bird.rs:50) and writes its next state to slot j of the outputs.
+template <bool STRICT, int QMODE>
+__global__ void __launch_bounds__(KB_FORCE_THREADS)
+    k_flock_agents(ForceArgs a, const float4* __restrict__ in_st, const uint32_t* __restrict__ in_ids,
+                   uint32_t nin) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nin) return;
+    const unsigned long long step = *a.step;
+    const float4 me = in_st[j];
+    const uint32_t my_id = in_ids[j];
+    Acc<STRICT> acc;
+    gather_candidates<STRICT, QMODE>(a, a.rep0, me, my_id, 0xFFFFFFFFu, acc);
+    force_finish<STRICT>(a, a.rep0, j, me, my_id, step, acc);
+}
+
+// Mark every live write-list entry whose id is in sorted[0..m) removed.
+__global__ void k_remove_ids(const uint32_t* __restrict__ ids, uint8_t* dead, uint32_t n,
+                             const uint32_t* __restrict__ sorted, uint32_t m, uint32_t* removed) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || dead[i]) return;
+    const uint32_t id = ids[i];
+    uint32_t lo = 0, hi = m;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (sorted[mid] < id) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo < m && sorted[lo] == id) {
+        dead[i] = 1;
+        atomicAdd(removed, 1u);
+    }
 }
 
 // ---------------------------------------------------------- scan
@@ -1256,6 +1300,28 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
         else { if (multi) KB_FORCE(false, 1, true); else KB_FORCE(false, 1, false); }
     }
 #undef KB_FORCE
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flock_agents(const ForceArgs& a, const float4* in_st, const uint32_t* in_ids,
+                               uint32_t nin, bool strict, int qmode, cudaStream_t s) {
+    if (nin == 0) return cudaSuccess;
+    if (a.nrep != 1) return cudaErrorInvalidValue;
+    const unsigned g = grid_for(nin, KB_FORCE_THREADS);
+    if (strict) {
+        if (qmode == 0) k_flock_agents<true, 0><<<g, KB_FORCE_THREADS, 0, s>>>(a, in_st, in_ids, nin);
+        else k_flock_agents<true, 1><<<g, KB_FORCE_THREADS, 0, s>>>(a, in_st, in_ids, nin);
+    } else {
+        if (qmode == 0) k_flock_agents<false, 0><<<g, KB_FORCE_THREADS, 0, s>>>(a, in_st, in_ids, nin);
+        else k_flock_agents<false, 1><<<g, KB_FORCE_THREADS, 0, s>>>(a, in_st, in_ids, nin);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_remove_ids(const uint32_t* ids, uint8_t* dead, uint32_t n, const uint32_t* sorted,
+                              uint32_t m, uint32_t* removed, cudaStream_t s) {
+    if (n == 0 || m == 0) return cudaSuccess;
+    k_remove_ids<<<grid_for(n, 256), 256, 0, s>>>(ids, dead, n, sorted, m, removed);
     return cudaGetLastError();
 }
 

@@ -69,6 +69,11 @@ struct ForceArgs {
 };
 constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
+// Bird::step of nin caller-given agents (in_st {x, y, dx, dy}, in_ids) against
+// the read buffer of a single replica; agent j's next state, id and bag key
+// go to slot j of a.out_st / a.out_ids / a.out_key, its arrival into a.hist.
+cudaError_t launch_flock_agents(const ForceArgs& a, const float4* in_st, const uint32_t* in_ids,
+                               uint32_t nin, bool strict, int qmode, cudaStream_t s);
 
 // Stencil-gather rebin: builds the canonical read buffer of the next step
 // from the write list (in the previous canonical order) and the scanned
@@ -161,6 +166,10 @@ cudaError_t launch_filter_key(const uint32_t* key, const uint8_t* dead, const fl
 // number marked to *removed.
 cudaError_t launch_remove(const uint32_t* key, uint8_t* dead, const uint32_t* ids, uint32_t n,
                           uint32_t target, uint32_t id, uint32_t* removed, cudaStream_t s);
+// Mark live write-list entries whose id is in sorted[0..m) (ascending) dead;
+// adds the number marked to *removed.
+cudaError_t launch_remove_ids(const uint32_t* ids, uint8_t* dead, uint32_t n, const uint32_t* sorted,
+                              uint32_t m, uint32_t* removed, cudaStream_t s);
 // Empty bags of the read buffer in index order, as (i*d, j*d).
 cudaError_t launch_empty_bags(const Rep& rep, const uint32_t* start, float2* out, uint64_t cap,
                               uint32_t* out_count, cudaStream_t s);

@@ -115,6 +115,34 @@ class Field2D:
         L.call("kb_field_remove_object_location", self._h, C.c_uint32(obj.id),
                L.fptr(loc.as_f32()))
 
+    def remove_ids(self, ids) -> int:
+        """Remove every write-buffer object with one of these ids (each one as
+        remove_object_location at its write location); returns the count."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32).reshape(-1)
+        n = C.c_size_t()
+        L.call("kb_field_remove_ids", self._h, C.c_size_t(len(ids)), L.uptr(ids), C.byref(n))
+        return n.value
+
+    def flock_compute(self, params, step: int) -> None:
+        """Bird::step of every agent of the read buffer into the write buffer
+        (the agent pass of one Schedule::step)."""
+        L.call("kb_flock_compute", self._h, C.byref(params.to_c()), C.c_uint64(step))
+
+    def flock_step(self, params, first_step: int, nsteps: int) -> None:
+        """nsteps whole steps (agent pass + lazy_update each), numbered from
+        first_step; runs of steps replay CUDA graphs."""
+        L.call("kb_flock_step", self._h, C.byref(params.to_c()), C.c_uint64(first_step),
+               C.c_uint32(nsteps))
+
+    def flock_compute_agents(self, params, step: int, ids, states) -> None:
+        """Bird::step of caller-held agents (states: n x {x, y, dx, dy})
+        against the read buffer, appended to the write buffer in order."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32).reshape(-1)
+        st = np.ascontiguousarray(states, dtype=np.float32).reshape(-1, 4)
+        assert len(ids) == len(st)
+        L.call("kb_flock_compute_agents", self._h, C.byref(params.to_c()), C.c_uint64(step),
+               C.c_size_t(len(ids)), L.uptr(ids), L.fptr(st))
+
     def lazy_update(self) -> None:
         """Field::lazy_update -- field_2d.rs:905-921"""
         L.call("kb_field_lazy_update", self._h)

@@ -59,6 +59,10 @@ _SIGS = {
                                                  C.c_size_t, _U32, _F, _F, C.c_uint32, C.c_uint32,
                                                  C.POINTER(_P)]),
     "orc_flock_compute": (C.c_int, [_P, C.POINTER(Params), C.c_uint64]),
+    "orc_bird_step": (None, [_P, C.POINTER(Params), C.c_uint64, C.c_uint32, _F, _F]),
+    "orc_flock_compute_agents": (C.c_int, [_P, C.POINTER(Params), C.c_uint64, C.c_size_t, _U32,
+                                           _F]),
+    "orc_field_remove_ids": (C.c_size_t, [_P, C.c_size_t, _U32]),
     "orc_flock_step_fp64": (C.c_size_t, [_P, C.POINTER(Params), C.c_uint64, _U32, _D,
                                          C.c_size_t]),
     "orc_simulate_timed": (C.c_double, [C.c_float, C.c_float, C.c_float, C.POINTER(Params),
@@ -191,6 +195,24 @@ class OracleField:
         """The agent pass only (every bird into the write buffer), no lazy_update."""
         if lib.orc_flock_compute(self.h, C.byref(p), step) != 0:
             raise IndexError("reference panics during the step")
+
+    def bird_step(self, p: Params, step, id, state4):
+        """Bird::step of one caller-held agent against the read buffer; its next
+        {x, y, dx, dy} (nothing written)."""
+        i4 = np.ascontiguousarray(state4, np.float32).reshape(4)
+        o4 = np.zeros(4, np.float32)
+        lib.orc_bird_step(self.h, C.byref(p), step, id, _f(i4), _f(o4))
+        return o4
+
+    def flock_compute_agents(self, p: Params, step, ids, states):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        st = np.ascontiguousarray(states, np.float32).reshape(-1, 4)
+        if lib.orc_flock_compute_agents(self.h, C.byref(p), step, len(ids), _u(ids), _f(st)) != 0:
+            raise IndexError("reference panics during the step")
+
+    def remove_ids(self, ids):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        return int(lib.orc_field_remove_ids(self.h, len(ids), _u(ids)))
 
     def flock_step_fp64(self, p: Params, step):
         n = self.iter(1)[0].shape[0]

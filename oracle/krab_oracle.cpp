@@ -661,6 +661,49 @@ int orc_flock_compute(void* fp, const orc_params* pp, uint64_t step) {
     return flock_compute(*(Field2D*)fp, to_params(pp), step) ? 0 : -1;
 }
 
+// Bird::step of one agent held by the caller (bird.rs:39-154) against the
+// read buffer; out4 = its next {x, y, dx, dy}.  Nothing is written.
+void orc_bird_step(void* fp, const orc_params* pp, uint64_t step, uint32_t id, const float* in4,
+                   float* out4) {
+    std::vector<Bird> vec;
+    const Bird b{id, in4[0], in4[1], in4[2], in4[3]};
+    const Bird nb = bird_step(*(Field2D*)fp, to_params(pp), b, step, vec);
+    out4[0] = nb.x; out4[1] = nb.y; out4[2] = nb.dx; out4[3] = nb.dy;
+}
+
+// Agents that the caller holds (ids, states n x 4), stepped in order
+// against the read buffer and written into the write buffer.
+int orc_flock_compute_agents(void* fp, const orc_params* pp, uint64_t step, size_t n,
+                             const uint32_t* ids, const float* states) {
+    Field2D* f = (Field2D*)fp;
+    const FlockParams p = to_params(pp);
+    std::vector<Bird> vec;
+    for (size_t j = 0; j < n; ++j) {
+        const Bird b{ids[j], states[4 * j], states[4 * j + 1], states[4 * j + 2], states[4 * j + 3]};
+        const Bird nb = bird_step(*f, p, b, step, vec);
+        if (!f->set_object_location(nb, nb.x, nb.y)) return -1;
+    }
+    return 0;
+}
+
+// Every write-buffer object whose id is in ids[0..n) removed (each one as
+// remove_object_location at its write location); returns the count.
+size_t orc_field_remove_ids(void* fp, size_t n, const uint32_t* ids) {
+    Field2D* f = (Field2D*)fp;
+    std::vector<uint32_t> s(ids, ids + n);
+    std::sort(s.begin(), s.end());
+    size_t removed = 0;
+    for (auto& bag : f->bags[f->write]) {
+        const size_t before = bag.size();
+        bag.erase(std::remove_if(bag.begin(), bag.end(),
+                                 [&](const Bird& o) { return std::binary_search(s.begin(), s.end(), o.id); }),
+                  bag.end());
+        removed += before - bag.size();
+    }
+    if (!f->density_check) f->nagents -= removed;
+    return removed;
+}
+
 int orc_flock_run(void* fp, const orc_params* pp, uint64_t first_step, uint32_t nsteps) {
     Field2D* f = (Field2D*)fp;
     FlockParams p = to_params(pp);

@@ -87,18 +87,15 @@ def test_1k_flock_neighbour_sets_bit_exact_every_step(gpu, kind):
 def test_compute_plus_lazy_update_equals_fused_steps(gpu):
     ids0, xy0, dxy0 = kg.gen_uniform(3000, 300.0, 300.0, 3, 1.0)
     p = kg.FlockParams(seed=9)
-    a = gpu_field(300.0, FLOCK_D, ids0, xy0, dxy0)
     b = gpu_field(300.0, FLOCK_D, ids0, xy0, dxy0)
-    state = kg.Flocker((300.0, 300.0), 3000, FLOCK_D, params=p)
-    state.field1.close()
-    state.field1 = a  # already initialised and past its step-0 update
+    state = kg.Flocker((300.0, 300.0), 3000, FLOCK_D, params=p, init_state=(ids0, xy0, dxy0))
     sched = kg.Schedule()
-    for t in range(30):  # the reference's per-step path: agents, then update
-        state.before_step(sched)
-        sched.step += 1
-        state.update(sched.step)
+    state.init(sched)
+    for t in range(30):  # the reference's per-step path: update at step 0, agents, update
+        sched.step_state(state)
+    assert sched.step == 30 and sched.time == 29.0
     step(b, p, 0, 30)  # graph-replayed steps
-    ia, sa = a.get_state()
+    ia, sa = state.field1.get_state()
     ib, sb = b.get_state()
     assert np.array_equal(ia, ib) and same_bits(sa, sb)
 
