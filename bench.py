@@ -422,6 +422,7 @@ def run_ours(args, wl):
         f.synchronize()
         kernel_ms, kernel_steps = f.kernel_times()
         f.set_kernel_timing(False)
+    dense = f.dense_active()  # the walk the timed steps used (chosen from the occupancies)
     total_s = allmax(ws, sum(step_ms) / 1e3)
     value = ws * n * K / total_s
     stats = f.step_stats()
@@ -517,6 +518,7 @@ def run_ours(args, wl):
                    "l2": "flushed (512 MiB write) before every timed step",
                    "kernel_timing": "per-launch CUDA events over a second pass of the same "
                                     "K steps (L2 flushed before each)",
+                   "candidate_walk": "per-run (dense)" if dense else "flat",
                    "warm_l2_value": warm_value},
         "roofline": {"bound": "hbm", "kernel": kname,
                      "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",

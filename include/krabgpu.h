@@ -46,6 +46,11 @@ typedef int32_t kb_status;
 #define KB_QUERY_RELAX 0 /* get_neighbors_within_relax_distance, field_2d.rs:472-516 */
 #define KB_QUERY_EXACT 1 /* get_neighbors_within_distance, field_2d.rs:386-440 (in-tree Bird) */
 
+/* Candidate-list walk of the force pass (kb_field_set_dense_mode). */
+#define KB_DENSE_AUTO 0 /* chosen from the bag occupancies (default) */
+#define KB_DENSE_OFF 1  /* one flat list over the three column runs */
+#define KB_DENSE_ON 2   /* each column run with a pointer; 8-bag rebin segments */
+
 /* Arithmetic of the flock step. */
 #define KB_ARITH_STRICT 0 /* IEEE f32 with the reference's rounding points: bit-exact */
 #define KB_ARITH_FAST 1   /* approximate division/sqrt; within 1e-5 of domain vs FP64 */
@@ -195,6 +200,16 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
  * tile_tx x tile_ty bags per tile (0 = automatic).  All modes give the same
  * bits, in both arithmetic modes. */
 kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty);
+/* Candidate-list walk of the separate-kernel step (no reference counterpart;
+ * tuning only): KB_DENSE_AUTO (default) switches to KB_DENSE_ON when the read
+ * buffer's estimated mean candidate count per boid (9 * sum of squared bag
+ * occupancies / N) is at least 48, measured after each general rebuild and
+ * every 64 steps without waiting.  ON walks each column run with a pointer
+ * and rebins 8-bag segments (faster for dense flocks); OFF keeps one flat
+ * list and 32-bag segments (faster for uniform ones).  Same bits either way.
+ * *active (kb_field_dense_active) = the walk the next step uses. */
+kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode);
+kb_status kb_field_dense_active(kb_field* f, int32_t* active);
 /* Per-kernel timing (no reference counterpart; measurement only).  While
  * enabled, every separate-kernel step that is not replayed from a graph (a
  * kb_flock_step call of fewer than 4 steps) records CUDA events around its

@@ -6,7 +6,7 @@ reference's API names (Field2D, State, Schedule, simulate, Flocker).
 """
 from . import _lib
 from ._lib import KbError, lib, LIB_PATH, KB_QUERY_RELAX, KB_QUERY_EXACT, KB_ARITH_STRICT, KB_ARITH_FAST
-from ._lib import KB_CELL_WRAP_CLAMP, KB_CELL_WRAP_TORUS
+from ._lib import KB_CELL_WRAP_CLAMP, KB_CELL_WRAP_TORUS, KB_DENSE_AUTO, KB_DENSE_OFF, KB_DENSE_ON
 from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
@@ -20,7 +20,7 @@ __all__ = [
     "Agent", "AgentImpl",
     "simulate_old", "gen_uniform", "gen_clustered", "KbError", "lib", "LIB_PATH",
     "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
-    "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS",
+    "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS", "KB_DENSE_AUTO", "KB_DENSE_OFF", "KB_DENSE_ON",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
     "ExploreMode", "FlockerConfig", "build_configurations", "explore", "random_search",
     "evolutionary_search", "write_csv",

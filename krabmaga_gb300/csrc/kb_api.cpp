@@ -240,10 +240,26 @@ struct kb_field {
     int a_last = 0;
     bool keys_valid = false;  // buf_key(a_last) holds the bag keys of the virtual write list
     int32_t tile_tx = 0, tile_ty = 0;  // 0: automatic
+    // Dense flocks (long candidate lists, single replica): the force pass
+    // walks each column run with a pointer and the rebin takes 8-bag
+    // segments.  Chosen (dense_mode KB_DENSE_AUTO) from the read buffer's sum
+    // of squared bag occupancies, about 9 * sum / N candidates per boid,
+    // measured after every general rebuild and every DENSE_REFRESH steps
+    // (read back without blocking).  Both paths give the same bits.
+    int32_t dense_mode = KB_DENSE_AUTO;
+    bool dense = false;
+    DevBuf<unsigned long long> occ_dev;
+    unsigned long long* occ_host = nullptr;  // pinned
+    cudaEvent_t occ_ev = nullptr;
+    bool occ_pending = false;
+    uint32_t occ_n = 0;  // boids when the pending measurement was taken
+    uint64_t steps_since_occ = 0;
 
     ~kb_field() {
         drop_graphs();
         if (stream) cudaStreamSynchronize(stream);
+        if (occ_ev) cudaEventDestroy(occ_ev);
+        if (occ_host) cudaFreeHost(occ_host);
         for (auto& k : kt_pending)
             for (cudaEvent_t e : k.ev) cudaEventDestroy(e);
         for (cudaEvent_t e : kt_pool) cudaEventDestroy(e);
@@ -369,6 +385,69 @@ uint32_t total_segments(const kb_field* f) {
     return t > 0xFFFFFFF0ull ? 0u : (uint32_t)t;
 }
 
+// ------------------------------------------------------------ dense flocks
+constexpr uint64_t DENSE_MIN_CANDIDATES = 48;  // estimated mean list length that switches
+constexpr uint64_t DENSE_REFRESH = 64;          // steps between two measurements
+
+bool dense_from(unsigned long long occ2, uint32_t n) {
+    return n > 0 && 9ull * occ2 >= DENSE_MIN_CANDIDATES * (unsigned long long)n;
+}
+
+void set_dense(kb_field* f, bool d) {
+    if (f->dense_mode == KB_DENSE_ON) d = true;
+    if (f->dense_mode == KB_DENSE_OFF || f->reps.size() != 1) d = false;
+    f->dense = d;
+}
+
+// Enqueue a measurement of the read buffer into the pinned word (no wait).
+kb_status occ_enqueue(kb_field* f) {
+    if (f->reps.size() != 1 || f->virt) return KB_OK;
+    if (!f->occ_host) {
+        if (cudaMallocHost(&f->occ_host, sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            f->occ_host = nullptr;
+            return KB_OK;  // no measurement: the flag stays as it is
+        }
+        cudaError_t e = f->occ_dev.alloc(1);
+        if (!e) e = cudaEventCreateWithFlags(&f->occ_ev, cudaEventDisableTiming);
+        if (e) return cuda_fail(e, "occupancy measurement");
+    }
+    KB_CUDA(cudaMemsetAsync(f->occ_dev.p, 0, sizeof(unsigned long long), f->stream));
+    KB_CUDA(launch_occupancy_sq(f->start[f->cur].p, f->ncells_total, f->occ_dev.p, f->stream));
+    KB_CUDA(cudaMemcpyAsync(f->occ_host, f->occ_dev.p, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaEventRecord(f->occ_ev, f->stream));
+    f->occ_pending = true;
+    f->occ_n = f->rn;
+    f->steps_since_occ = 0;
+    return KB_OK;
+}
+
+// Take a finished measurement, if any (never waits).
+void occ_poll(kb_field* f) {
+    if (!f->occ_pending) return;
+    const cudaError_t e = cudaEventQuery(f->occ_ev);
+    if (e == cudaErrorNotReady) return;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        f->occ_pending = false;
+        return;
+    }
+    f->occ_pending = false;
+    set_dense(f, dense_from(*f->occ_host, f->occ_n));
+}
+
+// Bag rows and segment count of the segment rebin.
+void rebin_geometry(const kb_field* f, RebinArgs* a) {
+    if (f->dense && f->reps.size() == 1) {
+        a->seg_rows = DENSE_SEG_ROWS;
+        a->nsegs = rep_segments(f->reps[0], DENSE_SEG_ROWS);
+    } else {
+        a->seg_rows = 0;
+        a->nsegs = total_segments(f);
+    }
+}
+
 kb_status upload_rep(kb_field* f) {
     assign_segments(f->reps);
     f->rep.seg_off = f->reps[0].seg_off;
@@ -482,7 +561,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     a.a_st = f->wst.p;
     a.a_ids = f->wid.p;
     a.ncells = f->ncells_total;
-    a.nsegs = total_segments(f);
+    rebin_geometry(f, &a);
     a.sblk = f->nblk_seg ? f->blk_seg.p : nullptr;
     a.nsblk = f->nblk_seg;
     a.s_st = f->rst.p;
@@ -517,6 +596,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     a.blk = f->nblk_force ? f->blk_force.p : nullptr;
     a.nblk = f->nblk_force;
     a.self_by_slot = f->ids_unique ? 1 : 0;
+    a.dense = f->dense ? 1 : 0;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
     f->hist_counted = true;
     return KB_OK;
@@ -542,7 +622,7 @@ kb_status materialize(kb_field* f) {
     r.a_st = buf_st(f, f->a_last);
     r.a_ids = buf_ids(f, f->a_last);
     r.ncells = f->ncells_total;
-    r.nsegs = total_segments(f);
+    rebin_geometry(f, &r);
     r.sblk = f->nblk_seg ? f->blk_seg.p : nullptr;
     r.nsblk = f->nblk_seg;
     r.s_st = buf_st(f, dst);
@@ -896,10 +976,15 @@ kb_status field_lazy_update(kb_field* f) {
     } else {
         st = general_rebuild(f, false);
         if (st) return st;
+        if ((st = occ_enqueue(f))) return st;  // completes with the read below
         uint32_t total = 0;
         st = read_u32(f, f->start[f->cur].p + f->ncells_total, &total);
         if (st) return st;
         f->rn = total;
+        if (f->occ_pending) {
+            f->occ_n = total;
+            occ_poll(f);
+        }
         // the id multiset may have changed
         if ((st = check_unique_ids(f))) return st;
     }
@@ -1502,6 +1587,24 @@ kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx,
     return KB_OK;
 }
 
+kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode) {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    if (mode != KB_DENSE_AUTO && mode != KB_DENSE_OFF && mode != KB_DENSE_ON)
+        return fail(KB_ERR_ARG, "dense mode must be KB_DENSE_AUTO, KB_DENSE_OFF or KB_DENSE_ON");
+    if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: the batch path keeps one flat list");
+    f->dense_mode = mode;
+    set_dense(f, f->dense);
+    if (mode == KB_DENSE_AUTO) f->steps_since_occ = DENSE_REFRESH;  // measure at the next step
+    return KB_OK;
+}
+
+kb_status kb_field_dense_active(kb_field* f, int32_t* active) {
+    if (!f || !active) return fail(KB_ERR_ARG, "null argument");
+    occ_poll(f);
+    *active = f->dense ? 1 : 0;
+    return KB_OK;
+}
+
 kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long* out16) {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
@@ -1731,6 +1834,10 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
     }
     if (done < nsteps && fused_eligible(f, p)) return tiled_steps(f, p, nsteps - done);
     if (f->virt && (st = materialize(f))) return st;
+    occ_poll(f);
+    if (f->dense_mode == KB_DENSE_AUTO && !f->occ_pending && f->steps_since_occ >= DENSE_REFRESH &&
+        (st = occ_enqueue(f)))
+        return st;
     const bool use_fast = all_fast_rebin_ok(f);
     // CUDA-graph replay of chunks of up to 100 steps (one graph per chunk
     // length and start parity; the graph reads the step number from device
@@ -1738,6 +1845,8 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
     const uint32_t CHUNK = 100;
     while (done < nsteps) {
         const uint32_t k = std::min(CHUNK, nsteps - done);
+        if (done) occ_poll(f);
+        f->steps_since_occ += k;
         if (k < 4) {
             if ((st = enqueue_steps(f, p, k, use_fast))) return st;
             done += k;
@@ -1752,6 +1861,7 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
         key.params.push_back((uint8_t)((f->rn >> 8) & 0xff));
         key.params.push_back((uint8_t)((f->rn >> 16) & 0xff));
         key.params.push_back((uint8_t)((f->rn >> 24) & 0xff));
+        key.params.push_back((uint8_t)f->dense);
         auto it = f->graphs.find(key);
         const int cur0 = f->cur;
         if (it == f->graphs.end()) {

@@ -121,7 +121,11 @@ __device__ __forceinline__ void columns_runs(const ForceArgs& a, const Rep& R, i
 }
 // The three runs of a one-bag ring as one flat list: a warp then iterates
 // the longest lane's total instead of the sum of the per-column maxima.
-template <bool STRICT>
+// DENSE: long lists; each run is walked with a plain pointer (one run after
+// the other, the same visiting order), which costs fewer instructions per
+// candidate once the runs are long enough that the per-run maxima of a warp
+// add little.
+template <bool STRICT, bool DENSE>
 // my_slot: the boid's own read-buffer slot when ids are unique (a candidate
 // is the boid itself exactly there), else ~0u and ids are compared.
 __device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, int mi, int Mi,
@@ -140,7 +144,16 @@ __device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, 
     const uint32_t P1 = e[0] - s[0], P2 = P1 + (e[1] - s[1]), T = P2 + (e[2] - s[2]);
     acc.vec += T;
     const uint32_t d1 = s[1] - P1, d2 = s[2] - P2;  // position = f + d (mod 2^32)
-    if (R.nowrap && my_slot != 0xFFFFFFFFu) {
+    if (DENSE && R.nowrap && my_slot != 0xFFFFFFFFu) {
+#pragma unroll 1
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t ek = e[k];
+            for (uint32_t q = s[k]; q < ek; ++q) {
+                const float4 o = __ldg(a.st + q);
+                if (q != my_slot) acc.template add<true>(R, me.x, me.y, o);
+            }
+        }
+    } else if (R.nowrap && my_slot != 0xFFFFFFFFu) {
         for (uint32_t f = 0; f < T; ++f) {
             const uint32_t p = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
             const float4 o = __ldg(a.st + p);
@@ -180,7 +193,7 @@ __device__ __forceinline__ void force_finish(const ForceArgs& a, const Rep& R, u
 // The candidate sums of one agent at `me` against the read buffer (the
 // query of bird.rs:41 and the loop of bird.rs:48-82).  my_slot: the agent's
 // own read-buffer slot when self is recognised by slot, else ~0u.
-template <bool STRICT, int QMODE>
+template <bool STRICT, int QMODE, bool DENSE = false>
 __device__ __forceinline__ void gather_candidates(const ForceArgs& a, const Rep& R, float4 me,
                                                   uint32_t my_id, uint32_t my_slot,
                                                   Acc<STRICT>& acc) {
@@ -194,7 +207,7 @@ __device__ __forceinline__ void gather_candidates(const ForceArgs& a, const Rep&
                 // a one-bag ring (the common case) as one flat list; the wider
                 // two-bag ring out of line
                 if (Mi - mi < 3)
-                    columns_flat3(a, R, mi, Mi, mj, Mj, me, my_id, acc, my_slot);
+                    columns_flat3<STRICT, DENSE>(a, R, mi, Mi, mj, Mj, me, my_id, acc, my_slot);
                 else columns_runs_5(a, R, mi, Mi, mj, Mj, me, my_id, acc);
             }
         } else {
@@ -232,13 +245,13 @@ __device__ __forceinline__ void gather_candidates(const ForceArgs& a, const Rep&
     }
 }
 
-template <bool STRICT, int QMODE>
+template <bool STRICT, int QMODE, bool DENSE>
 __device__ __forceinline__ void force_body(const ForceArgs& a, const Rep& R, uint32_t i) {
     const unsigned long long step = *a.step;
     const float4 me = __ldg(a.st + i);
     const uint32_t my_id = __ldg(a.ids + i);
     Acc<STRICT> acc;
-    gather_candidates<STRICT, QMODE>(a, R, me, my_id, a.self_by_slot ? i : 0xFFFFFFFFu, acc);
+    gather_candidates<STRICT, QMODE, DENSE>(a, R, me, my_id, a.self_by_slot ? i : 0xFFFFFFFFu, acc);
     force_finish<STRICT>(a, R, i, me, my_id, step, acc);
 }
 
@@ -292,7 +305,7 @@ __device__ __forceinline__ void load_rep_shared(Rep* dst, const Rep* src) {
         reinterpret_cast<uint32_t*>(dst)[threadIdx.x] = __ldg(reinterpret_cast<const uint32_t*>(src) + threadIdx.x);
 }
 
-template <bool STRICT, int QMODE, bool MULTI>
+template <bool STRICT, int QMODE, bool MULTI, bool DENSE = false>
 __global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI : KB_FORCE_MINB)
     k_flock_force(ForceArgs a) {
     pdl_enter();
@@ -305,11 +318,11 @@ __global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI 
         __syncthreads();
         const uint32_t k = e.y + threadIdx.x;
         if (k >= sR.boid_off + sR.nboids) return;
-        force_body<STRICT, QMODE>(a, sR, k);
+        force_body<STRICT, QMODE, false>(a, sR, k);
         return;
     }
     if (i >= a.n) return;
-    force_body<STRICT, QMODE>(a, a.rep0, i);
+    force_body<STRICT, QMODE, DENSE>(a, a.rep0, i);
 }
 
 // Bird::step for agents given by the caller rather than read from the read
@@ -803,15 +816,18 @@ __device__ __forceinline__ void seg_batch(const RebinArgs& a, bool valid, uint32
     }
 }
 
+// ROWS (<= 32) consecutive bags of one column per warp.
+template <int ROWS>
 __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, uint32_t g,
                                               uint32_t* cnt) {
+    static_assert(ROWS >= 1 && ROWS <= 32, "a segment's bags map to the lanes of one warp");
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t nsy = ((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS;
+    const uint32_t nsy = ((uint32_t)R.dh + ROWS - 1) / ROWS;
     const uint32_t local = g - R.seg_off;
     const uint32_t Xu = local / nsy;
     const int X = (int)Xu;
-    const int Y0 = (int)(local - Xu * nsy) * SEG_ROWS;
-    const int nb = min(SEG_ROWS, R.dh - Y0);
+    const int Y0 = (int)(local - Xu * nsy) * ROWS;
+    const int nb = min(ROWS, R.dh - Y0);
     const int Y1 = Y0 + nb - 1;
     const uint32_t c0 = R.cell_off + Xu * (uint32_t)R.dh + (uint32_t)Y0;
     const bool interior = X > 0 && X < R.seam && Y0 > 0 && Y1 < R.seam;
@@ -878,7 +894,7 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
 #define KB_REBIN_MINB 8
 #endif
 
-template <bool MULTI>
+template <bool MULTI, int ROWS = SEG_ROWS>
 __global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_seg(RebinArgs a) {
     pdl_enter();
     __shared__ uint32_t s_cnt[REBIN_SEG_WARPS][32];
@@ -892,12 +908,33 @@ __global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_s
         __syncthreads();
         const uint32_t g = e.y + w;
         if (g >= sR.seg_off + rep_segments_dev(sR)) return;  // whole warps
-        rebin_segment(a, sR, g, s_cnt[w]);
+        rebin_segment<SEG_ROWS>(a, sR, g, s_cnt[w]);
         return;
     }
     const uint32_t g = blockIdx.x * REBIN_SEG_WARPS + w;
     if (g >= a.nsegs) return;  // whole warps
-    rebin_segment(a, a.rep0, g, s_cnt[w]);
+    rebin_segment<ROWS>(a, a.rep0, g, s_cnt[w]);
+}
+
+// Sum of squared bag occupancies of a read buffer (its offsets), a measure
+// of how long the candidate lists are: about 9 * sum / N per boid.
+__global__ void k_occupancy_sq(const uint32_t* __restrict__ start, uint32_t ncells,
+                               unsigned long long* out) {
+    __shared__ unsigned long long s_part[8];
+    unsigned long long acc = 0;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
+        const unsigned long long o = (unsigned long long)(start[c + 1] - start[c]);
+        acc += o * o;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(FULL_MASK, acc, d);
+    if ((threadIdx.x & 31u) == 0u) s_part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_part[w];
+        atomicAdd(out, t);
+    }
 }
 
 // ---------------------------------------------------------- general sort
@@ -1292,6 +1329,10 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
     if (multi && a.blk == nullptr) return cudaErrorInvalidValue;
     const unsigned g = multi ? a.nblk : grid_for(a.n, KB_FORCE_THREADS);
 #define KB_FORCE(S, Q, MU) return launch_pdl(k_flock_force<S, Q, MU>, g, KB_FORCE_THREADS, s, a)
+    if (a.dense && qmode == 0 && !multi) {
+        if (strict) return launch_pdl(k_flock_force<true, 0, false, true>, g, KB_FORCE_THREADS, s, a);
+        return launch_pdl(k_flock_force<false, 0, false, true>, g, KB_FORCE_THREADS, s, a);
+    }
     if (strict) {
         if (qmode == 0) { if (multi) KB_FORCE(true, 0, true); else KB_FORCE(true, 0, false); }
         else { if (multi) KB_FORCE(true, 1, true); else KB_FORCE(true, 1, false); }
@@ -1329,11 +1370,23 @@ cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s) {
     if (a.key != nullptr && a.nsegs > 0 && (a.nrep == 1 || a.sblk != nullptr)) {
         if (a.nrep > 1) return launch_pdl(k_rebin_seg<true>, a.nsblk, 32 * REBIN_SEG_WARPS, s, a);
         const unsigned gs = grid_for(a.nsegs, REBIN_SEG_WARPS);
+        if (a.seg_rows == DENSE_SEG_ROWS)
+            return launch_pdl(k_rebin_seg<false, DENSE_SEG_ROWS>, gs, 32 * REBIN_SEG_WARPS, s, a);
+        if (a.seg_rows != 0 && a.seg_rows != SEG_ROWS) return cudaErrorInvalidValue;
         return launch_pdl(k_rebin_seg<false>, gs, 32 * REBIN_SEG_WARPS, s, a);
     }
     const unsigned g = grid_for(a.ncells > 0 ? a.ncells : 1, 256);
     if (a.nrep > 1) k_rebin<true><<<g, 256, 0, s>>>(a);
     else k_rebin<false><<<g, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occupancy_sq(const uint32_t* start, uint32_t ncells, unsigned long long* out,
+                                cudaStream_t s) {
+    if (ncells == 0) return cudaSuccess;
+    const unsigned g0 = grid_for(ncells, 256);
+    const unsigned g = g0 < 608u ? g0 : 608u;  // grid-stride: four blocks per SM of 152
+    k_occupancy_sq<<<g, 256, 0, s>>>(start, ncells, out);
     return cudaGetLastError();
 }
 

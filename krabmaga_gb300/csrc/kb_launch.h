@@ -66,6 +66,10 @@ struct ForceArgs {
     // ids are unique within every replica: a candidate is the boid itself
     // exactly when it is the boid's own slot, so no id is loaded per candidate
     int32_t self_by_slot;
+    // long candidate lists (dense flocks, single replica): walk each column
+    // run with a plain pointer instead of the flat index formula (the same
+    // visiting order, fewer instructions per candidate)
+    int32_t dense;
 };
 constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
@@ -89,7 +93,8 @@ struct RebinArgs {
     const float4* a_st;
     const uint32_t* a_ids;
     uint32_t ncells;
-    uint32_t nsegs;  // 32-bag column segments over all replicas (0: per-bag kernel only)
+    uint32_t nsegs;  // column segments over all replicas (0: per-bag kernel only)
+    int32_t seg_rows;  // bags per segment of a single replica: 0 (SEG_ROWS) or DENSE_SEG_ROWS
     // several replicas: one block per entry {replica, first segment}, up to
     // REBIN_SEG_WARPS segments of that replica
     const uint2* sblk;
@@ -101,11 +106,17 @@ struct RebinArgs {
 };
 // Bag segments of the segment rebin: SEG_ROWS consecutive bags of one column.
 constexpr int SEG_ROWS = 32;
+// Shorter segments for dense flocks: a segment's source runs are long there,
+// and the warp walks them in order, so fewer rows per warp shorten the tail.
+constexpr int DENSE_SEG_ROWS = 8;
 constexpr int REBIN_SEG_WARPS = 8;  // segments (warps) per block
-inline uint32_t rep_segments(const Rep& R) {
-    return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
+inline uint32_t rep_segments(const Rep& R, int rows = SEG_ROWS) {
+    return (uint32_t)R.dw * (((uint32_t)R.dh + (uint32_t)rows - 1) / (uint32_t)rows);
 }
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s);
+// *out += sum over bags of (start[c+1] - start[c])^2 (the caller zeroes *out).
+cudaError_t launch_occupancy_sq(const uint32_t* start, uint32_t ncells, unsigned long long* out,
+                                cudaStream_t s);
 // Whether any (replica, id) pair repeats in the read buffer (n boids, nrep
 // replicas by boid_off): an open-addressing table of cap (a power of two,
 // >= 2n) 64-bit words, cleared here; *dup is set to 1 on a repeat.

@@ -284,6 +284,16 @@ class Field2D:
         L.call("kb_field_set_step_options", self._h, C.c_int32(mode), C.c_int32(tile_tx),
                C.c_int32(tile_ty))
 
+    def set_dense_mode(self, mode: int = L.KB_DENSE_AUTO) -> None:
+        """Candidate-list walk: KB_DENSE_AUTO (by bag occupancy), _OFF (one flat
+        list, 32-bag rebin segments), _ON (per-run walk, 8-bag segments)."""
+        L.call("kb_field_set_dense_mode", self._h, C.c_int32(mode))
+
+    def dense_active(self) -> bool:
+        v = C.c_int32()
+        L.call("kb_field_dense_active", self._h, C.byref(v))
+        return bool(v.value)
+
     def autotune(self, params, first_step: int, steps_per_trial: int = 5, candidates=None):
         """Pick the fastest fused tile shape by timing real steps; returns
         (tx, ty, steps consumed, ms per step)."""

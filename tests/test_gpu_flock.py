@@ -316,6 +316,57 @@ def test_4m_clustered_quarter_size_digests(gpu):
     oc, od = o.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, q)
     assert np.array_equal(gc, oc) and np.array_equal(gd, od)
     assert gc.max() > 100  # dense cluster cores are exercised
+    assert f.dense_active()  # the per-run walk and 8-bag rebin segments ran
+
+
+@pytest.mark.parametrize("arith", [kg.KB_ARITH_STRICT, kg.KB_ARITH_FAST])
+def test_dense_walk_gives_the_same_bits(gpu, arith):
+    # A clustered flock takes the per-run candidate walk and 8-bag rebin
+    # segments by itself; forcing the flat walk gives the same bits over
+    # graph-replayed steps, and strict arithmetic equals the oracle.
+    n, side = 1 << 16, 1600.0
+    ids0, xy0, dxy0 = kg.gen_clustered(n, side, side, 16, 30.0, 0.3, 5)
+    p = kg.FlockParams(seed=3, arith=arith)
+    a = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    b = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    assert a.dense_active()
+    b.set_dense_mode(kg.KB_DENSE_OFF)
+    assert not b.dense_active()
+    step(a, p, 0, 12)
+    step(b, p, 0, 12)
+    ia, sa = a.get_state()
+    ib, sb = b.get_state()
+    assert np.array_equal(ia, ib) and same_bits(sa, sb)
+    assert a.device_flags() == 0 and b.device_flags() == 0
+    if arith == kg.KB_ARITH_STRICT:
+        o = oracle_field(side, FLOCK_D, ids0, xy0, dxy0)
+        o.flock_run(oracle.params_from(p), 0, 12)
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(ia, oids) and same_bits(sa, ost)
+
+
+def test_dense_walk_forced_on_a_uniform_flock(gpu):
+    n = 20000
+    side = float(np.float32(np.sqrt(n / 0.025)))
+    ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 9, 1.0)
+    p = kg.FlockParams(seed=4, arith=kg.KB_ARITH_FAST)
+    u = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    v = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    assert not u.dense_active()
+    u.set_dense_mode(kg.KB_DENSE_ON)
+    assert u.dense_active()
+    step(u, p, 0, 10)
+    step(v, p, 0, 10)
+    iu, su = u.get_state()
+    iv, sv = v.get_state()
+    assert np.array_equal(iu, iv) and same_bits(su, sv)
+    # back to automatic: the next step measures the occupancies again
+    u.set_dense_mode(kg.KB_DENSE_AUTO)
+    step(u, p, 10, 1)
+    u.synchronize()
+    assert not u.dense_active()
+    with pytest.raises(kg.KbError):
+        u.set_dense_mode(7)
 
 
 def test_device_jitter_matches_oracle_philox(gpu):
