@@ -33,6 +33,11 @@ KB_CELL_WRAP_TORUS = 1
 KB_DENSE_AUTO = 0
 KB_DENSE_OFF = 1
 KB_DENSE_ON = 2
+KB_PATH_SEPARATE = 0
+KB_PATH_FUSED = 1
+KB_PATH_TILED = 2
+KB_PATH_SMALL = 3
+KB_PATH_DENSE = 4
 
 STATUS_NAMES = {
     0: "KB_OK", 1: "KB_ERR_ARG", 2: "KB_ERR_OOM", 3: "KB_ERR_CUDA", 4: "KB_ERR_TIMEOUT",
@@ -168,6 +173,7 @@ _SIGS = {
     "kb_field_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "kb_field_set_dense_mode": (C.c_int32, [_P, C.c_int32]),
     "kb_field_dense_active": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
+    "kb_field_step_path": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "kb_field_step_stats": (C.c_int32, [_P, _U32]),
     "kb_field_set_kernel_timing": (C.c_int32, [_P, C.c_int32]),
     "kb_field_kernel_times": (C.c_int32, [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),

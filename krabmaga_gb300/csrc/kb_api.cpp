@@ -223,7 +223,9 @@ struct kb_field {
         FusedCfg occ_cfg{};
         int occ_strict = -1, occ_qmode = -1, occ_ctas = 0;
     } fused;
-    int fused_mode = 0;  // 0 separate kernels, 1 persistent fused, 2 split tile step
+    // 0 separate kernels (small fields: one block, kb_small.cu), 1 persistent
+    // fused, 2 split tile step, 3 separate kernels whatever the size
+    int fused_mode = 0;
     // Per-kernel timing of ungraphed separate-kernel steps: four events per
     // step (force | scan | rebin), read and recycled by kb_field_kernel_times.
     bool ktime = false;
@@ -435,6 +437,14 @@ void occ_poll(kb_field* f) {
     }
     f->occ_pending = false;
     set_dense(f, dense_from(*f->occ_host, f->occ_n));
+}
+
+// Whole steps in one thread block (kb_small.cu): a plain field small enough
+// for shared memory, on the default step path.
+bool small_eligible(const kb_field* f) {
+    return !f->is_batch && f->reps.size() == 1 && f->fused_mode == 0 && !f->virt && f->rn > 0 &&
+           f->rn <= SMALL_MAX_BOIDS && f->reps[0].ncells <= SMALL_MAX_CELLS &&
+           f->reps[0].cell_off == 0;
 }
 
 // Bag rows and segment count of the segment rebin.
@@ -661,7 +671,8 @@ FusedCfg fused_config(const kb_field* f, int dd) {
 }
 
 bool fused_eligible(const kb_field* f, const kb_flock_params* p) {
-    if (f->fused_mode == 0 || !f->layout_is_positions || f->rn == 0) return false;
+    if ((f->fused_mode != 1 && f->fused_mode != 2) || !f->layout_is_positions || f->rn == 0)
+        return false;
     if (p->query_mode != KB_QUERY_RELAX && p->query_mode != KB_QUERY_EXACT) return false;
     for (const Rep& R : f->reps)
         if (!R.toroidal || R.cell_wrap || !fast_rebin_ok(R) || R.dd > FUSED_DD_MAX || R.dw > 65535 ||
@@ -1579,7 +1590,7 @@ kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx,
     if (!f) return fail(KB_ERR_ARG, "null argument");
     if (tile_tx < 0 || tile_ty < 0 || tile_tx > 64 || tile_ty > 128)
         return fail(KB_ERR_ARG, "tile shape out of range (tx <= 64, ty <= 128)");
-    if (fused < 0 || fused > 2) return fail(KB_ERR_ARG, "step mode must be 0, 1 or 2");
+    if (fused < 0 || fused > 3) return fail(KB_ERR_ARG, "step mode must be 0, 1, 2 or 3");
     f->fused_mode = fused;
     f->tile_tx = tile_tx;
     f->tile_ty = tile_ty;
@@ -1595,6 +1606,17 @@ kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode) {
     f->dense_mode = mode;
     set_dense(f, f->dense);
     if (mode == KB_DENSE_AUTO) f->steps_since_occ = DENSE_REFRESH;  // measure at the next step
+    return KB_OK;
+}
+
+kb_status kb_field_step_path(kb_field* f, int32_t* path) {
+    if (!f || !path) return fail(KB_ERR_ARG, "null argument");
+    occ_poll(f);
+    kb_flock_params q{};
+    q.query_mode = KB_QUERY_RELAX;
+    if (fused_eligible(f, &q)) *path = f->fused_mode;
+    else if (small_eligible(f)) *path = KB_PATH_SMALL;
+    else *path = f->dense ? KB_PATH_DENSE : KB_PATH_SEPARATE;
     return KB_OK;
 }
 
@@ -1834,6 +1856,25 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
     }
     if (done < nsteps && fused_eligible(f, p)) return tiled_steps(f, p, nsteps - done);
     if (f->virt && (st = materialize(f))) return st;
+    if (small_eligible(f)) {
+        // a small field: whole steps in one block, up to 1000 per launch
+        while (done < nsteps) {
+            const uint32_t k = std::min<uint32_t>(1000u, nsteps - done);
+            SmallArgs a{};
+            a.rep = f->reps[0];
+            a.st = f->rst.p;
+            a.ids = f->rid.p;
+            a.start = f->start[f->cur].p;
+            a.n = f->rn;
+            a.nsteps = k;
+            a.step = f->dstep.p;
+            a.err = f->err.p;
+            a.self_by_slot = f->ids_unique ? 1 : 0;
+            KB_CUDA(launch_small_steps(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
+            done += k;
+        }
+        return KB_OK;
+    }
     occ_poll(f);
     if (f->dense_mode == KB_DENSE_AUTO && !f->occ_pending && f->steps_since_occ >= DENSE_REFRESH &&
         (st = occ_enqueue(f)))

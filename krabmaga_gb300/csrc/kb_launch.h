@@ -73,6 +73,30 @@ struct ForceArgs {
 };
 constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
+// Whole steps of a small single-replica field in one 1024-thread block
+// (kb_small.cu): the read buffer (st, ids, start over rep.ncells bags) is
+// loaded into shared memory, nsteps steps run there, and the final read
+// buffer, offsets and step counter (*step += nsteps) are written back.
+constexpr int SMALL_THREADS = 1024;
+// Measured on GB300 (uniform flocks, runs of 400 steps per call): the one
+// block takes 6.6 / 10.0 / 12.7 / 18.4 us per step at 16 / 256 / 512 / 1000
+// boids, the separate kernels 13.2 / 12.0 / 12.0 / 13.8 us.
+constexpr uint32_t SMALL_MAX_BOIDS = 256;
+constexpr uint32_t SMALL_MAX_CELLS = 4096;
+struct SmallArgs {
+    Rep rep;
+    float4* st;
+    uint32_t* ids;
+    uint32_t* start;
+    uint32_t n;
+    uint32_t nsteps;
+    unsigned long long* step;
+    uint32_t* err;
+    int32_t self_by_slot;
+};
+size_t small_smem_bytes(uint32_t n, uint32_t ncells);
+cudaError_t launch_small_steps(const SmallArgs& a, bool strict, int qmode, cudaStream_t s);
+
 // Bird::step of nin caller-given agents (in_st {x, y, dx, dy}, in_ids) against
 // the read buffer of a single replica; agent j's next state, id and bag key
 // go to slot j of a.out_st / a.out_ids / a.out_key, its arrival into a.hist.

@@ -278,8 +278,9 @@ class Field2D:
         return counts[: len(q)], dig[: len(q)]
 
     def set_step_options(self, mode=0, tile_tx: int = 0, tile_ty: int = 0) -> None:
-        """Step path: 0 separate kernels (default), 2 tiled split, 1 persistent
-        (True/False mean 2/0); tile shape in bags (0 = automatic)."""
+        """Step path: 0 separate kernels (default; fields of at most 256 boids
+        run whole steps in one block), 3 separate kernels whatever the size, 2 tiled split,
+        1 persistent (True/False mean 2/0); tile shape in bags (0 = automatic)."""
         mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)
         L.call("kb_field_set_step_options", self._h, C.c_int32(mode), C.c_int32(tile_tx),
                C.c_int32(tile_ty))
@@ -288,6 +289,12 @@ class Field2D:
         """Candidate-list walk: KB_DENSE_AUTO (by bag occupancy), _OFF (one flat
         list, 32-bag rebin segments), _ON (per-run walk, 8-bag segments)."""
         L.call("kb_field_set_dense_mode", self._h, C.c_int32(mode))
+
+    def step_path(self) -> int:
+        """KB_PATH_* of the next kb_flock_step."""
+        v = C.c_int32()
+        L.call("kb_field_step_path", self._h, C.byref(v))
+        return v.value
 
     def dense_active(self) -> bool:
         v = C.c_int32()
