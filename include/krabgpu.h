@@ -223,8 +223,9 @@ kb_status kb_field_dense_active(kb_field* f, int32_t* active);
 /* Per-kernel timing (no reference counterpart; measurement only).  While
  * enabled, every separate-kernel step that is not replayed from a graph (a
  * kb_flock_step call of fewer than 4 steps) records CUDA events around its
- * three launches on the field's stream.  kb_field_kernel_times waits for
- * them, returns the summed milliseconds of {force, scan, rebin} and the
+ * launches on the field's stream (force | the offsets scan | rebin; the
+ * one-block path of small fields records none).  kb_field_kernel_times waits
+ * for them, returns the summed milliseconds of {force, scan, rebin} and the
  * number of steps timed, and starts a new tally. */
 kb_status kb_field_set_kernel_timing(kb_field* f, int32_t enable);
 kb_status kb_field_kernel_times(kb_field* f, double ms[3], uint64_t* steps);
