@@ -194,8 +194,9 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
 /* Step implementation options (no reference counterpart; tuning only).
  * mode (the `fused` argument): 0 (default) the separate force / scan / rebin
  * kernels (a plain field replays runs of 4 steps or more from CUDA graphs),
- * except that a plain field of at most 256 boids and 4096 bags runs whole
- * steps in one thread block (shared memory, up to 1000 steps per launch);
+ * except that a call of 2 steps or more on a plain field of at most 1536
+ * boids and 4096 bags runs whole steps in one 8-block thread-block cluster
+ * (shared memory, up to 1000 steps per launch);
  * 3 the separate kernels whatever the field's size;
  * for eligible fields (toroidal, square, jump < discretization) 2 the tiled
  * step as two launches per step (stage + rebin + force per tile, then the
@@ -216,7 +217,7 @@ kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode);
 #define KB_PATH_SEPARATE 0 /* separate kernels, flat candidate list */
 #define KB_PATH_FUSED 1    /* persistent fused tiles */
 #define KB_PATH_TILED 2    /* split tile step */
-#define KB_PATH_SMALL 3    /* whole steps in one thread block */
+#define KB_PATH_SMALL 3    /* whole steps in one cluster (calls of 2 steps or more) */
 #define KB_PATH_DENSE 4    /* separate kernels, per-run walk (dense flocks) */
 kb_status kb_field_step_path(kb_field* f, int32_t* path);
 kb_status kb_field_dense_active(kb_field* f, int32_t* active);

@@ -1856,8 +1856,10 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
     }
     if (done < nsteps && fused_eligible(f, p)) return tiled_steps(f, p, nsteps - done);
     if (f->virt && (st = materialize(f))) return st;
-    if (small_eligible(f)) {
-        // a small field: whole steps in one block, up to 1000 per launch
+    if (small_eligible(f) && nsteps - done >= 2) {
+        // a small field: whole steps in one cluster, up to 1000 per launch
+        // (a single step is quicker on the separate kernels: the cluster's
+        // launch, load and write-back cost more than it saves there)
         while (done < nsteps) {
             const uint32_t k = std::min<uint32_t>(1000u, nsteps - done);
             SmallArgs a{};

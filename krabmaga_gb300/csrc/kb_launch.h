@@ -73,15 +73,17 @@ struct ForceArgs {
 };
 constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
-// Whole steps of a small single-replica field in one 1024-thread block
-// (kb_small.cu): the read buffer (st, ids, start over rep.ncells bags) is
-// loaded into shared memory, nsteps steps run there, and the final read
-// buffer, offsets and step counter (*step += nsteps) are written back.
+// Whole steps of a small single-replica field in one cluster of SMALL_CTAS
+// blocks (kb_small.cu): every block loads the read buffer (st, ids, start
+// over rep.ncells bags) into its shared memory, nsteps steps run there, and
+// the final read buffer, offsets and step counter (*step += nsteps) are
+// written back.
 constexpr int SMALL_THREADS = 1024;
-// Measured on GB300 (uniform flocks, runs of 400 steps per call): the one
-// block takes 6.6 / 10.0 / 12.7 / 18.4 us per step at 16 / 256 / 512 / 1000
-// boids, the separate kernels 13.2 / 12.0 / 12.0 / 13.8 us.
-constexpr uint32_t SMALL_MAX_BOIDS = 256;
+constexpr uint32_t SMALL_CTAS = 8;  // a portable cluster size
+// Measured on GB300 (uniform flocks, 400-step calls): 7.0 / 9.2 / 11.6 /
+// 13.4 / 15.1 us per step at 16 / 256 / 1000 / 1500 / 2048 boids, against
+// 13.6 / 12.1 / 14.0 / 14.7 / 14.9 us for the separate kernels.
+constexpr uint32_t SMALL_MAX_BOIDS = 1536;
 constexpr uint32_t SMALL_MAX_CELLS = 4096;
 struct SmallArgs {
     Rep rep;

@@ -1,27 +1,35 @@
-// kb_small.cu -- whole steps of a small field in one thread block.
+// kb_small.cu -- whole steps of a small field in one thread-block cluster.
 //
 // A field of at most SMALL_MAX_BOIDS boids and SMALL_MAX_CELLS bags (the
-// reference's own test fields) is launch-bound on the separate-kernel path:
-// four launches per step for a few microseconds of work.  Here one
-// 1024-thread block loads the read buffer and its bag offsets into shared
-// memory and runs every step of the call there:
-//   1. the agent pass: Bird::step for every boid against the read buffer
-//      (the same candidate order, accumulator and finish as k_flock_force),
-//      next states into a write list in read order, arrivals counted per bag;
-//   2. lazy_update: an exclusive scan of the arrivals into the next bag
-//      offsets, then a stable scatter of the write list by bag key by one
-//      warp in list order (__match_any_sync ranks equal keys by lane, a
-//      per-bag cursor carries the rank across batches), which is the
-//      reference's insertion order inside a bag;
-// and writes the final read buffer, its offsets and the step counter back.
-// The scatter needs no bound on how far a boid moves.  Beyond a few hundred
-// boids one SM's issue rate and the one-warp scatter cost more than the
-// separate kernels' launches (the bound SMALL_MAX_BOIDS is measured).
+// 1,000-boid Flockers case, the reference's own test fields) is launch-bound
+// on the separate-kernel path: four launches per step for a few microseconds
+// of work.  Here a cluster of SMALL_CTAS blocks runs every step of the call
+// in one launch.  Each block holds a full copy of the read buffer and its
+// bag offsets in shared memory and owns one contiguous chunk of the boids:
+//   1. agent pass: Bird::step for the chunk's boids against the local copy
+//      (the same candidate order, accumulator and finish as k_flock_force);
+//      next states, ids and bag keys go to a local write list, arrivals are
+//      counted per bag in the block's own counters;
+//   -- cluster barrier --
+//   2. lazy_update: every block sums the counters of all blocks through
+//      distributed shared memory, scans them into the next bag offsets, and
+//      places its own chunk: position = offset of the bag + arrivals from
+//      lower-ranked blocks (earlier in list order) + rank inside the chunk
+//      (one warp walks the chunk in list order, __match_any_sync ranks equal
+//      keys, a per-bag cursor carries the rank), which is the reference's
+//      insertion order inside a bag; each record is written into every
+//      block's copy of the next read buffer;
+//   -- cluster barrier --
+// and block 0 writes the final read buffer, offsets and step counter back.
+// No bound on how far a boid moves is needed.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "kb_common.h"
 #include "kb_device.cuh"
 #include "kb_launch.h"
+
+namespace cg = cooperative_groups;
 
 namespace kb {
 namespace {
@@ -65,15 +73,18 @@ __device__ __forceinline__ void gather_small(const Rep& R, const float4* st, con
     }
 }
 
-// Exclusive scan of in[0..n) into out[0..n] (out[n] = total), n <= 4096, by
-// a 1024-thread block; in[] is zeroed as it is read.
-__device__ __forceinline__ void block_scan_small(uint32_t* in, uint32_t* out, uint32_t n,
+// Exclusive scan of in[0..n) into out[0..n] (out[n] = total) by one block of
+// SMALL_THREADS threads, n <= SMALL_THREADS * SMALL_SCAN_ITEMS; in may be out.
+constexpr int SMALL_SCAN_ITEMS = (int)SMALL_MAX_CELLS / SMALL_THREADS;
+static_assert(SMALL_SCAN_ITEMS * SMALL_THREADS == (int)SMALL_MAX_CELLS, "scan tiling");
+__device__ __forceinline__ void block_scan_small(const uint32_t* in, uint32_t* out, uint32_t n,
                                                  uint32_t* warp_sums) {
     const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
-    const uint32_t b = t * 4u;
-    uint32_t v[4], sum = 0;
+    constexpr uint32_t NW = SMALL_THREADS / 32;
+    const uint32_t b = t * SMALL_SCAN_ITEMS;
+    uint32_t v[SMALL_SCAN_ITEMS], sum = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < SMALL_SCAN_ITEMS; ++j) {
         v[j] = b + j < n ? in[b + j] : 0u;
         sum += v[j];
     }
@@ -86,61 +97,85 @@ __device__ __forceinline__ void block_scan_small(uint32_t* in, uint32_t* out, ui
     if (lane == 31u) warp_sums[w] = incl;
     __syncthreads();
     if (w == 0) {
-        uint32_t x = warp_sums[lane], xi = x;
+        const uint32_t x = lane < NW ? warp_sums[lane] : 0u;
+        uint32_t xi = x;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t y = __shfl_up_sync(SMALL_FULL, xi, d);
             if (lane >= (uint32_t)d) xi += y;
         }
-        warp_sums[lane] = xi - x;  // exclusive prefix of each warp
-        if (lane == 31u) warp_sums[32] = xi;  // total
+        if (lane < NW) warp_sums[lane] = xi - x;  // exclusive prefix of each warp
+        if (lane == 31u) warp_sums[32] = xi;      // total
     }
     __syncthreads();
     uint32_t run = warp_sums[w] + incl - sum;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        if (b + j < n) {
-            out[b + j] = run;
-            in[b + j] = 0u;
-        }
+    for (int j = 0; j < SMALL_SCAN_ITEMS; ++j) {
+        if (b + j < n) out[b + j] = run;
         run += v[j];
     }
     if (t == 0) out[n] = warp_sums[32];
     __syncthreads();
 }
 
+// Shared-memory layout (byte offsets), the same in every block of the cluster.
+struct SmallLayout {
+    uint32_t rd_st, wr_st, rd_id, wr_id, wr_key, start, nstart, cnt, cur, bytes;
+};
+__host__ __device__ inline SmallLayout small_layout(uint32_t n, uint32_t ncells, uint32_t chunk) {
+    SmallLayout L{};
+    uint32_t o = 0;
+    L.rd_st = o;  o += n * 16u;
+    L.wr_st = o;  o += chunk * 16u;
+    L.rd_id = o;  o += n * 4u;
+    L.wr_id = o;  o += chunk * 4u;
+    L.wr_key = o; o += chunk * 4u;
+    L.start = o;  o += (ncells + 1u) * 4u;
+    L.nstart = o; o += (ncells + 1u) * 4u;
+    L.cnt = o;    o += ncells * 4u;
+    L.cur = o;    o += ncells * 4u;
+    L.bytes = o;
+    return L;
+}
+
 template <bool STRICT, int QMODE>
 __global__ void __launch_bounds__(SMALL_THREADS, 1) k_small_steps(SmallArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cl = cg::this_cluster();
     const Rep& R = a.rep;
     const uint32_t n = a.n, C = R.ncells;
-    float4* s_rd = reinterpret_cast<float4*>(smem);   // read buffer (canonical)
-    float4* s_wr = s_rd + n;                           // write list (read order)
-    uint32_t* i_rd = reinterpret_cast<uint32_t*>(s_wr + n);
-    uint32_t* i_wr = i_rd + n;
-    uint32_t* key = i_wr + n;
-    uint32_t* start = key + n;          // offsets of the read buffer (C+1)
-    uint32_t* nstart = start + C + 1;   // offsets of the next one (C+1)
-    uint32_t* cnt = nstart + C + 1;     // arrivals per bag, then the scatter cursors (C)
+    const uint32_t rank = cl.block_rank();
+    const uint32_t chunk = (n + SMALL_CTAS - 1) / SMALL_CTAS;
+    const uint32_t lo = min(n, rank * chunk), hi = min(n, lo + chunk);
+    const SmallLayout Lo = small_layout(n, C, chunk);
+    float4* rd_st = reinterpret_cast<float4*>(smem + Lo.rd_st);
+    uint32_t* rd_id = reinterpret_cast<uint32_t*>(smem + Lo.rd_id);
+    uint32_t* start = reinterpret_cast<uint32_t*>(smem + Lo.start);
+    uint32_t* nstart = reinterpret_cast<uint32_t*>(smem + Lo.nstart);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + Lo.cnt);  // own arrivals per bag
+    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + Lo.cur);  // placement cursors
+    float4* wr_st = reinterpret_cast<float4*>(smem + Lo.wr_st);
+    uint32_t* wr_id = reinterpret_cast<uint32_t*>(smem + Lo.wr_id);
+    uint32_t* wr_key = reinterpret_cast<uint32_t*>(smem + Lo.wr_key);
     __shared__ uint32_t warp_sums[33];
     __shared__ uint32_t s_err;
     const uint32_t t = threadIdx.x;
     for (uint32_t i = t; i < n; i += blockDim.x) {
-        s_rd[i] = a.st[i];
-        i_rd[i] = a.ids[i];
+        rd_st[i] = a.st[i];
+        rd_id[i] = a.ids[i];
     }
     for (uint32_t c = t; c <= C; c += blockDim.x) start[c] = a.start[c];
-    for (uint32_t c = t; c < C; c += blockDim.x) cnt[c] = 0u;
     if (t == 0) s_err = 0u;
     unsigned long long step = *a.step;
-    __syncthreads();
     for (uint32_t s = 0; s < a.nsteps; ++s, ++step) {
-        // 1. agent pass
-        for (uint32_t i = t; i < n; i += blockDim.x) {
-            const float4 me = s_rd[i];
-            const uint32_t my_id = i_rd[i];
+        // 1. agent pass over the own chunk
+        for (uint32_t c = t; c < C; c += blockDim.x) cnt[c] = 0u;
+        __syncthreads();
+        for (uint32_t i = lo + t; i < hi; i += blockDim.x) {
+            const float4 me = rd_st[i];
+            const uint32_t my_id = rd_id[i];
             Acc<STRICT> acc;
-            gather_small<STRICT, QMODE>(R, s_rd, i_rd, start, me, my_id,
+            gather_small<STRICT, QMODE>(R, rd_st, rd_id, start, me, my_id,
                                         a.self_by_slot ? i : 0xFFFFFFFFu, acc);
             const float4 nx = finish_bird<STRICT>(R, me, my_id, step, acc);
             int64_t idx = bag_index(R, disc(nx.x, R), disc(nx.y, R));
@@ -151,70 +186,106 @@ __global__ void __launch_bounds__(SMALL_THREADS, 1) k_small_steps(SmallArgs a) {
             }
             if (!isfinite(nx.x) || !isfinite(nx.y)) flags |= ERR_NONFINITE;
             if (flags) atomicOr(&s_err, flags);
-            s_wr[i] = nx;
-            i_wr[i] = my_id;
-            key[i] = (uint32_t)idx;
+            wr_st[i - lo] = nx;
+            wr_id[i - lo] = my_id;
+            wr_key[i - lo] = (uint32_t)idx;
             atomicAdd(&cnt[idx], 1u);
         }
+        cl.sync();  // every block's counters are final; no block reads rd_* any more
+        // 2. next offsets (all arrivals) and this chunk's cursors (arrivals
+        //    from lower-ranked blocks come first inside a bag)
+        for (uint32_t c = t; c < C; c += blockDim.x) {
+            uint32_t tot = 0, below = 0;
+            for (uint32_t q = 0; q < SMALL_CTAS; ++q) {
+                const uint32_t v = *cl.map_shared_rank(cnt + c, q);
+                tot += v;
+                below += q < rank ? v : 0u;
+            }
+            cur[c] = below;
+            nstart[c] = tot;
+        }
         __syncthreads();
-        // 2. lazy_update: next offsets, cursors, stable scatter
-        block_scan_small(cnt, nstart, C, warp_sums);
-        for (uint32_t c = t; c < C; c += blockDim.x) cnt[c] = nstart[c];
+        block_scan_small(nstart, nstart, C, warp_sums);
+        for (uint32_t c = t; c < C; c += blockDim.x) cur[c] += nstart[c];
         __syncthreads();
         if (t < 32u) {
             const uint32_t lt = (1u << t) - 1u;
-            for (uint32_t base = 0; base < n; base += 32u) {
-                const uint32_t i = base + t;
-                const bool valid = i < n;
-                const uint32_t k = valid ? key[i] : 0xFFFFFFFFu;
+            for (uint32_t base = 0; base < hi - lo; base += 32u) {
+                const uint32_t j = base + t;
+                const bool valid = j < hi - lo;
+                const uint32_t k = valid ? wr_key[j] : 0xFFFFFFFFu;
                 const uint32_t peers = __match_any_sync(SMALL_FULL, k);
-                const uint32_t rank = __popc(peers & lt);
-                const uint32_t pos = valid ? cnt[k] + rank : 0u;
+                const uint32_t r = __popc(peers & lt);
+                const uint32_t pos = valid ? cur[k] + r : 0u;
                 __syncwarp();
                 if (valid) {
-                    if (rank + 1u == (uint32_t)__popc(peers)) cnt[k] = pos + 1u;
-                    s_rd[pos] = s_wr[i];
-                    i_rd[pos] = i_wr[i];
+                    if (r + 1u == (uint32_t)__popc(peers)) cur[k] = pos + 1u;
+                    wr_key[j] = pos;  // the key becomes the destination slot
                 }
                 __syncwarp();
             }
         }
         __syncthreads();
-        for (uint32_t c = t; c <= C; c += blockDim.x) {
-            start[c] = nstart[c];
-            if (c < C) cnt[c] = 0u;
+        // every block's copy of the next read buffer gets this chunk
+        for (uint32_t x = t; x < (hi - lo) * SMALL_CTAS; x += blockDim.x) {
+            const uint32_t j = x / SMALL_CTAS, q = x % SMALL_CTAS;
+            const uint32_t pos = wr_key[j];
+            *cl.map_shared_rank(rd_st + pos, q) = wr_st[j];
+            *cl.map_shared_rank(rd_id + pos, q) = wr_id[j];
         }
-        __syncthreads();
+        for (uint32_t c = t; c <= C; c += blockDim.x) start[c] = nstart[c];
+        cl.sync();  // every copy of the next read buffer is complete; counters are free
     }
-    for (uint32_t i = t; i < n; i += blockDim.x) {
-        a.st[i] = s_rd[i];
-        a.ids[i] = i_rd[i];
+    if (rank == 0) {
+        for (uint32_t i = t; i < n; i += blockDim.x) {
+            a.st[i] = rd_st[i];
+            a.ids[i] = rd_id[i];
+        }
+        for (uint32_t c = t; c <= C; c += blockDim.x) a.start[c] = start[c];
+        if (t == 0) *a.step = step;
     }
-    for (uint32_t c = t; c <= C; c += blockDim.x) a.start[c] = start[c];
-    if (t == 0) {
-        *a.step = step;
-        if (s_err) atomicOr(a.err, s_err);
-    }
+    __syncthreads();
+    if (t == 0 && s_err) atomicOr(a.err, s_err);
 }
 
 }  // namespace
 
 size_t small_smem_bytes(uint32_t n, uint32_t ncells) {
-    return (size_t)n * (2 * sizeof(float4) + 3 * sizeof(uint32_t)) +
-           (size_t)(3 * (size_t)ncells + 2) * sizeof(uint32_t);
+    return small_layout(n, ncells, (n + SMALL_CTAS - 1) / SMALL_CTAS).bytes;
 }
 
 cudaError_t launch_small_steps(const SmallArgs& a, bool strict, int qmode, cudaStream_t s) {
     if (a.nsteps == 0) return cudaSuccess;
-    if (a.n > SMALL_MAX_BOIDS || a.rep.ncells > SMALL_MAX_CELLS || a.rep.cell_off != 0)
+    if (a.n == 0 || a.n > SMALL_MAX_BOIDS || a.rep.ncells > SMALL_MAX_CELLS || a.rep.cell_off != 0)
         return cudaErrorInvalidValue;
     const size_t bytes = small_smem_bytes(a.n, a.rep.ncells);
     void (*k)(SmallArgs) = strict ? (qmode == 0 ? k_small_steps<true, 0> : k_small_steps<true, 1>)
                                   : (qmode == 0 ? k_small_steps<false, 0> : k_small_steps<false, 1>);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    // the largest layout once per kernel (and device), not per launch
+    static thread_local int opted[4] = {-1, -1, -1, -1};
+    const int ki = (strict ? 2 : 0) + (qmode == 0 ? 0 : 1);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    k<<<1, SMALL_THREADS, bytes, s>>>(a);
-    return cudaGetLastError();
+    if (opted[ki] != dev) {
+        const size_t most = small_smem_bytes(SMALL_MAX_BOIDS, SMALL_MAX_CELLS);
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+        if (e != cudaSuccess) return e;
+        opted[ki] = dev;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(SMALL_CTAS, 1, 1);
+    cfg.blockDim = dim3(SMALL_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = SMALL_CTAS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, a);
 }
 
 }  // namespace kb

@@ -278,8 +278,9 @@ class Field2D:
         return counts[: len(q)], dig[: len(q)]
 
     def set_step_options(self, mode=0, tile_tx: int = 0, tile_ty: int = 0) -> None:
-        """Step path: 0 separate kernels (default; fields of at most 256 boids
-        run whole steps in one block), 3 separate kernels whatever the size, 2 tiled split,
+        """Step path: 0 separate kernels (default; runs of steps on fields of
+        at most 1536 boids take one thread-block cluster), 3 separate kernels
+        whatever the size, 2 tiled split,
         1 persistent (True/False mean 2/0); tile shape in bags (0 = automatic)."""
         mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)
         L.call("kb_field_set_step_options", self._h, C.c_int32(mode), C.c_int32(tile_tx),

@@ -1,5 +1,6 @@
-"""Whole steps of a small field in one thread block, the default step path for
-plain fields of at most 256 boids and 4096 bags (kb_small.cu): bit-exact
+"""Whole steps of a small field in one thread-block cluster, the default step
+path for runs of steps on plain fields of at most 1536 boids and 4096 bags
+(kb_small.cu): bit-exact
 against the oracle in strict arithmetic, and the same bits as the separate
 kernels (step mode 3) in fast arithmetic."""
 import ctypes as C
@@ -23,7 +24,10 @@ CASES = {
     "true_torus": (80.0, 80.0, FLOCK_D, True, kg.KB_CELL_WRAP_TORUS, 160, 10.0),
     # dense: about 40 candidates per boid
     "full": (40.0, 40.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 256, 10.0),
-    # many bags: 4096 (64 x 64, the largest the block takes)
+    # the 1,000-boid Flockers case and the largest field the cluster takes
+    "c1k": (200.0, 200.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 1000, 10.0),
+    "max": (247.0, 247.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 1536, 10.0),
+    # many bags: 4096 (64 x 64, the most the cluster takes)
     "wide": (float(np.float32(63.0) * np.float32(FLOCK_D)), float(np.float32(63.0) * np.float32(FLOCK_D)),
              FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 250, 10.0),
 }
@@ -81,7 +85,7 @@ def test_small_path_with_repeated_ids(gpu):
     assert np.array_equal(ids, oids) and same_bits(st, ost)
 
 
-@pytest.mark.parametrize("case", ["c1", "full"])
+@pytest.mark.parametrize("case", ["c1", "full", "c1k", "max"])
 def test_small_path_equals_separate_kernels(gpu, case):
     a, _ = fields(case, seed=8)
     b, _ = fields(case, seed=8)
