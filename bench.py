@@ -370,12 +370,13 @@ def run_ours(args, wl):
         one_step(step_no)
         step_no += 1
     f.synchronize()
-    if args.profile:  # a short plain run for a profiler: warm-up, then `steps` launches
+    if args.profile:  # a short plain run for a profiler: warm-up, then `steps` calls
         if args.phase_clocks:
             L.call("kb_field_phase_clocks", f.handle, C.c_int32(1), None)
+        k = max(1, args.profile_call_steps)  # steps per kb_flock_step call
         for _ in range(args.steps):
-            one_step(step_no)
-            step_no += 1
+            L.call("kb_flock_step", f.handle, C.byref(pc), C.c_uint64(step_no), C.c_uint32(k))
+            step_no += k
         f.synchronize()
         out = {"profile_run": True, "steps": args.steps, "stats": f.step_stats()}
         if args.phase_clocks:
@@ -560,6 +561,9 @@ def main():
     ap.add_argument("--mode", type=int, default=0,
                     help="step path: 2 tiled split (default), 1 persistent, 0 separate kernels")
     ap.add_argument("--profile", action="store_true", help="short plain run for ncu, no timing")
+    ap.add_argument("--profile-call-steps", type=int, default=1,
+                    help="with --profile: steps per kb_flock_step call (runs of 2 or more take "
+                         "the cluster path on fields of at most 4096 boids)")
     ap.add_argument("--sweep-reps", type=int, default=512)
     ap.add_argument("--sweep-steps", type=int, default=500)
     ap.add_argument("--serve-seconds", type=float, default=60.0)

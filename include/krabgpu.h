@@ -194,7 +194,7 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
 /* Step implementation options (no reference counterpart; tuning only).
  * mode (the `fused` argument): 0 (default) the separate force / scan / rebin
  * kernels (a plain field replays runs of 4 steps or more from CUDA graphs),
- * except that a call of 2 steps or more on a plain field of at most 1536
+ * except that a call of 2 steps or more on a plain field of at most 4096
  * boids and 4096 bags runs whole steps in one 8-block thread-block cluster
  * (shared memory, up to 1000 steps per launch);
  * 3 the separate kernels whatever the field's size;

@@ -80,10 +80,10 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
 // written back.
 constexpr int SMALL_THREADS = 1024;
 constexpr uint32_t SMALL_CTAS = 8;  // a portable cluster size
-// Measured on GB300 (uniform flocks, 400-step calls): 7.0 / 9.2 / 11.6 /
-// 13.4 / 15.1 us per step at 16 / 256 / 1000 / 1500 / 2048 boids, against
-// 13.6 / 12.1 / 14.0 / 14.7 / 14.9 us for the separate kernels.
-constexpr uint32_t SMALL_MAX_BOIDS = 1536;
+// Measured on GB300 (uniform flocks, 400-step calls): 4.8 / 7.0 / 9.3 / 13.9 us
+// per step at 16 / 1000 / 2048 / 4096 boids, against 13.5 / 14.2 / 14.7 /
+// 15.4 us for the separate kernels; the bound is the shared memory.
+constexpr uint32_t SMALL_MAX_BOIDS = 4096;
 constexpr uint32_t SMALL_MAX_CELLS = 4096;
 struct SmallArgs {
     Rep rep;

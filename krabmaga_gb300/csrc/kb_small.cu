@@ -8,17 +8,18 @@
 // bag offsets in shared memory and owns one contiguous chunk of the boids:
 //   1. agent pass: Bird::step for the chunk's boids against the local copy
 //      (the same candidate order, accumulator and finish as k_flock_force);
-//      next states, ids and bag keys go to a local write list, arrivals are
-//      counted per bag in the block's own counters;
+//      next states and ids go to a local write list, and each bag key is
+//      written into every block's copy of the list of keys (distributed
+//      shared memory);
 //   -- cluster barrier --
-//   2. lazy_update: every block sums the counters of all blocks through
-//      distributed shared memory, scans them into the next bag offsets, and
-//      places its own chunk: position = offset of the bag + arrivals from
-//      lower-ranked blocks (earlier in list order) + rank inside the chunk
-//      (one warp walks the chunk in list order, __match_any_sync ranks equal
-//      keys, a per-bag cursor carries the rank), which is the reference's
-//      insertion order inside a bag; each record is written into every
-//      block's copy of the next read buffer;
+//   2. lazy_update: every block counts all keys in its own shared memory,
+//      scans the counts into the next bag offsets, and places its own chunk:
+//      position = offset of the bag + arrivals from lower-ranked blocks
+//      (earlier in list order) + rank inside the chunk (one warp walks the
+//      chunk in list order, __match_any_sync ranks equal keys, a per-bag
+//      cursor carries the rank), which is the reference's insertion order
+//      inside a bag; each record is written into every block's copy of the
+//      next read buffer;
 //   -- cluster barrier --
 // and block 0 writes the final read buffer, offsets and step counter back.
 // No bound on how far a boid moves is needed.
@@ -36,17 +37,61 @@ namespace {
 
 constexpr uint32_t SMALL_FULL = 0xFFFFFFFFu;
 
+// One candidate of the relaxed query in list order: self is skipped (by
+// slot when ids are unique, else by id).
+template <bool STRICT>
+__device__ __forceinline__ void take_small(const Rep& R, const uint32_t* ids, uint32_t p, float4 o,
+                                           float4 me, uint32_t my_id, uint32_t my_slot,
+                                           Acc<STRICT>& acc) {
+    const bool self = my_slot != 0xFFFFFFFFu ? p == my_slot : ids[p] == my_id;
+    if (!self) acc.add(R, me.x, me.y, o);
+}
+
 // Bird::step's candidate sums for `me` against a read buffer in shared
 // memory: the query's cells x-outer / y-inner (t_transform wraps the range
 // where the field does), each bag in insertion order, the exact query's
 // corner rule (check_circle) for QMODE 1.  Self is the slot my_slot when ids
-// are unique, else every candidate with the boid's id.
+// are unique, else every candidate with the boid's id.  The relaxed query of
+// a clamped one-bag ring (the common case) walks its three column runs as one
+// flat list, two candidates per iteration, so the loads and reciprocals of
+// the next candidate overlap the sums of the current one (the sums are still
+// taken in list order: the same bits).
 template <bool STRICT, int QMODE>
 __device__ __forceinline__ void gather_small(const Rep& R, const float4* st, const uint32_t* ids,
                                              const uint32_t* start, float4 me, uint32_t my_id,
                                              uint32_t my_slot, Acc<STRICT>& acc) {
     int mi, Mi, mj, Mj;
     if (!cell_range(R, me.x, me.y, R.dd, &mi, &Mi, &mj, &Mj)) return;
+    if (QMODE == 0 && R.toroidal && !R.cell_wrap && Mi - mi < 3) {
+        if (mj > Mj) return;
+        uint32_t s[3], e[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            s[k] = e[k] = 0u;
+            if (mi + k <= Mi) {
+                const uint32_t colbase = (uint32_t)(mi + k) * (uint32_t)R.dh;
+                s[k] = start[colbase + (uint32_t)mj];
+                e[k] = start[colbase + (uint32_t)Mj + 1u];
+            }
+        }
+        const uint32_t P1 = e[0] - s[0], P2 = P1 + (e[1] - s[1]), T = P2 + (e[2] - s[2]);
+        const uint32_t d1 = s[1] - P1, d2 = s[2] - P2;  // position = f + d (mod 2^32)
+        acc.vec += T;
+        uint32_t f = 0;
+        for (; f + 1u < T; f += 2u) {
+            const uint32_t g = f + 1u;
+            const uint32_t p0 = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
+            const uint32_t p1 = g < P1 ? s[0] + g : (g < P2 ? g + d1 : g + d2);
+            const float4 o0 = st[p0], o1 = st[p1];
+            take_small(R, ids, p0, o0, me, my_id, my_slot, acc);
+            take_small(R, ids, p1, o1, me, my_id, my_slot, acc);
+        }
+        if (f < T) {
+            const uint32_t p0 = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
+            take_small(R, ids, p0, st[p0], me, my_id, my_slot, acc);
+        }
+        return;
+    }
     for (int ci = mi; ci <= Mi; ++ci) {
         const int bx = t_transform(ci, R.max_x);
         const uint32_t colbase = (uint32_t)bx * (uint32_t)R.dh;
@@ -120,7 +165,7 @@ __device__ __forceinline__ void block_scan_small(const uint32_t* in, uint32_t* o
 
 // Shared-memory layout (byte offsets), the same in every block of the cluster.
 struct SmallLayout {
-    uint32_t rd_st, wr_st, rd_id, wr_id, wr_key, start, nstart, cnt, cur, bytes;
+    uint32_t rd_st, wr_st, rd_id, wr_id, wr_key, keys, start, nstart, cnt, cur, bytes;
 };
 __host__ __device__ inline SmallLayout small_layout(uint32_t n, uint32_t ncells, uint32_t chunk) {
     SmallLayout L{};
@@ -130,6 +175,7 @@ __host__ __device__ inline SmallLayout small_layout(uint32_t n, uint32_t ncells,
     L.rd_id = o;  o += n * 4u;
     L.wr_id = o;  o += chunk * 4u;
     L.wr_key = o; o += chunk * 4u;
+    L.keys = o;   o += n * 4u;
     L.start = o;  o += (ncells + 1u) * 4u;
     L.nstart = o; o += (ncells + 1u) * 4u;
     L.cnt = o;    o += ncells * 4u;
@@ -152,8 +198,9 @@ __global__ void __launch_bounds__(SMALL_THREADS, 1) k_small_steps(SmallArgs a) {
     uint32_t* rd_id = reinterpret_cast<uint32_t*>(smem + Lo.rd_id);
     uint32_t* start = reinterpret_cast<uint32_t*>(smem + Lo.start);
     uint32_t* nstart = reinterpret_cast<uint32_t*>(smem + Lo.nstart);
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + Lo.cnt);  // own arrivals per bag
-    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + Lo.cur);  // placement cursors
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + Lo.cnt);  // arrivals per bag
+    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + Lo.cur);  // lower-ranked arrivals, cursors
+    uint32_t* keys = reinterpret_cast<uint32_t*>(smem + Lo.keys);  // every boid's next bag
     float4* wr_st = reinterpret_cast<float4*>(smem + Lo.wr_st);
     uint32_t* wr_id = reinterpret_cast<uint32_t*>(smem + Lo.wr_id);
     uint32_t* wr_key = reinterpret_cast<uint32_t*>(smem + Lo.wr_key);
@@ -169,8 +216,10 @@ __global__ void __launch_bounds__(SMALL_THREADS, 1) k_small_steps(SmallArgs a) {
     unsigned long long step = *a.step;
     for (uint32_t s = 0; s < a.nsteps; ++s, ++step) {
         // 1. agent pass over the own chunk
-        for (uint32_t c = t; c < C; c += blockDim.x) cnt[c] = 0u;
-        __syncthreads();
+        for (uint32_t c = t; c < C; c += blockDim.x) {
+            cnt[c] = 0u;
+            cur[c] = 0u;
+        }
         for (uint32_t i = lo + t; i < hi; i += blockDim.x) {
             const float4 me = rd_st[i];
             const uint32_t my_id = rd_id[i];
@@ -189,23 +238,18 @@ __global__ void __launch_bounds__(SMALL_THREADS, 1) k_small_steps(SmallArgs a) {
             wr_st[i - lo] = nx;
             wr_id[i - lo] = my_id;
             wr_key[i - lo] = (uint32_t)idx;
-            atomicAdd(&cnt[idx], 1u);
+#pragma unroll
+            for (uint32_t q = 0; q < SMALL_CTAS; ++q) *cl.map_shared_rank(keys + i, q) = (uint32_t)idx;
         }
-        cl.sync();  // every block's counters are final; no block reads rd_* any more
+        cl.sync();  // every copy of the keys is complete; no block reads rd_* any more
         // 2. next offsets (all arrivals) and this chunk's cursors (arrivals
-        //    from lower-ranked blocks come first inside a bag)
-        for (uint32_t c = t; c < C; c += blockDim.x) {
-            uint32_t tot = 0, below = 0;
-            for (uint32_t q = 0; q < SMALL_CTAS; ++q) {
-                const uint32_t v = *cl.map_shared_rank(cnt + c, q);
-                tot += v;
-                below += q < rank ? v : 0u;
-            }
-            cur[c] = below;
-            nstart[c] = tot;
+        //    from lower-ranked blocks, earlier in the list, come first in a bag)
+        for (uint32_t i = t; i < n; i += blockDim.x) {
+            atomicAdd(&cnt[keys[i]], 1u);
+            if (i < lo) atomicAdd(&cur[keys[i]], 1u);
         }
         __syncthreads();
-        block_scan_small(nstart, nstart, C, warp_sums);
+        block_scan_small(cnt, nstart, C, warp_sums);
         for (uint32_t c = t; c < C; c += blockDim.x) cur[c] += nstart[c];
         __syncthreads();
         if (t < 32u) {

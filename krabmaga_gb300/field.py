@@ -279,7 +279,7 @@ class Field2D:
 
     def set_step_options(self, mode=0, tile_tx: int = 0, tile_ty: int = 0) -> None:
         """Step path: 0 separate kernels (default; runs of steps on fields of
-        at most 1536 boids take one thread-block cluster), 3 separate kernels
+        at most 4096 boids take one thread-block cluster), 3 separate kernels
         whatever the size, 2 tiled split,
         1 persistent (True/False mean 2/0); tile shape in bags (0 = automatic)."""
         mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else int(mode)

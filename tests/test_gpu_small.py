@@ -1,5 +1,5 @@
 """Whole steps of a small field in one thread-block cluster, the default step
-path for runs of steps on plain fields of at most 1536 boids and 4096 bags
+path for runs of steps on plain fields of at most 4096 boids and 4096 bags
 (kb_small.cu): bit-exact
 against the oracle in strict arithmetic, and the same bits as the separate
 kernels (step mode 3) in fast arithmetic."""
@@ -26,7 +26,7 @@ CASES = {
     "full": (40.0, 40.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 256, 10.0),
     # the 1,000-boid Flockers case and the largest field the cluster takes
     "c1k": (200.0, 200.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 1000, 10.0),
-    "max": (247.0, 247.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 1536, 10.0),
+    "max": (405.0, 405.0, FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 4096, 10.0),
     # many bags: 4096 (64 x 64, the most the cluster takes)
     "wide": (float(np.float32(63.0) * np.float32(FLOCK_D)), float(np.float32(63.0) * np.float32(FLOCK_D)),
              FLOCK_D, True, kg.KB_CELL_WRAP_CLAMP, 250, 10.0),
