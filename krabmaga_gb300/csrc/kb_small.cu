@@ -214,6 +214,10 @@ __global__ void __launch_bounds__(SMALL_THREADS, 1) k_small_steps(SmallArgs a) {
     for (uint32_t c = t; c <= C; c += blockDim.x) start[c] = a.start[c];
     if (t == 0) s_err = 0u;
     unsigned long long step = *a.step;
+    // every block of the cluster is running (its shared memory may be written
+    // through the cluster) and has its whole copy loaded before any thread
+    // reads a neighbour
+    cl.sync();
     for (uint32_t s = 0; s < a.nsteps; ++s, ++step) {
         // 1. agent pass over the own chunk
         for (uint32_t c = t; c < C; c += blockDim.x) {
