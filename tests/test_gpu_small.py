@@ -121,3 +121,38 @@ def test_small_path_reports_positions_outside_the_matrix(gpu):
     with pytest.raises(kg.KbError):
         f.synchronize()
     assert f.device_flags(clear=True) & 0x1  # KB_FLAG_KEY_RANGE
+
+
+def test_small_path_random_fields_equal_separate_kernels(gpu):
+    # seeded random small fields (size, density, bag size, torus options, query kind): the
+    # cluster path and the separate kernels give the same bits over a run of steps
+    rng = np.random.default_rng(2024)
+    ran = 0
+    for case in range(24):
+        n = int(rng.choice([1, 2, 31, 200, 999, 2500, 4096]))
+        dens = float(rng.uniform(0.01, 0.2))
+        side = float(np.float32(max(20.0, np.sqrt(n / dens))))
+        d = float(np.float32(rng.choice([10.0 / 1.5, 5.0, 10.0])))
+        tor = bool(rng.integers(0, 2))
+        wrap = kg.KB_CELL_WRAP_TORUS if (tor and rng.integers(0, 2)) else kg.KB_CELL_WRAP_CLAMP
+        kind = int(rng.integers(0, 2))
+        cells = (int(np.ceil(np.float32(side) / np.float32(d))) + 1) ** 2
+        ids, xy, dxy = kg.gen_uniform(n, side, side, 100 + case, 1.0)
+        p = kg.FlockParams(seed=case, query_mode=kind, arith=kg.KB_ARITH_FAST,
+                           jump=float(rng.uniform(0.3, 1.5)))
+        out = []
+        for mode in (0, 3):
+            f = kg.Field2D(side, side, d, tor, cell_wrap=wrap, capacity_hint=n)
+            f.set_step_options(mode)
+            f.set_locations(ids, xy, dxy)
+            f.lazy_update()
+            if mode == 0 and cells <= 4096:
+                assert f.step_path() == kg.KB_PATH_SMALL, (case, n, cells)
+                ran += 1
+            step(f, p, 0, 12)
+            out.append(f.get_state())
+            assert f.device_flags() == 0, case
+            f.close()
+        (ia, sa), (ib, sb) = out
+        assert np.array_equal(ia, ib) and same_bits(sa, sb), (case, n, side, d, tor, wrap, kind)
+    assert ran >= 12
