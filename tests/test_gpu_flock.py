@@ -296,6 +296,58 @@ def test_1m_flock_full_size_one_step(gpu):
     assert f.device_flags() == 0
 
 
+def test_1m_flock_ten_strict_steps_match_oracle(gpu):
+    """The C2 workload (1,048,576 boids) for ten strict steps, graph-replayed on
+    the separate kernels: the whole state equals the oracle's after them."""
+    n = 1 << 20
+    side = float(np.float32(np.sqrt(n / 0.025)))
+    ids0, xy0, dxy0 = kg.gen_uniform(n, side, side, 7, 1.0)
+    f = gpu_field(side, FLOCK_D, ids0, xy0, dxy0)
+    o = oracle_field(side, FLOCK_D, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=7, arith=kg.KB_ARITH_STRICT)
+    step(f, p, 0, 10)
+    o.flock_run(oracle.params_from(p), 0, 10)
+    ids, st = f.get_state()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+    assert f.device_flags() == 0
+
+
+def test_1m_flock_invariants_after_300_fast_steps(gpu):
+    """Size-independent properties of the C2 workload after 300 fast steps
+    (the benchmark's arithmetic): every id once, every heading of length jump,
+    every position on the torus, the read buffer in canonical bag order with
+    each boid in the bag of its position, and neighbour counts and digests of
+    a sample equal to the oracle's on the same read buffer."""
+    n = 1 << 20
+    side = np.float32(np.sqrt(n / 0.025))
+    ids0, xy0, dxy0 = kg.gen_uniform(n, float(side), float(side), 7, 1.0)
+    f = gpu_field(float(side), FLOCK_D, ids0, xy0, dxy0)
+    p = kg.FlockParams(seed=7, arith=kg.KB_ARITH_FAST)
+    step(f, p, 0, 300)
+    assert f.device_flags() == 0
+    ids, st = f.get_state()
+    assert np.array_equal(np.sort(ids), np.arange(n, dtype=np.uint32))
+    speed = np.hypot(st[:, 2].astype(np.float64), st[:, 3].astype(np.float64))
+    assert np.all(np.abs(speed - 0.7) < 1e-5)
+    assert np.all((st[:, :2] >= 0) & (st[:, :2] <= side))
+    d = np.float32(FLOCK_D)
+    cx = np.floor(st[:, 0] / d).astype(np.int64)
+    cy = np.floor(st[:, 1] / d).astype(np.int64)
+    dh = int(np.ceil(side / d)) + 1
+    bag = cx * dh + cy
+    assert np.all(np.diff(bag) >= 0)  # bags ascending in read order
+    o = oracle.OracleField(float(side), float(side), FLOCK_D, True)
+    o.set_many(ids, st[:, :2], st[:, 2:])
+    o.lazy_update()
+    oids, ost, _ = o.iter(1)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)  # same canonical order
+    q = st[::53, :2]
+    gc, gd = f.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, q)
+    oc, od = o.neighbor_digest(kg.KB_QUERY_RELAX, 10.0, q)
+    assert np.array_equal(gc, oc) and np.array_equal(gd, od)
+
+
 def test_4m_clustered_quarter_size_digests(gpu):
     """Clustered stress (256 Gaussian clusters, sigma 40) at a quarter of the
     4,194,304-boid size: after 3 strict steps the state equals the oracle's
