@@ -292,3 +292,158 @@ def evolutionary_search(init_population: Callable[[], List],
         crossover(population)
         population = [mutation(ind) for ind in population]
     return rows
+
+
+# ------------------------------------------------------------ bayesian_search!
+class GaussianProcess:
+    """Gaussian-process regression, the surrogate of bayesian_search!
+    (src/explore/bayesian.rs:135, 214, through the friedrich crate, which is
+    not part of the reference tree).  Restated from the standard equations:
+    a constant prior mean (the mean of the outputs), a Gaussian kernel
+    k(a, b) = s^2 exp(-|a - b|^2 / (2 l^2)) with s^2 the variance of the
+    outputs and l the median distance between the inputs, and a small noise
+    term on the diagonal.  The kernel is refitted when samples are added."""
+
+    def __init__(self, x, y, noise: float = 1e-6):
+        self.noise = float(noise)
+        self.x = np.asarray(x, np.float64).reshape(len(y), -1)
+        self.y = np.asarray(y, np.float64).reshape(-1)
+        self._fit()
+
+    def _fit(self) -> None:
+        x, y = self.x, self.y
+        self.mean = float(y.mean())
+        self.s2 = float(y.var()) if y.var() > 0 else 1.0
+        d = np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))
+        off = d[np.triu_indices(len(x), 1)]
+        self.l = float(np.median(off)) if off.size and np.median(off) > 0 else 1.0
+        k = self._k(x, x) + self.noise * self.s2 * np.eye(len(x))
+        self.chol = np.linalg.cholesky(k)
+        self.alpha = np.linalg.solve(self.chol.T, np.linalg.solve(self.chol, y - self.mean))
+
+    def _k(self, a, b):
+        d2 = ((a[:, None, :] - b[None, :, :]) ** 2).sum(-1)
+        return self.s2 * np.exp(-d2 / (2.0 * self.l * self.l))
+
+    def add_samples(self, x, y) -> None:
+        """GaussianProcess::add_samples (bayesian.rs:159)."""
+        self.x = np.vstack([self.x, np.asarray(x, np.float64).reshape(len(y), -1)])
+        self.y = np.concatenate([self.y, np.asarray(y, np.float64).reshape(-1)])
+        self._fit()
+
+    def predict(self, x):
+        """Posterior mean at one point (a 1-d array) or at every row of x."""
+        q = np.asarray(x, np.float64)
+        one = q.ndim == 1
+        q = q.reshape(-1, self.x.shape[1])
+        m = self.mean + self._k(q, self.x) @ self.alpha
+        return float(m[0]) if one else m
+
+    def predict_variance(self, x):
+        """Posterior variance at one point or at every row of x."""
+        q = np.asarray(x, np.float64)
+        one = q.ndim == 1
+        q = q.reshape(-1, self.x.shape[1])
+        v = np.linalg.solve(self.chol, self._k(self.x, q))
+        var = np.maximum(self.s2 - (v * v).sum(0), 0.0)
+        return float(var[0]) if one else var
+
+
+def generate_samples(batch_size: int, scale: float, num_of_params: int,
+                     rng: Optional[np.random.Generator] = None) -> np.ndarray:
+    """bayesian.rs:246-258: batch_size points, each coordinate uniform in
+    [-scale, scale] (a seeded generator instead of the reference's rand::rng)."""
+    rng = rng if rng is not None else np.random.default_rng()
+    return rng.uniform(-1.0, 1.0, (int(batch_size), int(num_of_params))) * float(scale)
+
+
+def expected_improvement(x_init, x, gp: GaussianProcess):
+    """bayesian.rs:296-329: (mu - best) Phi(z) + sigma phi(z), z = (mu - best) /
+    sigma, best the largest posterior mean over the evaluated points; 0 where
+    sigma is 0.  x may be one point or a matrix of points (one result each)."""
+    import math
+    q = np.asarray(x, np.float64)
+    one = q.ndim == 1
+    q = q.reshape(-1, gp.x.shape[1])
+    mu = np.atleast_1d(gp.predict(q))
+    sigma = np.sqrt(np.atleast_1d(gp.predict_variance(q)))
+    best = float(np.max(np.atleast_1d(gp.predict(np.asarray(x_init, np.float64)))))
+    ei = np.zeros(len(q))
+    ok = sigma > 0
+    z = (mu[ok] - best) / sigma[ok]
+    cdf = 0.5 * (1.0 + np.vectorize(math.erf)(z / math.sqrt(2.0)))
+    pdf = np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    ei[ok] = (mu[ok] - best) * cdf + sigma[ok] * pdf
+    return float(ei[0]) if one else ei
+
+
+def acquisition_function(x_init, x_samples, gp: GaussianProcess) -> np.ndarray:
+    """bayesian.rs:268-289: the sample with the highest expected improvement
+    (the first one among equals)."""
+    xs = np.asarray(x_samples, np.float64)
+    return xs[int(np.argmax(expected_improvement(x_init, xs, gp)))].copy()
+
+
+def bayesian_search(init_parameters: Callable[[], Sequence[Sequence[float]]],
+                    objective_function: Callable[[np.ndarray], float], gen_params,
+                    n_iter: int, batch_size: Optional[int] = None,
+                    scale: Optional[float] = None, seed: int = 0,
+                    log: Optional[Callable[[str], None]] = None) -> Tuple[np.ndarray, float]:
+    """bayesian_search! (src/explore/bayesian.rs:104-244): maximise
+    objective_function.  The first pattern passes gen_params, a function of
+    the evaluated points returning candidate points; the second passes the
+    number of parameters and then batch_size and scale, and the candidates
+    are generate_samples(batch_size, scale, num_of_params).  Every iteration
+    evaluates the candidate with the highest expected improvement and adds
+    it to the Gaussian process.  Returns (best point, best value).  With
+    flock_objective the evaluations are flock runs on the device."""
+    rng = np.random.default_rng(seed)
+    x_init = [np.asarray(x, np.float64) for x in init_parameters()]
+    y_init = [float(objective_function(x)) for x in x_init]
+    k = int(np.argmax(y_init))
+    x_max, y_max = x_init[k].copy(), y_init[k]
+    gp = GaussianProcess(np.vstack(x_init), y_init)
+    for i in range(int(n_iter)):
+        if callable(gen_params):
+            samples = np.asarray(gen_params(x_init), np.float64)
+        else:
+            samples = generate_samples(batch_size, scale, int(gen_params), rng)
+        x_next = acquisition_function(np.vstack(x_init), samples, gp)
+        y_next = float(objective_function(x_next))
+        if log is not None:
+            log(f"iteration {i}: point {x_next.tolist()}, f(x) = {y_next}, "
+                f"predicted {gp.predict(x_next)}")
+        gp.add_samples(x_next[None, :], [y_next])
+        x_init.append(x_next)
+        if y_next > y_max:
+            x_max, y_max = x_next.copy(), y_next
+    return x_max, y_max
+
+
+def flock_objective(base: FlockerConfig, names: Sequence[str],
+                    value_of: Callable[[List[dict]], float], step: int, reps: int = 1,
+                    init_seed: int = 0, device: int = 0) -> Callable[[np.ndarray], float]:
+    """An objective for bayesian_search whose evaluation is a flock run on
+    the device: point x sets the configuration fields names[i] = x[i]; the
+    point's reps runs go as one batch for step steps, and value_of receives
+    their observables (the OUTPUTS of explore).  Run k of the whole search
+    starts from Philox(init_seed + k)."""
+    counter = [0]
+
+    def f(x) -> float:
+        cfg = base
+        for nm, v in zip(names, np.asarray(x, np.float64).tolist()):
+            cfg = _apply(cfg, nm, float(v))
+        reps_list = []
+        for _ in range(int(reps)):
+            reps_list.append(_replica(cfg, init_seed + counter[0]))
+            counter[0] += 1
+        b = Batch(reps_list, device=device)
+        try:
+            b.step(0, int(step), 1, 100)
+            mom = b.moments()
+        finally:
+            b.close()
+        return float(value_of([_observables(mom[r]) for r in range(int(reps))]))
+
+    return f

@@ -81,3 +81,46 @@ def test_csv_layout(tmp_path):
     # f32 to_string() (2000 has none)
     assert got[1] == ["0", "0", "1.0", "300", "0.25", "0.5", "2000"]
     assert got[2][4] == "0.125"
+
+
+# bayesian_search! (src/explore/bayesian.rs) on the host: the reference's own
+# doc example, x^2 + y^2 minimised by maximising its negative, both patterns
+
+
+def _init():
+    return [[-2.0, -2.0], [8.0, 1.0], [-1.0, 5.0], [4.0, -2.0]]
+
+
+def _objective_square(x):
+    return -1.0 * (x[0] ** 2 + x[1] ** 2)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_bayesian_search_optional_pattern_finds_the_minimum(seed):
+    ex = importlib.import_module("krabmaga_gb300.explore")
+    x, y = ex.bayesian_search(_init, _objective_square, 2, 20, batch_size=500, scale=10.0,
+                              seed=seed)
+    assert abs(x[0]) < 1.0 and abs(x[1]) < 1.0
+    assert y == _objective_square(x)
+
+
+def test_bayesian_search_main_pattern_and_its_parts():
+    import numpy as np
+    ex = importlib.import_module("krabmaga_gb300.explore")
+
+    def gen(xs):
+        return np.random.default_rng(len(xs)).uniform(-10.0, 10.0, (500, 2))
+
+    x, y = ex.bayesian_search(_init, _objective_square, gen, 20)
+    assert abs(x[0]) < 1.0 and abs(x[1]) < 1.0
+    # the surrogate interpolates its samples; expected improvement is 0 where
+    # the variance is 0 and positive elsewhere; the acquisition takes the max
+    pts = np.array(_init(), float)
+    vals = [_objective_square(p) for p in pts]
+    gp = ex.GaussianProcess(pts, vals)
+    assert np.allclose(gp.predict(pts), vals, atol=1e-3 * max(abs(v) for v in vals))
+    assert gp.predict_variance(pts).max() < 1e-3 * np.var(vals)
+    cand = ex.generate_samples(50, 10.0, 2, np.random.default_rng(0))
+    ei = ex.expected_improvement(pts, cand, gp)
+    assert (ei >= 0).all() and ei.max() > 0
+    assert np.array_equal(ex.acquisition_function(pts, cand, gp), cand[int(np.argmax(ei))])

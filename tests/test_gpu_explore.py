@@ -154,3 +154,21 @@ def test_evolutionary_search_rows_equal_single_runs(gpu):
     rows2 = kg.evolutionary_search(init_population, make_config, fitness, selection, mutation,
                                    crossover, lambda a, b: a > b, -1.0, 5, step=5, reps=1)
     assert {r["generation"] for r in rows2} == {1}
+
+
+def test_bayesian_search_over_flock_runs(gpu):
+    # the objective is a flock run on the device: the order parameter of two
+    # runs of 40 steps as a function of the consistency weight
+    import numpy as np
+    ex = importlib.import_module("krabmaga_gb300.explore")
+    base = kg.FlockerConfig(initial_flockers=400, dim=130.0)
+    order = lambda obs: float(np.mean([o["order"] for o in obs]))
+    f = ex.flock_objective(base, ["consistency"], order, step=40, reps=2, init_seed=3)
+    g = ex.flock_objective(base, ["consistency"], order, step=40, reps=2, init_seed=3)
+    assert f(np.array([1.0])) == g(np.array([1.0]))  # the same runs, the same value
+
+    def gen(xs):
+        return np.random.default_rng(len(xs)).uniform(0.0, 3.0, (64, 1))
+
+    x, y = ex.bayesian_search(lambda: [[0.1], [2.0]], f, gen, 4)
+    assert 0.0 <= x[0] <= 3.0 and 0.0 <= y <= 1.0
