@@ -12,7 +12,8 @@ from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
 from .explore import (ExploreMode, FlockerConfig, bayesian_search, build_configurations,
-                      evolutionary_search, explore, flock_objective, random_search, write_csv)
+                      evolutionary_search, explore, flock_objective, gen_param, load_csv,
+                      random_search, write_csv)
 from .model import (Agent, AgentImpl, FlockParams, Flocker, Schedule, State, gen_clustered,
                     gen_uniform, simulate, simulate_old)
 
@@ -25,7 +26,8 @@ __all__ = [
     "KB_PATH_SEPARATE", "KB_PATH_FUSED", "KB_PATH_TILED", "KB_PATH_SMALL", "KB_PATH_DENSE",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
     "ExploreMode", "FlockerConfig", "build_configurations", "explore", "random_search",
-    "evolutionary_search", "write_csv", "bayesian_search", "flock_objective",
+    "evolutionary_search", "write_csv", "bayesian_search", "flock_objective", "gen_param",
+    "load_csv",
 ]
 
 

@@ -447,3 +447,36 @@ def flock_objective(base: FlockerConfig, names: Sequence[str],
         return float(value_of([_observables(mom[r]) for r in range(int(reps))]))
 
     return f
+
+
+# ------------------------------------------------------------ sweep inputs
+def gen_param(kind, minimum, maximum, n: int = 1,
+              rng: Optional[np.random.Generator] = None) -> list:
+    """gen_param! (src/lib.rs:1823-1852): n values uniform over [min, max) of
+    type kind (int or float), for parameter sweeps.  As the macro does, a
+    reversed range is swapped and an empty one widened by 1; n = 0 gives no
+    value (the macro takes its argument n, not the adjusted count).  A seeded
+    generator stands in for rand::rng()."""
+    rng = rng if rng is not None else np.random.default_rng()
+    lo, hi = kind(minimum), kind(maximum)
+    if lo > hi:
+        lo, hi = hi, lo
+    elif lo == hi:
+        hi = hi + kind(1)
+    if kind is int:
+        return [int(v) for v in rng.integers(lo, hi, int(n))]
+    return [kind(v) for v in rng.uniform(lo, hi, int(n))]
+
+
+def load_csv(path: str, *fields: Tuple[str, type]) -> tuple:
+    """load_csv! (src/lib.rs:1854-1890): the columns of a CSV file with a
+    header row, one list per (name, type) field taken by position, each value
+    parsed as its type."""
+    cols = [[] for _ in fields]
+    with open(path, newline="") as fh:
+        rows = csv.reader(fh)
+        next(rows, None)  # the header (csv::Reader reads one by default)
+        for rec in rows:
+            for i, (_, kind) in enumerate(fields):
+                cols[i].append(kind(rec[i]))
+    return tuple(cols)

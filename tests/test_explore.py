@@ -124,3 +124,24 @@ def test_bayesian_search_main_pattern_and_its_parts():
     ei = ex.expected_improvement(pts, cand, gp)
     assert (ei >= 0).all() and ei.max() > 0
     assert np.array_equal(ex.acquisition_function(pts, cand, gp), cand[int(np.argmax(ei))])
+
+
+def test_gen_param_as_the_macro():
+    import numpy as np
+    ex = importlib.import_module("krabmaga_gb300.explore")
+    rng = np.random.default_rng(1)
+    u = ex.gen_param(int, 0, 10, 5, rng)
+    assert len(u) == 5 and all(isinstance(v, int) and 0 <= v < 10 for v in u)
+    f = ex.gen_param(float, 10.0, 0.0, 50, rng)          # a reversed range is swapped
+    assert len(f) == 50 and all(0.0 <= v < 10.0 for v in f)
+    assert ex.gen_param(int, 3, 3, 4, rng) == [3, 3, 3, 3]  # an empty range widens by 1
+    assert ex.gen_param(float, 0.0, 1.0, 0, rng) == []
+    assert len(ex.gen_param(float, 0.0, 1.0)) == 1
+
+
+def test_load_csv_columns_by_position(tmp_path):
+    ex = importlib.import_module("krabmaga_gb300.explore")
+    p = tmp_path / "params.csv"
+    p.write_text("cohesion,jump,n\n0.5,0.7,100\n1.5,0.9,200\n")
+    coh, jump, n = ex.load_csv(str(p), ("cohesion", float), ("jump", float), ("n", int))
+    assert coh == [0.5, 1.5] and jump == [0.7, 0.9] and n == [100, 200]
