@@ -126,6 +126,14 @@ kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float 
  * Agent::is_stopped, schedule.rs:401) is dropped this way: the reference
  * writes nothing for it.  *removed (may be NULL) = objects removed. */
 kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t* removed);
+/* Lookups by object (the parallel build's Field2D::get / get_location,
+ * field_2d.rs:165-170, 189-191, and get_unbuffered / get_location_unbuffered,
+ * field_2d.rs:194-217): for each ids[q], found[q] = 1 and states[4q..4q+3] =
+ * its {x, y, dx, dy} when an object with that id is in the read buffer
+ * (buffered != 0) or the write buffer (buffered == 0); the first one in
+ * stored order when several share the id; found[q] = 0 (None) otherwise. */
+kb_status kb_field_get_locations(kb_field* f, int32_t buffered, size_t n, const uint32_t* ids,
+                                 float* states, int32_t* found);
 /* Field::lazy_update -- field_2d.rs:905-921: the write buffer becomes the
  * read buffer and a new empty write buffer starts. */
 kb_status kb_field_lazy_update(kb_field* f);

@@ -154,6 +154,8 @@ _SIGS = {
     "kb_field_set_locations": (C.c_int32, [_P, C.c_size_t, _U32, _F, _F]),
     "kb_field_remove_object_location": (C.c_int32, [_P, C.c_uint32, _F]),
     "kb_field_remove_ids": (C.c_int32, [_P, C.c_size_t, _U32, _SZ]),
+    "kb_field_get_locations": (C.c_int32, [_P, C.c_int32, C.c_size_t, _U32, _F,
+                                           C.POINTER(C.c_int32)]),
     "kb_field_lazy_update": (C.c_int32, [_P]),
     "kb_field_num_agents": (C.c_int32, [_P, _SZ]),
     "kb_field_num_objects": (C.c_int32, [_P, _SZ]),

@@ -1755,6 +1755,43 @@ kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_
     return KB_OK;
 }
 
+kb_status kb_field_get_locations(kb_field* f, int32_t buffered, size_t n, const uint32_t* ids,
+                                 float* states, int32_t* found) {
+    if (!f || (n && (!ids || !states || !found))) return fail(KB_ERR_ARG, "null argument");
+    if (n == 0) return KB_OK;
+    if (n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many ids");
+    DeviceGuard g(f->device);
+    kb_status st = buffered ? materialize(f) : flush_pending(f);
+    if (st) return st;
+    std::vector<uint32_t> sorted(ids, ids + n);
+    std::sort(sorted.begin(), sorted.end());
+    sorted.erase(std::unique(sorted.begin(), sorted.end()), sorted.end());
+    const uint32_t m = (uint32_t)sorted.size();
+    DevBuf<uint32_t> dq, dfirst;
+    DevBuf<float4> dout;
+    cudaError_t e;
+    if ((e = dq.alloc(m)) || (e = dfirst.alloc(m)) || (e = dout.alloc(m))) return cuda_fail(e, "id lookup");
+    KB_CUDA(cudaMemcpyAsync(dq.p, sorted.data(), sizeof(uint32_t) * m, cudaMemcpyHostToDevice, f->stream));
+    if (buffered)
+        KB_CUDA(launch_find_ids(f->rid.p, nullptr, f->rst.p, f->rn, dq.p, m, dfirst.p, dout.p, f->stream));
+    else
+        KB_CUDA(launch_find_ids(f->wid.p, f->wdead.p, f->wst.p, f->wn, dq.p, m, dfirst.p, dout.p, f->stream));
+    std::vector<uint32_t> first(m);
+    std::vector<float4> out(m);
+    KB_CUDA(cudaMemcpyAsync(first.data(), dfirst.p, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaMemcpyAsync(out.data(), dout.p, sizeof(float4) * m, cudaMemcpyDeviceToHost, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    for (size_t q = 0; q < n; ++q) {
+        const size_t j = std::lower_bound(sorted.begin(), sorted.end(), ids[q]) - sorted.begin();
+        found[q] = first[j] != 0xFFFFFFFFu ? 1 : 0;
+        states[4 * q] = out[j].x;
+        states[4 * q + 1] = out[j].y;
+        states[4 * q + 2] = out[j].z;
+        states[4 * q + 3] = out[j].w;
+    }
+    return KB_OK;
+}
+
 kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t* removed) {
     if (!f || (n && !ids)) return fail(KB_ERR_ARG, "null argument");
     if (removed) *removed = 0;

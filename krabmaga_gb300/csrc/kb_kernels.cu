@@ -361,6 +361,31 @@ __global__ void k_remove_ids(const uint32_t* __restrict__ ids, uint8_t* dead, ui
     }
 }
 
+// first[j] = the smallest index i < n with ids[i] == sorted[j] (live entries
+// only when dead != nullptr); first[] starts at ~0u.
+__global__ void k_find_ids(const uint32_t* __restrict__ ids, const uint8_t* __restrict__ dead,
+                           uint32_t n, const uint32_t* __restrict__ sorted, uint32_t m,
+                           uint32_t* first) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (dead && dead[i])) return;
+    const uint32_t id = ids[i];
+    uint32_t lo = 0, hi = m;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (sorted[mid] < id) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo < m && sorted[lo] == id) atomicMin(&first[lo], i);
+}
+
+__global__ void k_gather_found(const float4* __restrict__ st, const uint32_t* __restrict__ first,
+                               uint32_t m, float4* __restrict__ out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const uint32_t i = first[j];
+    out[j] = i == 0xFFFFFFFFu ? make_float4(0.f, 0.f, 0.f, 0.f) : st[i];
+}
+
 // ---------------------------------------------------------- scan
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
@@ -1356,6 +1381,17 @@ cudaError_t launch_flock_agents(const ForceArgs& a, const float4* in_st, const u
         if (qmode == 0) k_flock_agents<false, 0><<<g, KB_FORCE_THREADS, 0, s>>>(a, in_st, in_ids, nin);
         else k_flock_agents<false, 1><<<g, KB_FORCE_THREADS, 0, s>>>(a, in_st, in_ids, nin);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_find_ids(const uint32_t* ids, const uint8_t* dead, const float4* st, uint32_t n,
+                            const uint32_t* sorted, uint32_t m, uint32_t* first, float4* out,
+                            cudaStream_t s) {
+    if (m == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(uint32_t) * m, s);
+    if (e != cudaSuccess) return e;
+    if (n) k_find_ids<<<grid_for(n, 256), 256, 0, s>>>(ids, dead, n, sorted, m, first);
+    k_gather_found<<<grid_for(m, 256), 256, 0, s>>>(st, first, m, out);
     return cudaGetLastError();
 }
 

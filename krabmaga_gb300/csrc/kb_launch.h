@@ -203,6 +203,12 @@ cudaError_t launch_filter_key(const uint32_t* key, const uint8_t* dead, const fl
 // number marked to *removed.
 cudaError_t launch_remove(const uint32_t* key, uint8_t* dead, const uint32_t* ids, uint32_t n,
                           uint32_t target, uint32_t id, uint32_t* removed, cudaStream_t s);
+// For each id sorted[j] (ascending, distinct): first[j] = the first index i
+// < n with ids[i] == sorted[j] (skipping dead entries when dead != nullptr),
+// ~0u when none, and out[j] = st[first[j]] (zeros when none).
+cudaError_t launch_find_ids(const uint32_t* ids, const uint8_t* dead, const float4* st, uint32_t n,
+                            const uint32_t* sorted, uint32_t m, uint32_t* first, float4* out,
+                            cudaStream_t s);
 // Mark live write-list entries whose id is in sorted[0..m) (ascending) dead;
 // adds the number marked to *removed.
 cudaError_t launch_remove_ids(const uint32_t* ids, uint8_t* dead, uint32_t n, const uint32_t* sorted,

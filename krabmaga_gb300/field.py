@@ -115,6 +115,40 @@ class Field2D:
         L.call("kb_field_remove_object_location", self._h, C.c_uint32(obj.id),
                L.fptr(loc.as_f32()))
 
+    def get_locations(self, ids, buffered: bool = True):
+        """Lookups by id in the read buffer (or, buffered=False, the write
+        buffer): (found bool[n], states f32[n, 4]); the first stored object
+        when several share an id."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32).reshape(-1)
+        st = np.zeros((max(len(ids), 1), 4), np.float32)
+        found = np.zeros(max(len(ids), 1), np.int32)
+        L.call("kb_field_get_locations", self._h, C.c_int32(1 if buffered else 0),
+               C.c_size_t(len(ids)), L.uptr(ids), L.fptr(st),
+               found.ctypes.data_as(C.POINTER(C.c_int32)))
+        return found[: len(ids)].astype(bool), st[: len(ids)]
+
+    def get(self, obj: Bird) -> Optional[Bird]:
+        """Field2D::get (parallel build, field_2d.rs:165-170): the stored copy
+        of the object (read buffer), or None."""
+        found, st = self.get_locations([obj.id], True)
+        return _birds([obj.id], st)[0] if found[0] else None
+
+    def get_location(self, obj: Bird) -> Optional[Real2D]:
+        """Field2D::get_location (parallel build, field_2d.rs:189-191)."""
+        found, st = self.get_locations([obj.id], True)
+        return Real2D(float(st[0, 0]), float(st[0, 1])) if found[0] else None
+
+    def get_unbuffered(self, obj: Bird) -> Optional[Bird]:
+        """Field2D::get_unbuffered (parallel build, field_2d.rs:202-217): the
+        copy in the write buffer, or None."""
+        found, st = self.get_locations([obj.id], False)
+        return _birds([obj.id], st)[0] if found[0] else None
+
+    def get_location_unbuffered(self, obj: Bird) -> Optional[Real2D]:
+        """Field2D::get_location_unbuffered (parallel build, field_2d.rs:194-197)."""
+        found, st = self.get_locations([obj.id], False)
+        return Real2D(float(st[0, 0]), float(st[0, 1])) if found[0] else None
+
     def remove_ids(self, ids) -> int:
         """Remove every write-buffer object with one of these ids (each one as
         remove_object_location at its write location); returns the count."""

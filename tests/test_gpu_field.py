@@ -274,3 +274,37 @@ def test_bulk_set_rejects_bad_objects_and_keeps_the_write_buffer(gpu):
     got, st = f.get_state()
     assert list(got) == [1] + list(range(10, 20))
     assert f.nagents == 11
+
+
+def test_lookups_by_object_read_and_write_buffers(gpu):
+    # the parallel build's get / get_location (read buffer) and get_unbuffered /
+    # get_location_unbuffered (write buffer): the stored copy or None
+    f = kg.Field2D(10.0, 10.0, 0.5, True)
+    a, b = Bird(1, Real2D(1.0, 2.0), Real2D(0.5, 0.0)), Bird(2, Real2D(7.0, 3.0))
+    f.set_object_location(a, a.pos)
+    f.set_object_location(b, b.pos)
+    assert f.get(a) is None and f.get_location_unbuffered(a) == Real2D(1.0, 2.0)
+    f.lazy_update()
+    assert f.get_location(a) == Real2D(1.0, 2.0) and f.get(b) == b
+    assert f.get(a).last_d == Real2D(0.5, 0.0)
+    assert f.get_unbuffered(a) is None and f.get(Bird(9, Real2D(0.0, 0.0))) is None
+    moved = Bird(1, Real2D(4.0, 4.0))
+    f.set_object_location(moved, moved.pos)
+    assert f.get_location_unbuffered(a) == Real2D(4.0, 4.0)
+    assert f.get_location(a) == Real2D(1.0, 2.0)  # the read buffer until lazy_update
+    f.lazy_update()
+    assert f.get_location(a) == Real2D(4.0, 4.0) and f.get(b) is None
+    # many at once, after steps of a flock: equal to the stored states
+    ids, xy, dxy = kg.gen_uniform(3000, 300.0, 300.0, 5, 1.0)
+    g = kg.Field2D(300.0, 300.0, float(np.float32(10.0) / np.float32(1.5)), True)
+    g.set_locations(ids, xy, dxy)
+    g.lazy_update()
+    L.call("kb_flock_step", g.handle, C.byref(kg.FlockParams(seed=2).to_c()), C.c_uint64(0),
+           C.c_uint32(5))
+    sid, sst = g.get_state()
+    q = np.concatenate([sid[::7], [70000, 70001]]).astype(np.uint32)
+    found, st = g.get_locations(q)
+    assert found[:-2].all() and not found[-2:].any()
+    order = {int(i): k for k, i in enumerate(sid)}
+    want = sst[[order[int(i)] for i in q[:-2]]]
+    assert np.array_equal(st[:-2].view(np.uint32), want.view(np.uint32))
