@@ -107,18 +107,20 @@ def test_small_path_equals_separate_kernels(gpu, case):
     assert np.array_equal(ca, cb) and np.array_equal(da, db)
 
 
-def test_small_path_reports_positions_outside_the_matrix(gpu):
+@pytest.mark.parametrize("mode", [0, 3])
+def test_positions_outside_the_matrix_are_flagged_on_both_paths(gpu, mode):
     # y wraps with the width (bird.rs:147): on a field wider than high a lone
-    # bird heading up leaves the bag matrix; the reference panics there, the
-    # step raises the key-range flag
+    # bird heading up leaves the bag matrix; the reference panics there, and
+    # both step paths raise the key-range flag
     f = kg.Field2D(200.0, 20.0, FLOCK_D, True)
+    f.set_step_options(mode)
     f.set_locations(np.array([7], np.uint32), np.array([[199.0, 19.0]], np.float32),
                     np.array([[0.0, 1.0]], np.float32))
     f.lazy_update()
-    assert f.step_path() == kg.KB_PATH_SMALL
+    assert f.step_path() == (kg.KB_PATH_SMALL if mode == 0 else kg.KB_PATH_SEPARATE)
     p = kg.FlockParams(seed=1, arith=kg.KB_ARITH_STRICT, jump=6.0)
-    step(f, p, 0, 30)
     with pytest.raises(kg.KbError):
+        step(f, p, 0, 30)
         f.synchronize()
     assert f.device_flags(clear=True) & 0x1  # KB_FLAG_KEY_RANGE
 
