@@ -12,11 +12,7 @@
 #include <utility>
 #include <vector>
 
-#include "../../include/krabgpu.h"
-#include "kb_common.h"
-#include "kb_fused.h"
-#include "kb_launch.h"
-#include "kb_runtime.h"
+#include "kb_field_impl.h"
 
 namespace kb {
 
@@ -44,7 +40,7 @@ int64_t host_bag_index(const Rep& R, float x, float y) {
 }
 
 bool make_rep_geometry(float w, float h, float d, int toroidal, Rep* R, std::string* why,
-                       int cell_wrap = KB_CELL_WRAP_CLAMP) {
+                       int cell_wrap) {
     if (!(std::isfinite(w) && std::isfinite(h) && std::isfinite(d)) || w <= 0.f || h <= 0.f ||
         d <= 0.f) {
         *why = "width, height and discretization must be finite and positive";
@@ -130,173 +126,11 @@ bool fast_rebin_ok(const Rep& R) {
 
 }  // namespace kb
 
-using namespace kb;
 
 // ========================================================================
-struct kb_field {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    Rep rep{};                  // replica 0: the plain field's geometry + last parameters
-    std::vector<Rep> reps;      // every replica (a plain field holds one, == rep)
-    uint32_t ncells_total = 0;  // bags over all replicas
-    uint32_t cells_cap = 0;     // bag arrays are sized for this many bags
-    Rep rep_uploaded{};         // last replica record written to the device (plain fields)
-    bool rep_valid = false;
-    unsigned long long dstep_host = 0;  // the device step counter once queued work has run
-    bool is_batch = false;
-    DevBuf<Rep> d_rep;
-    // read buffer
-    uint32_t cap = 0;
-    DevBuf<float4> rst;
-    DevBuf<uint32_t> rid;
-    DevBuf<uint32_t> start[2];
-    int cur = 0;
-    uint32_t rn = 0;
-    // write list
-    DevBuf<float4> wst;
-    DevBuf<uint32_t> wid, wkey;
-    DevBuf<uint8_t> wdead;
-    uint32_t wn = 0;
-    bool w_from_compute = false;   // write list == one flock pass over the read buffer
-    bool w_has_dead = false;
-    bool layout_is_positions = true;  // every stored bag == discretize(own pos)
-    std::vector<float4> p_st;
-    std::vector<uint32_t> p_id, p_key;
-    bool p_loc_differs = false;
-    // step temporaries
-    DevBuf<uint32_t> hist, cursor, tid, tsrc, rkey, tkey;
-    bool hist_counted = false;  // a force pass has counted arrivals into hist (no scan since)
-    // Every replica's ids are distinct in the read buffer (checked on the
-    // device after each general rebuild; the step paths keep the id multiset)
-    bool ids_unique = false;
-    DevBuf<unsigned long long> dup_tab;
-    // Several replicas: block tables of the force and segment-rebin kernels
-    // ({replica, first boid} / {replica, first segment}), no block spanning
-    // two replicas; rebuilt with the replica table.
-    DevBuf<uint2> blk_force, blk_seg;
-    std::vector<uint2> blk_force_h, blk_seg_h;
-    uint32_t nblk_force = 0, nblk_seg = 0;
-    DevBuf<float4> tst;
-    DevBuf<ScanCtl> scan_ctl, aux_ctl;
-    DevBuf<unsigned long long> tstate, aux_tstate;
-    uint32_t aux_tiles = 0;
-    DevBuf<uint32_t> err;
-    DevBuf<unsigned long long> dstep;
-    DevBuf<uint32_t> small;  // 16 words of scratch for counts
-    // Field2D bookkeeping (field_2d.rs:276, 284-287)
-    size_t nagents = 0;
-    bool density_check = false;
-    // graphs: (steps per graph, start parity, params) -> exec
-    struct GraphKey {
-        uint32_t steps;
-        int parity;
-        std::vector<uint8_t> params;
-        bool operator<(const GraphKey& o) const {
-            if (steps != o.steps) return steps < o.steps;
-            if (parity != o.parity) return parity < o.parity;
-            return params < o.params;
-        }
-    };
-    std::map<GraphKey, cudaGraphExec_t> graphs;
-    // split-step graphs: (steps, cur, a_last, virt) -> exec + end state
-    struct SGraph {
-        cudaGraphExec_t exec;
-        int cur, a_last;
-    };
-    std::map<std::vector<uint32_t>, SGraph> sgraphs;
-    // persistent fused step (kb_fused.cu)
-    struct Fused {
-        bool ready = false;
-        uint32_t n = 0;
-        int strict = -1, qmode = -1, dd = -1;
-        FusedCfg cfg{};
-        uint32_t nctas = 0;
-        uint32_t ntiles = 0;
-        DevBuf<Tile> tiles;
-        DevBuf<float4> g_st;
-        DevBuf<uint32_t> g_ids;
-        DevBuf<unsigned long long> scan_state;
-        DevBuf<uint32_t> ctl;  // [0] tile counter, [1..2] barrier, [3] scan epoch, [4] overflow tiles
-        DevBuf<unsigned long long> phase_cycles;  // per-CTA phase clocks when profiling
-        bool profile = false;
-        bool occ_valid = false;  // cached occupancy of the last configuration
-        FusedCfg occ_cfg{};
-        int occ_strict = -1, occ_qmode = -1, occ_ctas = 0;
-    } fused;
-    // 0 separate kernels (small fields: one block, kb_small.cu), 1 persistent
-    // fused, 2 split tile step, 3 separate kernels whatever the size
-    int fused_mode = 0;
-    // Per-kernel timing of ungraphed separate-kernel steps: four events per
-    // step (force | scan | rebin), read and recycled by kb_field_kernel_times.
-    bool ktime = false;
-    struct KtStep {
-        cudaEvent_t ev[4];
-    };
-    std::vector<cudaEvent_t> kt_pool;
-    std::vector<KtStep> kt_pending;
-    int kt_cur = -1;  // step whose scan|rebin boundary fast_rebuild records
-    // After fused steps the read buffer can stay virtual: the last write list
-    // (in buffer a_last: 0 rst, 1 wst, 2 tst) plus start[1-cur] (its bag
-    // offsets) and start[cur] (the read buffer's bag offsets).
-    bool virt = false;
-    int a_last = 0;
-    bool keys_valid = false;  // buf_key(a_last) holds the bag keys of the virtual write list
-    int32_t tile_tx = 0, tile_ty = 0;  // 0: automatic
-    // Dense flocks (long candidate lists, single replica): the force pass
-    // walks each column run with a pointer and the rebin takes 8-bag
-    // segments.  Chosen (dense_mode KB_DENSE_AUTO) from the read buffer's sum
-    // of squared bag occupancies, about 9 * sum / N candidates per boid,
-    // measured after every general rebuild and every DENSE_REFRESH steps
-    // (read back without blocking).  Both paths give the same bits.
-    int32_t dense_mode = KB_DENSE_AUTO;
-    bool dense = false;
-    DevBuf<unsigned long long> occ_dev;
-    unsigned long long* occ_host = nullptr;  // pinned
-    cudaEvent_t occ_ev = nullptr;
-    bool occ_pending = false;
-    uint32_t occ_n = 0;  // boids when the pending measurement was taken
-    uint64_t steps_since_occ = 0;
 
-    ~kb_field() {
-        drop_graphs();
-        if (stream) cudaStreamSynchronize(stream);
-        if (occ_ev) cudaEventDestroy(occ_ev);
-        if (occ_host) cudaFreeHost(occ_host);
-        for (auto& k : kt_pending)
-            for (cudaEvent_t e : k.ev) cudaEventDestroy(e);
-        for (cudaEvent_t e : kt_pool) cudaEventDestroy(e);
-        if (stream) cudaStreamDestroy(stream);
-    }
-    void drop_graphs() {
-        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
-        graphs.clear();
-        for (auto& kv : sgraphs) cudaGraphExecDestroy(kv.second.exec);
-        sgraphs.clear();
-    }
-};
 
-namespace {
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int now = -1;
-        cudaGetDevice(&now);
-        if (prev >= 0 && now != prev) cudaSetDevice(prev);
-    }
-};
-
-#define KB_CUDA(call)                                   \
-    do {                                                \
-        cudaError_t e_ = (call);                        \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-    } while (0)
-
-kb_status materialize(kb_field* f);
 
 kb_status grow(kb_field* f, uint32_t need) {
     if (need <= f->cap) return KB_OK;
@@ -1007,7 +841,6 @@ kb_status field_lazy_update(kb_field* f) {
     return KB_OK;
 }
 
-}  // namespace
 
 // ====================================================================== C ABI
 extern "C" {
@@ -1026,11 +859,10 @@ int32_t kb_device_count(void) {
 
 }  // extern "C"
 
-namespace {
 
 // Allocate a field over a replica table (cell_off/boid_off already set).
 kb_status field_new(int device, const std::vector<Rep>& reps, bool is_batch, uint32_t capacity,
-                    kb_field** out, uint32_t cells_cap = 0) {
+                    kb_field** out, uint32_t cells_cap) {
     *out = nullptr;
     int ndev = kb_device_count();
     if (ndev <= 0) return fail(KB_ERR_NO_DEVICE, "no CUDA device visible");
@@ -1145,7 +977,6 @@ kb_status field_set_reps(kb_field* f, const std::vector<Rep>& reps) {
     return build_rep_blocks(f);
 }
 
-}  // namespace
 
 namespace kb {
 // The field's device and its read buffer as query arguments, for query
@@ -1644,10 +1475,60 @@ kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long*
     return KB_OK;
 }
 
-static kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_step,
+}  // extern "C"
+
+// Time `steps` fused steps under each candidate tile shape (real steps of
+// the simulation, numbered from first_step) and keep the fastest shape.
+kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                                 uint32_t steps, const int32_t* cand, int32_t ncand,
                                 int32_t* best_out, float* best_ms_out,
-                                kb_status (*run)(void*, uint64_t, uint32_t), void* ctx);
+                                kb_status (*run)(void*, uint64_t, uint32_t), void* ctx) {
+    static const int32_t defaults[] = {8, 16, 8, 32, 16, 16, 16, 32, 32, 32, 16, 64, 32, 16};
+    if (!cand || ncand <= 0) {
+        cand = defaults;
+        ncand = (int32_t)(sizeof(defaults) / sizeof(defaults[0]) / 2);
+    }
+    cudaEvent_t e0, e1;
+    KB_CUDA(cudaEventCreate(&e0));
+    KB_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_i = -1;
+    uint64_t step = first_step;
+    kb_status st = KB_OK;
+    for (int32_t i = 0; i < ncand && !st; ++i) {
+        f->tile_tx = cand[2 * i];
+        f->tile_ty = cand[2 * i + 1];
+        f->fused.ready = false;
+        if ((st = run(ctx, step, 1))) break;  // prepares the layout, warms up
+        step += 1;
+        if (cudaEventRecord(e0, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        if ((st = run(ctx, step, steps))) break;
+        step += steps;
+        if (cudaEventRecord(e1, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        if (cudaEventSynchronize(e1) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            best_i = i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    f->tile_tx = cand[2 * best_i];
+    f->tile_ty = cand[2 * best_i + 1];
+    f->fused.ready = false;
+    if (best_out) {
+        best_out[0] = f->tile_tx;
+        best_out[1] = f->tile_ty;
+        best_out[2] = (int32_t)(step - first_step);  // steps consumed
+    }
+    if (best_ms_out) *best_ms_out = best / (float)steps;
+    return KB_OK;
+}
+
+extern "C" {
 
 struct FieldTuneCtx {
     kb_field* f;
@@ -1846,7 +1727,9 @@ static int kt_begin(kb_field* f, bool fast) {
     return (int)f->kt_pending.size() - 1;
 }
 
-static kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps, bool fast) {
+}  // extern "C"
+
+kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps, bool fast) {
     for (uint32_t s = 0; s < nsteps; ++s) {
         const int t = kt_begin(f, fast);
         if (t >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[t].ev[0], f->stream));
@@ -1864,6 +1747,8 @@ static kb_status enqueue_steps(kb_field* f, const kb_flock_params* p, uint32_t n
     }
     return KB_OK;
 }
+
+extern "C" {
 
 static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                                  uint32_t nsteps) {
@@ -2003,894 +1888,6 @@ kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_st
     kb_status st = flock_step_impl(f, p, first_step, nsteps);
     if (f) f->dstep_host = st ? ~0ull : first_step + nsteps;  // unknown after a failure
     return st;
-}
-
-}  // extern "C"
-
-// ====================================================================== batch
-struct kb_batch {
-    kb_field* f = nullptr;
-    kb_flock_params common{};  // query mode and arithmetic shared by the replicas
-    std::vector<uint8_t> have;  // replica initialised
-    struct GKey {
-        uint32_t launches, spl;
-        int cur, a_last, virt;
-        bool operator<(const GKey& o) const {
-            if (launches != o.launches) return launches < o.launches;
-            if (spl != o.spl) return spl < o.spl;
-            if (cur != o.cur) return cur < o.cur;
-            if (a_last != o.a_last) return a_last < o.a_last;
-            return virt < o.virt;
-        }
-    };
-    struct GVal {
-        cudaGraphExec_t exec;
-        int cur, a_last;
-    };
-    std::map<GKey, GVal> graphs;
-    ~kb_batch() {
-        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
-        if (f) {
-            cudaStreamSynchronize(f->stream);
-            delete f;
-        }
-    }
-};
-
-extern "C" {
-
-kb_status kb_batch_create(int32_t device, uint32_t nrep, const kb_replica_desc* reps,
-                          kb_batch** out) {
-    if (!reps || !out || nrep == 0) return fail(KB_ERR_ARG, "null argument or no replicas");
-    *out = nullptr;
-    std::vector<Rep> table(nrep);
-    uint64_t cells = 0, boids = 0;
-    std::string why;
-    for (uint32_t r = 0; r < nrep; ++r) {
-        const kb_replica_desc& d = reps[r];
-        if (!make_rep_geometry(d.width, d.height, d.discretization, d.toroidal, &table[r], &why,
-                               d.cell_wrap))
-            return fail(KB_ERR_ARG, "replica " + std::to_string(r) + ": " + why);
-        if (!params_ok(&d.params, &why)) return fail(KB_ERR_ARG, "replica " + std::to_string(r) + ": " + why);
-        if (d.params.query_mode != reps[0].params.query_mode || d.params.arith != reps[0].params.arith)
-            return fail(KB_ERR_ARG, "all replicas of a batch share query_mode and arith");
-        set_rep_params(&table[r], &d.params);
-        table[r].cell_off = (uint32_t)cells;
-        table[r].boid_off = (uint32_t)boids;
-        table[r].nboids = d.nboids;
-        cells += table[r].ncells;
-        boids += d.nboids;
-        if (cells > 0xF0000000ull || boids > 0xF0000000ull) return fail(KB_ERR_ARG, "batch too large");
-    }
-    kb_field* f = nullptr;
-    kb_status st = field_new(device, table, true, (uint32_t)boids, &f);
-    if (st) return st;
-    kb_batch* b = new kb_batch();
-    b->f = f;
-    b->common = reps[0].params;
-    b->have.assign(nrep, 0);
-    *out = b;
-    return KB_OK;
-}
-
-kb_status kb_batch_destroy(kb_batch* b) {
-    if (!b) return KB_OK;
-    DeviceGuard g(b->f->device);
-    delete b;
-    return KB_OK;
-}
-
-kb_status kb_batch_set_replica(kb_batch* b, uint32_t r, size_t n, const uint32_t* ids,
-                               const float* xy, const float* dxy) {
-    if (!b || (n && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
-    kb_field* f = b->f;
-    if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
-    if (b->have[r]) return fail(KB_ERR_STATE, "replica already set (create a new batch to reset)");
-    if (n != f->reps[r].nboids) return fail(KB_ERR_ARG, "boid count differs from the replica's nboids");
-    const Rep& R = f->reps[r];
-    const size_t old = f->p_id.size();
-    for (size_t i = 0; i < n; ++i) {
-        if (!(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) && std::isfinite(dxy[2 * i]) &&
-              std::isfinite(dxy[2 * i + 1]))) {
-            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
-            return fail(KB_ERR_ARG, "non-finite position or heading");
-        }
-        const int64_t idx = host_bag_index(R, xy[2 * i], xy[2 * i + 1]);
-        if (idx < 0) {
-            f->p_st.resize(old); f->p_id.resize(old); f->p_key.resize(old);
-            return fail(KB_ERR_RANGE, "location outside the replica's bag matrix");
-        }
-        f->p_st.push_back(make_float4(xy[2 * i], xy[2 * i + 1], dxy[2 * i], dxy[2 * i + 1]));
-        f->p_id.push_back(ids[i]);
-        f->p_key.push_back(R.cell_off + (uint32_t)idx);
-    }
-    b->have[r] = 1;
-    return KB_OK;
-}
-
-// Build the packed read buffer (every replica must be set).
-kb_status kb_batch_commit(kb_batch* b) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    for (size_t r = 0; r < b->have.size(); ++r)
-        if (!b->have[r]) return fail(KB_ERR_STATE, "replica " + std::to_string(r) + " not set");
-    kb_field* f = b->f;
-    DeviceGuard g(f->device);
-    kb_status st = field_lazy_update(f);
-    if (st) return st;
-    uint64_t expect = 0;
-    for (const Rep& R : f->reps) expect += R.nboids;
-    if (f->rn != expect) return fail(KB_ERR_STATE, "packed boid count mismatch");
-    return upload_rep(f);
-}
-
-// nsteps steps of every replica, each replica with its own parameters.
-// steps_per_launch (0 = all) persistent steps per kernel launch; with
-// graph_launches > 1 that many launches are captured into one CUDA graph
-// and replayed.
-kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint32_t steps_per_launch,
-                        uint32_t graph_launches) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    kb_field* f = b->f;
-    if (f->wn || !f->p_id.empty()) return fail(KB_ERR_STATE, "batch not committed");
-    if (nsteps == 0) return KB_OK;
-    DeviceGuard g(f->device);
-    const kb_flock_params* p = &b->common;
-    kb_status st;
-    KB_CUDA(launch_set_u64(f->dstep.p, first_step, f->stream));
-    f->dstep_host = ~0ull;
-    if (!fused_eligible(f, p)) {
-        if ((st = materialize(f))) return st;
-        if ((st = grow(f, f->rn))) return st;
-        return enqueue_steps(f, p, nsteps, all_fast_rebin_ok(f) && f->layout_is_positions);
-    }
-    if ((st = grow(f, f->rn))) return st;
-    if ((st = fused_prepare(f, p))) return st;
-    if (f->fused_mode == 2)  // split: two launches per step, graphs of graph_launches steps
-        return split_steps_graphed(f, p, nsteps, graph_launches > 1 ? graph_launches : 100);
-    const uint32_t spl = steps_per_launch == 0 ? nsteps : std::min(steps_per_launch, nsteps);
-    uint32_t done = 0;
-    while (done < nsteps) {
-        const uint32_t left = nsteps - done;
-        const uint32_t full = left / spl;
-        if (graph_launches > 1 && full >= 2) {
-            const uint32_t L = std::min(graph_launches, full);
-            kb_batch::GKey key{L, spl, f->cur, f->a_last, f->virt ? 1 : 0};
-            auto it = b->graphs.find(key);
-            if (it == b->graphs.end()) {
-                const int cur0 = f->cur, al0 = f->a_last;
-                const bool v0 = f->virt;
-                cudaGraph_t graph = nullptr;
-                KB_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
-                st = KB_OK;
-                for (uint32_t k = 0; k < L && !st; ++k) st = fused_steps(f, p, spl);
-                cudaError_t ce = cudaStreamEndCapture(f->stream, &graph);
-                if (st) {
-                    if (graph) cudaGraphDestroy(graph);
-                    return st;
-                }
-                if (ce) return cuda_fail(ce, "cudaStreamEndCapture");
-                cudaGraphExec_t exec = nullptr;
-                ce = cudaGraphInstantiate(&exec, graph, 0);
-                cudaGraphDestroy(graph);
-                if (ce) return cuda_fail(ce, "cudaGraphInstantiate");
-                it = b->graphs.emplace(key, kb_batch::GVal{exec, f->cur, f->a_last}).first;
-                f->cur = cur0;
-                f->a_last = al0;
-                f->virt = v0;
-            }
-            KB_CUDA(cudaGraphLaunch(it->second.exec, f->stream));
-            f->cur = it->second.cur;
-            f->a_last = it->second.a_last;
-            f->virt = true;
-            done += L * spl;
-        } else {
-            const uint32_t k = std::min(spl, left);
-            if ((st = fused_steps(f, p, k))) return st;
-            done += k;
-        }
-    }
-    return KB_OK;
-}
-
-// Time `steps` fused steps under each candidate tile shape (real steps of
-// the simulation, numbered from first_step) and keep the fastest shape.
-static kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_step,
-                                uint32_t steps, const int32_t* cand, int32_t ncand,
-                                int32_t* best_out, float* best_ms_out,
-                                kb_status (*run)(void*, uint64_t, uint32_t), void* ctx) {
-    static const int32_t defaults[] = {8, 16, 8, 32, 16, 16, 16, 32, 32, 32, 16, 64, 32, 16};
-    if (!cand || ncand <= 0) {
-        cand = defaults;
-        ncand = (int32_t)(sizeof(defaults) / sizeof(defaults[0]) / 2);
-    }
-    cudaEvent_t e0, e1;
-    KB_CUDA(cudaEventCreate(&e0));
-    KB_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int best_i = -1;
-    uint64_t step = first_step;
-    kb_status st = KB_OK;
-    for (int32_t i = 0; i < ncand && !st; ++i) {
-        f->tile_tx = cand[2 * i];
-        f->tile_ty = cand[2 * i + 1];
-        f->fused.ready = false;
-        if ((st = run(ctx, step, 1))) break;  // prepares the layout, warms up
-        step += 1;
-        if (cudaEventRecord(e0, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
-        if ((st = run(ctx, step, steps))) break;
-        step += steps;
-        if (cudaEventRecord(e1, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
-        if (cudaEventSynchronize(e1) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-            best = ms;
-            best_i = i;
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (st) return st;
-    f->tile_tx = cand[2 * best_i];
-    f->tile_ty = cand[2 * best_i + 1];
-    f->fused.ready = false;
-    if (best_out) {
-        best_out[0] = f->tile_tx;
-        best_out[1] = f->tile_ty;
-        best_out[2] = (int32_t)(step - first_step);  // steps consumed
-    }
-    if (best_ms_out) *best_ms_out = best / (float)steps;
-    return KB_OK;
-}
-
-static kb_status run_batch_steps(void* ctx, uint64_t first, uint32_t n) {
-    return kb_batch_step((kb_batch*)ctx, first, n, 0, 0);
-}
-
-kb_status kb_batch_autotune(kb_batch* b, uint64_t first_step, uint32_t steps_per_trial,
-                            const int32_t* candidates, int32_t ncand, int32_t best[3],
-                            float* ms_per_step) {
-    if (!b || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
-    DeviceGuard g(b->f->device);
-    if (!fused_eligible(b->f, &b->common)) return fail(KB_ERR_STATE, "batch not eligible for the fused step");
-    return autotune_tiles(b->f, &b->common, first_step, steps_per_trial, candidates, ncand, best,
-                          ms_per_step, run_batch_steps, b);
-}
-
-kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* states, size_t cap,
-                               size_t* n) {
-    if (!b || !n) return fail(KB_ERR_ARG, "null argument");
-    kb_field* f = b->f;
-    if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
-    DeviceGuard g(f->device);
-    kb_status st = materialize(f);
-    if (st) return st;
-    const Rep& R = f->reps[r];
-    uint32_t lo = 0, hi = 0;
-    KB_CUDA(cudaMemcpyAsync(&lo, f->start[f->cur].p + R.cell_off, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
-    KB_CUDA(cudaMemcpyAsync(&hi, f->start[f->cur].p + R.cell_off + R.ncells, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
-    KB_CUDA(cudaStreamSynchronize(f->stream));
-    *n = hi - lo;
-    const size_t take = std::min<size_t>(hi - lo, cap);
-    if (take) {
-        if (ids) KB_CUDA(cudaMemcpyAsync(ids, f->rid.p + lo, sizeof(uint32_t) * take, cudaMemcpyDeviceToHost, f->stream));
-        if (states) KB_CUDA(cudaMemcpyAsync(states, f->rst.p + lo, sizeof(float4) * take, cudaMemcpyDeviceToHost, f->stream));
-    }
-    KB_CUDA(cudaStreamSynchronize(f->stream));
-    return check_flags(f);
-}
-
-// Moments of every replica's headings, reduced on the device.
-static kb_status field_moments(kb_field* f, double* out) {
-    DeviceGuard g(f->device);
-    kb_status st = materialize(f);
-    if (st) return st;
-    if ((st = upload_rep(f))) return st;
-    const uint32_t nr = (uint32_t)f->reps.size();
-    DevBuf<double> d;
-    cudaError_t e = d.alloc(4 * (size_t)nr);
-    if (e) return cuda_fail(e, "moments");
-    KB_CUDA(launch_moments(f->d_rep.p, nr, f->start[f->cur].p, f->rst.p, d.p, f->stream));
-    KB_CUDA(cudaMemcpyAsync(out, d.p, sizeof(double) * 4 * nr, cudaMemcpyDeviceToHost, f->stream));
-    KB_CUDA(cudaStreamSynchronize(f->stream));
-    return check_flags(f);
-}
-
-kb_status kb_batch_moments(kb_batch* b, double* out) {
-    if (!b || !out) return fail(KB_ERR_ARG, "null argument");
-    return field_moments(b->f, out);
-}
-
-kb_status kb_field_moments(kb_field* f, double out4[4]) {
-    if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
-    if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: use kb_batch_moments");
-    return field_moments(f, out4);
-}
-
-// Rebuild a committed batch with a new replica table: slot i of `reps`
-// takes the canonical records of old replica src[i] (src[i] >= 0) or, for
-// src[i] < 0, the n host objects given (a new replica's initial state).
-static kb_status batch_repack(kb_batch* b, std::vector<Rep> reps, const std::vector<int64_t>& src,
-                              size_t n_new, const uint32_t* ids, const float* xy, const float* dxy) {
-    kb_field* f = b->f;
-    DeviceGuard g(f->device);
-    kb_status st = materialize(f);
-    if (st) return st;
-    const std::vector<Rep> old = f->reps;
-    std::vector<PackEntry> plan;
-    uint64_t cells = 0, boids = 0, host_off = 0;
-    bool have_host = false;
-    for (size_t i = 0; i < reps.size(); ++i) {
-        Rep& R = reps[i];
-        R.cell_off = (uint32_t)cells;
-        R.boid_off = (uint32_t)boids;
-        if (src[i] >= 0) {
-            PackEntry e{};
-            e.dst_off = (uint32_t)boids;
-            e.n = R.nboids;
-            e.rep = (uint32_t)i;
-            e.src_off = old[(size_t)src[i]].boid_off;
-            e.kind = 0u;
-            if (e.n) plan.push_back(e);
-        } else {
-            have_host = true;
-            host_off = boids;
-        }
-        cells += R.ncells;
-        boids += R.nboids;
-    }
-    if (cells > 0xF0000000ull || boids > 0xF0000000ull) return fail(KB_ERR_ARG, "batch too large");
-    if ((st = grow(f, (uint32_t)std::max<uint64_t>(boids, 1)))) return st;
-    if ((st = grow_cells(f, cells))) return st;
-    DevBuf<PackEntry> dplan;
-    if (!plan.empty()) {
-        cudaError_t e = dplan.alloc(plan.size());
-        if (e) return cuda_fail(e, "repack plan");
-        KB_CUDA(cudaMemcpyAsync(dplan.p, plan.data(), sizeof(PackEntry) * plan.size(), cudaMemcpyHostToDevice, f->stream));
-    }
-    // the read buffer (rst) is the copy source; the write list the target
-    if ((st = field_set_reps(f, reps))) return st;
-    if (!plan.empty())
-        KB_CUDA(launch_repack(dplan.p, (int32_t)plan.size(), (uint32_t)boids, f->d_rep.p, f->rst.p,
-                              f->rid.p, f->wst.p, f->wid.p, f->wkey.p, f->wdead.p, f->err.p, f->stream));
-    if (have_host && n_new) {
-        const Rep& R = f->reps[std::find(src.begin(), src.end(), (int64_t)-1) - src.begin()];
-        const uint32_t m = (uint32_t)n_new, at = (uint32_t)host_off;
-        float2* sxy = reinterpret_cast<float2*>(f->tst.p);
-        KB_CUDA(cudaMemcpyAsync(sxy, xy, sizeof(float2) * m, cudaMemcpyHostToDevice, f->stream));
-        KB_CUDA(cudaMemcpyAsync(sxy + m, dxy, sizeof(float2) * m, cudaMemcpyHostToDevice, f->stream));
-        KB_CUDA(cudaMemcpyAsync(f->wid.p + at, ids, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, f->stream));
-        KB_CUDA(cudaMemsetAsync(f->small.p, 0xFF, sizeof(uint32_t), f->stream));
-        KB_CUDA(launch_pack_locations(R, sxy, sxy + m, m, f->wst.p + at, f->wkey.p + at, f->wdead.p + at,
-                                      f->small.p, f->stream));
-        uint32_t bad = 0;
-        if ((st = read_u32(f, f->small.p, &bad))) return st;
-        if (bad != 0xFFFFFFFFu)
-            return fail(KB_ERR_RANGE, "new replica: object " + std::to_string(bad) +
-                                          " outside its bag matrix on the device");
-    }
-    f->wn = (uint32_t)boids;
-    f->w_from_compute = false;
-    f->w_has_dead = false;
-    f->virt = false;
-    f->p_st.clear(); f->p_id.clear(); f->p_key.clear();
-    if ((st = general_rebuild(f, false))) return st;
-    f->rn = (uint32_t)boids;
-    f->wn = 0;
-    f->layout_is_positions = true;
-    if ((st = check_unique_ids(f))) return st;
-    b->have.assign(reps.size(), 1);
-    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second.exec);
-    b->graphs.clear();
-    return check_flags(f);
-}
-
-kb_status kb_batch_remove_replica(kb_batch* b, uint32_t r) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    kb_field* f = b->f;
-    if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
-    if (f->reps.size() < 2) return fail(KB_ERR_STATE, "a batch keeps at least one replica");
-    if (f->wn || !f->p_id.empty() || std::find(b->have.begin(), b->have.end(), 0) != b->have.end())
-        return fail(KB_ERR_STATE, "batch not committed");
-    std::vector<Rep> reps;
-    std::vector<int64_t> src;
-    for (uint32_t i = 0; i < f->reps.size(); ++i)
-        if (i != r) {
-            reps.push_back(f->reps[i]);
-            src.push_back(i);
-        }
-    return batch_repack(b, reps, src, 0, nullptr, nullptr, nullptr);
-}
-
-kb_status kb_batch_add_replica(kb_batch* b, const kb_replica_desc* d, const uint32_t* ids,
-                               const float* xy, const float* dxy, uint64_t origin_step,
-                               uint32_t* index) {
-    if (!b || !d || !index || (d->nboids && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
-    kb_field* f = b->f;
-    if (f->wn || !f->p_id.empty() || std::find(b->have.begin(), b->have.end(), 0) != b->have.end())
-        return fail(KB_ERR_STATE, "batch not committed");
-    Rep R;
-    std::string why;
-    if (!make_rep_geometry(d->width, d->height, d->discretization, d->toroidal, &R, &why, d->cell_wrap))
-        return fail(KB_ERR_ARG, why);
-    if (!params_ok(&d->params, &why)) return fail(KB_ERR_ARG, why);
-    if (d->params.query_mode != b->common.query_mode || d->params.arith != b->common.arith)
-        return fail(KB_ERR_ARG, "all replicas of a batch share query_mode and arith");
-    set_rep_params(&R, &d->params);
-    R.nboids = d->nboids;
-    // checked here so that a refused replica leaves the batch as it was
-    for (uint32_t i = 0; i < d->nboids; ++i) {
-        if (!(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) && std::isfinite(dxy[2 * i]) &&
-              std::isfinite(dxy[2 * i + 1])))
-            return fail(KB_ERR_ARG, "object " + std::to_string(i) + ": non-finite position or heading");
-        if (host_bag_index(R, xy[2 * i], xy[2 * i + 1]) < 0)
-            return fail(KB_ERR_RANGE, "object " + std::to_string(i) + ": location outside the replica's bag matrix");
-    }
-    R.origin_lo = (uint32_t)origin_step;
-    R.origin_hi = (uint32_t)(origin_step >> 32);
-    std::vector<Rep> reps = f->reps;
-    std::vector<int64_t> src;
-    for (uint32_t i = 0; i < reps.size(); ++i) src.push_back(i);
-    reps.push_back(R);
-    src.push_back(-1);
-    kb_status st = batch_repack(b, reps, src, d->nboids, ids, xy, dxy);
-    if (st) return st;
-    *index = (uint32_t)(reps.size() - 1);
-    return KB_OK;
-}
-
-kb_status kb_batch_synchronize(kb_batch* b) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    return kb_field_synchronize(b->f);
-}
-
-kb_status kb_batch_cuda_stream(kb_batch* b, void** stream) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    return kb_field_cuda_stream(b->f, stream);
-}
-
-kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    return kb_field_set_step_options(b->f, fused, tile_tx, tile_ty);
-}
-
-kb_status kb_batch_step_stats(kb_batch* b, uint32_t out4[4]) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    return kb_field_step_stats(b->f, out4);
-}
-
-kb_status kb_batch_device_flags(kb_batch* b, uint32_t* flags, int32_t clear) {
-    if (!b) return fail(KB_ERR_ARG, "null argument");
-    return kb_field_device_flags(b->f, flags, clear);
-}
-
-}  // extern "C"
-
-// ====================================================================== serving
-// A continuous-batching request loop.  Requests (each a whole Flockers
-// simulation) are admitted while a slot is free and their device state fits
-// the HBM budget; all admitted requests advance together in one batched
-// field, one persistent launch per epoch.  An epoch runs until the next
-// request finishes, at most `quantum` steps; between epochs finished
-// requests are copied out (their latency ends when the result is on the
-// host) and queued ones join: the batch is repacked on the device (running
-// replicas copied in canonical order, new ones generated in place) and one
-// stable sort rebuilds the bag offsets.  Each request keeps its own step
-// numbering (Rep::origin), so its result equals a run of it alone.
-#include <chrono>
-#include <condition_variable>
-#include <deque>
-#include <mutex>
-#include <thread>
-
-namespace {
-
-using Clock = std::chrono::steady_clock;
-
-struct SrvReq {
-    uint64_t ticket = 0;
-    kb_request r{};
-    Rep geom{};
-    uint64_t bytes = 0;
-    Clock::time_point t_arrive, t_admit, t_done;
-    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
-    uint32_t remaining = 0;
-    uint32_t boid_off = 0;  // in the current packing
-    bool fresh = true;
-    std::vector<uint32_t> ids;
-    std::vector<float> st;
-    std::string error;
-};
-
-uint64_t request_bytes(const Rep& R, uint32_t n) {
-    // read buffer + two write lists + sort scratch per boid; offsets per bag
-    return (uint64_t)n * (16 + 4) * 6 + (uint64_t)R.ncells * 4 * 4;
-}
-
-}  // namespace
-
-struct kb_server {
-    kb_server_desc desc{};
-    kb_field* f = nullptr;
-    kb_flock_params common{};
-    std::thread loop;
-    std::mutex mu;
-    std::condition_variable cv, cv_done;
-    bool stop = false;
-    std::deque<SrvReq*> queue;
-    std::vector<SrvReq*> active;
-    std::map<uint64_t, SrvReq*> all;
-    uint64_t next_ticket = 1;
-    uint64_t used_bytes = 0;
-    uint64_t global_step = 0;
-    DevBuf<PackEntry> plan;
-    // stats
-    std::vector<double> latencies;
-    double updates = 0.0;
-    uint64_t launches = 0, repacks = 0, max_active = 0, completed = 0, failed = 0;
-    Clock::time_point t_first, t_last;
-    bool any = false;
-    double busy_s = 0.0;
-};
-
-namespace {
-
-kb_status srv_repack(kb_server* S, std::vector<SrvReq*>& act) {
-    kb_field* f = S->f;
-    kb_status st = materialize(f);
-    if (st) return st;
-    std::vector<Rep> reps;
-    std::vector<PackEntry> plan;
-    uint64_t cells = 0, boids = 0;
-    for (SrvReq* q : act) {
-        Rep R = q->geom;
-        R.cell_off = (uint32_t)cells;
-        R.boid_off = (uint32_t)boids;
-        R.nboids = q->r.nboids;
-        if (q->fresh) {
-            R.origin_lo = (uint32_t)S->global_step;
-            R.origin_hi = (uint32_t)(S->global_step >> 32);
-        }
-        PackEntry e{};
-        e.dst_off = (uint32_t)boids;
-        e.n = q->r.nboids;
-        e.rep = (uint32_t)reps.size();
-        e.src_off = q->boid_off;
-        e.kind = q->fresh ? 1u : 0u;
-        e.seed_lo = (uint32_t)q->r.init_seed;
-        e.seed_hi = (uint32_t)(q->r.init_seed >> 32);
-        e.heading_scale = q->r.heading_scale;
-        plan.push_back(e);
-        q->geom = R;
-        q->boid_off = (uint32_t)boids;
-        cells += R.ncells;
-        boids += q->r.nboids;
-        reps.push_back(R);
-    }
-    if (boids > f->cap) return fail(KB_ERR_OOM, "server boid capacity exceeded");
-    if (plan.size() > S->plan.n) {
-        cudaError_t e = S->plan.alloc(std::max<size_t>(plan.size(), 2 * S->plan.n + 16));
-        if (e) return cuda_fail(e, "repack plan");
-    }
-    KB_CUDA(cudaMemcpyAsync(S->plan.p, plan.data(), sizeof(PackEntry) * plan.size(), cudaMemcpyHostToDevice, f->stream));
-    // the old read buffer (rst) is the copy source; the write list the target
-    if ((st = field_set_reps(f, reps))) return st;  // synchronises the stream (plan copied)
-    KB_CUDA(launch_repack(S->plan.p, (int32_t)plan.size(), (uint32_t)boids, f->d_rep.p, f->rst.p, f->rid.p,
-                          f->wst.p, f->wid.p, f->wkey.p, f->wdead.p, f->err.p, f->stream));
-    f->wn = (uint32_t)boids;
-    f->w_from_compute = false;
-    f->w_has_dead = false;
-    f->virt = false;
-    if ((st = general_rebuild(f, false))) return st;
-    f->rn = (uint32_t)boids;
-    set_ids_unique(f, true);  // every request's boids are ids 0..n-1
-    f->wn = 0;
-    f->layout_is_positions = true;
-    for (SrvReq* q : act) q->fresh = false;
-    S->repacks++;
-    return KB_OK;
-}
-
-void srv_fail_all(kb_server* S, std::vector<SrvReq*>& act, const std::string& why) {
-    std::lock_guard<std::mutex> lk(S->mu);
-    for (SrvReq* q : act) {
-        q->state = 3;
-        q->error = why;
-        q->t_done = Clock::now();
-        S->used_bytes -= q->bytes;
-        S->failed++;
-    }
-    act.clear();
-    S->cv_done.notify_all();
-}
-
-void srv_loop(kb_server* S) {
-    cudaSetDevice(S->desc.device);
-    kb_field* f = S->f;
-    std::vector<SrvReq*> act;
-    bool changed = false;
-    for (;;) {
-        {
-            std::unique_lock<std::mutex> lk(S->mu);
-            while (!S->stop && S->queue.empty() && act.empty()) S->cv.wait(lk);
-            if (S->stop) break;
-            while (!S->queue.empty() && act.size() < S->desc.max_slots &&
-                   S->used_bytes + S->queue.front()->bytes <= S->desc.hbm_budget_bytes) {
-                SrvReq* q = S->queue.front();
-                S->queue.pop_front();
-                q->state = 1;
-                q->t_admit = Clock::now();
-                q->fresh = true;
-                S->used_bytes += q->bytes;
-                act.push_back(q);
-                changed = true;
-            }
-            S->active = act;
-            S->max_active = std::max<uint64_t>(S->max_active, act.size());
-        }
-        if (act.empty()) continue;
-        const auto t0 = Clock::now();
-        kb_status st = KB_OK;
-        if (changed) st = srv_repack(S, act);
-        changed = false;
-        uint32_t K = S->desc.quantum_steps ? S->desc.quantum_steps : 100;
-        for (SrvReq* q : act) K = std::min(K, q->remaining);
-        if (!st) {
-            st = launch_set_u64(f->dstep.p, S->global_step, f->stream) ? fail(KB_ERR_CUDA, "step") : KB_OK;
-            f->dstep_host = ~0ull;
-        }
-        if (!st && K > 0) {
-            if (fused_eligible(f, &S->common)) {
-                st = tiled_steps(f, &S->common, K);
-            } else {
-                if (!(st = materialize(f))) st = enqueue_steps(f, &S->common, K, all_fast_rebin_ok(f));
-            }
-            S->launches++;
-        }
-        if (st) {
-            srv_fail_all(S, act, g_last_error);
-            changed = true;
-            continue;
-        }
-        S->global_step += K;
-        double upd = 0.0;
-        for (SrvReq* q : act) {
-            q->remaining -= K;
-            upd += (double)q->r.nboids * K;
-        }
-        // copy out the finished requests
-        bool any_done = false;
-        for (SrvReq* q : act) any_done |= (q->remaining == 0);
-        if (any_done) {
-            if (!(st = materialize(f))) {
-                std::vector<uint32_t> lohi(2 * act.size());
-                for (size_t i = 0; i < act.size(); ++i) {
-                    if (act[i]->remaining) continue;
-                    const Rep& R = act[i]->geom;
-                    cudaMemcpyAsync(&lohi[2 * i], f->start[f->cur].p + R.cell_off, 4, cudaMemcpyDeviceToHost, f->stream);
-                    cudaMemcpyAsync(&lohi[2 * i + 1], f->start[f->cur].p + R.cell_off + R.ncells, 4, cudaMemcpyDeviceToHost, f->stream);
-                }
-                if (cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
-                for (size_t i = 0; i < act.size() && !st; ++i) {
-                    SrvReq* q = act[i];
-                    if (q->remaining) continue;
-                    const uint32_t lo = lohi[2 * i], n = lohi[2 * i + 1] - lohi[2 * i];
-                    q->ids.resize(n);
-                    q->st.resize((size_t)n * 4);
-                    if (n) {
-                        cudaMemcpyAsync(q->ids.data(), f->rid.p + lo, 4ull * n, cudaMemcpyDeviceToHost, f->stream);
-                        cudaMemcpyAsync(q->st.data(), f->rst.p + lo, 16ull * n, cudaMemcpyDeviceToHost, f->stream);
-                    }
-                }
-                if (!st && cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
-                uint32_t flags = 0;
-                if (!st) {
-                    cudaMemcpy(&flags, f->err.p, 4, cudaMemcpyDeviceToHost);
-                    if (flags) st = fail(KB_ERR_DEVICE_FLAG, "device error word set during serving");
-                }
-            }
-            if (st) {
-                srv_fail_all(S, act, g_last_error);
-                changed = true;
-                continue;
-            }
-        }
-        const auto t1 = Clock::now();
-        {
-            std::lock_guard<std::mutex> lk(S->mu);
-            S->busy_s += std::chrono::duration<double>(t1 - t0).count();
-            S->updates += upd;
-            std::vector<SrvReq*> keep;
-            for (SrvReq* q : act) {
-                if (q->remaining == 0) {
-                    q->state = 2;
-                    q->t_done = t1;
-                    S->used_bytes -= q->bytes;
-                    S->latencies.push_back(std::chrono::duration<double>(q->t_done - q->t_arrive).count());
-                    S->completed++;
-                    S->t_last = t1;
-                    changed = true;
-                } else {
-                    keep.push_back(q);
-                }
-            }
-            act.swap(keep);
-            S->active = act;
-            if (changed) S->cv_done.notify_all();
-        }
-    }
-}
-
-}  // namespace
-
-extern "C" {
-
-kb_status kb_server_create(const kb_server_desc* desc, kb_server** out) {
-    if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
-    if (desc->max_slots == 0 || desc->max_request_boids == 0)
-        return fail(KB_ERR_ARG, "max_slots and max_request_boids must be positive");
-    *out = nullptr;
-    kb_flock_params p{};
-    p.query_mode = desc->query_mode;
-    p.arith = desc->arith;
-    p.jump = 0.5f;
-    p.neighbor_radius = 1.0f;
-    std::string why;
-    if (!params_ok(&p, &why)) return fail(KB_ERR_ARG, why);
-    const uint64_t cap = (uint64_t)desc->max_slots * desc->max_request_boids;
-    const uint64_t cells = (uint64_t)desc->max_slots * desc->max_request_cells;
-    if (cap > 0xF0000000ull || cells > 0xF0000000ull) return fail(KB_ERR_ARG, "capacity too large");
-    Rep R;
-    if (!make_rep_geometry(16.0f, 16.0f, 4.0f, 1, &R, &why)) return fail(KB_ERR_ARG, why);
-    kb_field* f = nullptr;
-    kb_status st = field_new(desc->device, std::vector<Rep>{R}, true, (uint32_t)cap, &f,
-                             (uint32_t)std::max<uint64_t>(cells, R.ncells));
-    if (st) return st;
-    kb_server* S = new kb_server();
-    S->desc = *desc;
-    S->f = f;
-    S->common = p;
-    S->loop = std::thread(srv_loop, S);
-    *out = S;
-    return KB_OK;
-}
-
-kb_status kb_server_destroy(kb_server* S) {
-    if (!S) return KB_OK;
-    {
-        std::lock_guard<std::mutex> lk(S->mu);
-        S->stop = true;
-    }
-    S->cv.notify_all();
-    if (S->loop.joinable()) S->loop.join();
-    {
-        DeviceGuard g(S->f->device);
-        cudaStreamSynchronize(S->f->stream);
-        delete S->f;
-    }
-    for (auto& kv : S->all) delete kv.second;
-    delete S;
-    return KB_OK;
-}
-
-kb_status kb_server_submit(kb_server* S, const kb_request* r, uint64_t* ticket) {
-    if (!S || !r || !ticket) return fail(KB_ERR_ARG, "null argument");
-    std::string why;
-    if (!params_ok(&r->params, &why)) return fail(KB_ERR_ARG, why);
-    if (r->params.query_mode != S->desc.query_mode || r->params.arith != S->desc.arith)
-        return fail(KB_ERR_ARG, "request query_mode/arith differ from the server's");
-    if (r->nboids == 0 || r->nboids > S->desc.max_request_boids || r->steps == 0)
-        return fail(KB_ERR_ARG, "request size out of range");
-    SrvReq* q = new SrvReq();
-    q->r = *r;
-    if (!make_rep_geometry(r->side, r->side, r->discretization, 1, &q->geom, &why)) {
-        delete q;
-        return fail(KB_ERR_ARG, why);
-    }
-    if (q->geom.ncells > S->desc.max_request_cells) {
-        delete q;
-        return fail(KB_ERR_ARG, "request bag matrix above max_request_cells");
-    }
-    set_rep_params(&q->geom, &r->params);
-    q->bytes = request_bytes(q->geom, r->nboids);
-    if (q->bytes > S->desc.hbm_budget_bytes) {
-        delete q;
-        return fail(KB_ERR_BUSY, "request larger than the whole HBM budget");
-    }
-    q->remaining = r->steps;
-    q->t_arrive = Clock::now();
-    {
-        std::lock_guard<std::mutex> lk(S->mu);
-        q->ticket = S->next_ticket++;
-        S->all[q->ticket] = q;
-        S->queue.push_back(q);
-        if (!S->any) {
-            S->any = true;
-            S->t_first = q->t_arrive;
-        }
-    }
-    S->cv.notify_all();
-    *ticket = q->ticket;
-    return KB_OK;
-}
-
-kb_status kb_server_poll(kb_server* S, uint64_t ticket, int32_t* state, double* latency_s) {
-    if (!S || !state) return fail(KB_ERR_ARG, "null argument");
-    std::lock_guard<std::mutex> lk(S->mu);
-    auto it = S->all.find(ticket);
-    if (it == S->all.end()) return fail(KB_ERR_ARG, "unknown ticket");
-    *state = it->second->state;
-    if (latency_s)
-        *latency_s = it->second->state >= 2
-                         ? std::chrono::duration<double>(it->second->t_done - it->second->t_arrive).count()
-                         : 0.0;
-    if (it->second->state == 3) return fail(KB_ERR_STATE, it->second->error);
-    return KB_OK;
-}
-
-kb_status kb_server_result(kb_server* S, uint64_t ticket, uint32_t* ids, float* states, size_t cap,
-                           size_t* n) {
-    if (!S || !n) return fail(KB_ERR_ARG, "null argument");
-    std::lock_guard<std::mutex> lk(S->mu);
-    auto it = S->all.find(ticket);
-    if (it == S->all.end()) return fail(KB_ERR_ARG, "unknown ticket");
-    SrvReq* q = it->second;
-    if (q->state != 2) return fail(KB_ERR_STATE, q->state == 3 ? q->error : "request not finished");
-    *n = q->ids.size();
-    const size_t take = std::min(cap, q->ids.size());
-    if (ids && take) std::memcpy(ids, q->ids.data(), 4 * take);
-    if (states && take) std::memcpy(states, q->st.data(), 16 * take);
-    return KB_OK;
-}
-
-kb_status kb_server_release(kb_server* S, uint64_t ticket) {
-    if (!S) return fail(KB_ERR_ARG, "null argument");
-    std::lock_guard<std::mutex> lk(S->mu);
-    auto it = S->all.find(ticket);
-    if (it == S->all.end()) return fail(KB_ERR_ARG, "unknown ticket");
-    if (it->second->state < 2) return fail(KB_ERR_STATE, "request still queued or running");
-    delete it->second;
-    S->all.erase(it);
-    return KB_OK;
-}
-
-kb_status kb_server_wait_idle(kb_server* S, double timeout_s) {
-    if (!S) return fail(KB_ERR_ARG, "null argument");
-    std::unique_lock<std::mutex> lk(S->mu);
-    const auto until = Clock::now() + std::chrono::duration<double>(timeout_s);
-    while (!(S->queue.empty() && S->active.empty())) {
-        if (S->cv_done.wait_until(lk, until) == std::cv_status::timeout &&
-            !(S->queue.empty() && S->active.empty()))
-            return fail(KB_ERR_TIMEOUT, "requests still pending");
-    }
-    return KB_OK;
-}
-
-kb_status kb_server_stats(kb_server* S, kb_server_report* out) {
-    if (!S || !out) return fail(KB_ERR_ARG, "null argument");
-    std::lock_guard<std::mutex> lk(S->mu);
-    std::vector<double> v = S->latencies;
-    std::sort(v.begin(), v.end());
-    auto pct = [&](double p) {
-        if (v.empty()) return 0.0;
-        const size_t i = (size_t)std::min<double>(v.size() - 1, std::ceil(p * v.size()) - 1);
-        return v[i];
-    };
-    std::memset(out, 0, sizeof(*out));
-    out->completed = S->completed;
-    out->failed = S->failed;
-    out->queued = S->queue.size();
-    out->running = S->active.size();
-    out->p50_s = pct(0.50);
-    out->p99_s = pct(0.99);
-    out->max_s = v.empty() ? 0.0 : v.back();
-    out->boid_updates = S->updates;
-    out->wall_s = S->any && S->completed ? std::chrono::duration<double>(S->t_last - S->t_first).count() : 0.0;
-    out->busy_s = S->busy_s;
-    out->launches = S->launches;
-    out->repacks = S->repacks;
-    out->max_active = S->max_active;
-    return KB_OK;
 }
 
 }  // extern "C"
