@@ -230,7 +230,11 @@ void srv_loop(kb_server* S) {
                 uint32_t flags = 0;
                 if (!st) {
                     cudaMemcpy(&flags, f->err.p, 4, cudaMemcpyDeviceToHost);
-                    if (flags) st = fail(KB_ERR_DEVICE_FLAG, "device error word set during serving");
+                    if (flags) {
+                        st = fail(KB_ERR_DEVICE_FLAG, "device error word set during serving");
+                        // the word belongs to the failed batch: later requests start clean
+                        cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream);
+                    }
                 }
             }
             if (st) {
