@@ -32,8 +32,13 @@ struct kb_batch {
         int cur, a_last;
     };
     std::map<GKey, GVal> graphs;
-    ~kb_batch() {
+    uint64_t graph_epoch = 0;  // the field's graph_epoch when `graphs` were captured
+    void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+    }
+    ~kb_batch() {
+        drop_graphs();
         if (f) {
             cudaStreamSynchronize(f->stream);
             delete f;
@@ -149,6 +154,10 @@ kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint3
     }
     if ((st = grow(f, f->rn))) return st;
     if ((st = fused_prepare(f, p))) return st;
+    if (b->graph_epoch != f->graph_epoch) {  // captured over buffers or a tile shape since replaced
+        b->drop_graphs();
+        b->graph_epoch = f->graph_epoch;
+    }
     if (f->fused_mode == 2)  // split: two launches per step, graphs of graph_launches steps
         return split_steps_graphed(f, p, nsteps, graph_launches > 1 ? graph_launches : 100);
     const uint32_t spl = steps_per_launch == 0 ? nsteps : std::min(steps_per_launch, nsteps);
@@ -334,8 +343,7 @@ static kb_status batch_repack(kb_batch* b, std::vector<Rep> reps, const std::vec
     f->layout_is_positions = true;
     if ((st = check_unique_ids(f))) return st;
     b->have.assign(reps.size(), 1);
-    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second.exec);
-    b->graphs.clear();
+    b->drop_graphs();
     return check_flags(f);
 }
 

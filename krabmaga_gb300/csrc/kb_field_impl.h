@@ -90,6 +90,10 @@ struct kb_field {
         int cur, a_last;
     };
     std::map<std::vector<uint32_t>, SGraph> sgraphs;
+    // Bumped whenever the graphs above are dropped (buffers reallocated, the
+    // fused configuration rebuilt): graphs cached outside the field over its
+    // buffers (a batch's) are stale once it moves.
+    uint64_t graph_epoch = 0;
     // persistent fused step (kb_fused.cu)
     struct Fused {
         bool ready = false;
@@ -154,6 +158,7 @@ struct kb_field {
         if (stream) cudaStreamDestroy(stream);
     }
     void drop_graphs() {
+        graph_epoch++;
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         graphs.clear();
         for (auto& kv : sgraphs) cudaGraphExecDestroy(kv.second.exec);

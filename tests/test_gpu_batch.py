@@ -49,6 +49,24 @@ def test_batch_replicas_match_oracle(gpu, grouping, mode):
         assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_graphs_follow_a_tile_change(gpu, mode):
+    # graphs replayed before a tile change are not replayed after it: the
+    # change rebuilds the tile table, and the next steps capture new graphs
+    reps = small_sweep(kg.KB_ARITH_STRICT)[:4]
+    b = kg.Batch(reps)
+    b.set_step_options(mode, 4, 4)
+    b.step(0, 8, 1, 4)
+    assert b.step_stats()["tile"] == (4, 4)
+    b.set_step_options(mode, 16, 8)
+    b.step(8, 8, 1, 4)
+    assert b.step_stats()["tile"] == (16, 8)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 16)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
 def test_batch_exact_query_matches_oracle(gpu):
     reps = small_sweep(kg.KB_ARITH_STRICT, kg.KB_QUERY_EXACT)[:4]
     b = kg.Batch(reps)
