@@ -7,7 +7,8 @@ reference's API names (Field2D, State, Schedule, simulate, Flocker).
 from . import _lib
 from ._lib import KbError, lib, LIB_PATH, KB_QUERY_RELAX, KB_QUERY_EXACT, KB_ARITH_STRICT, KB_ARITH_FAST
 from ._lib import (KB_CELL_WRAP_CLAMP, KB_CELL_WRAP_TORUS, KB_DENSE_AUTO, KB_DENSE_OFF, KB_DENSE_ON,
-                   KB_PATH_DENSE, KB_PATH_FUSED, KB_PATH_SEPARATE, KB_PATH_SMALL, KB_PATH_TILED)
+                   KB_PATH_DENSE, KB_PATH_FUSED, KB_PATH_SEPARATE, KB_PATH_SMALL, KB_PATH_TILED,
+                   KB_FLAG_KEY_RANGE, KB_FLAG_REBIN_MISS, KB_FLAG_SPIN_TIMEOUT, KB_FLAG_NONFINITE)
 from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
@@ -24,6 +25,7 @@ __all__ = [
     "KB_QUERY_RELAX", "KB_QUERY_EXACT", "KB_ARITH_STRICT", "KB_ARITH_FAST", "device_count",
     "KB_CELL_WRAP_CLAMP", "KB_CELL_WRAP_TORUS", "KB_DENSE_AUTO", "KB_DENSE_OFF", "KB_DENSE_ON",
     "KB_PATH_SEPARATE", "KB_PATH_FUSED", "KB_PATH_TILED", "KB_PATH_SMALL", "KB_PATH_DENSE",
+    "KB_FLAG_KEY_RANGE", "KB_FLAG_REBIN_MISS", "KB_FLAG_SPIN_TIMEOUT", "KB_FLAG_NONFINITE",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
     "ExploreMode", "FlockerConfig", "build_configurations", "explore", "random_search",
     "evolutionary_search", "write_csv", "bayesian_search", "flock_objective", "gen_param",

@@ -23,6 +23,11 @@ KB_ERR_RANGE = 7
 KB_ERR_NO_DEVICE = 8
 KB_ERR_BUSY = 9
 
+KB_FLAG_KEY_RANGE = 0x1
+KB_FLAG_REBIN_MISS = 0x2
+KB_FLAG_SPIN_TIMEOUT = 0x4
+KB_FLAG_NONFINITE = 0x8
+
 KB_QUERY_RELAX = 0
 KB_QUERY_EXACT = 1
 KB_ARITH_STRICT = 0

@@ -1,0 +1,76 @@
+"""The Python mirror's view of the C ABI equals the header's: every
+constant `include/krabgpu.h` defines has the same value in `_lib`, and every
+public struct has the same size and field offsets as `ctypes` lays it out.
+The header is compiled as plain C by the host compiler (no GPU needed)."""
+import ctypes as C
+import json
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from krabmaga_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "krabgpu.h")
+
+STRUCTS = {
+    "kb_field_desc": L.FieldDesc,
+    "kb_flock_params": L.FlockParamsC,
+    "kb_replica_desc": L.ReplicaDesc,
+    "kb_server_desc": L.ServerDesc,
+    "kb_request": L.RequestC,
+    "kb_server_report": L.ServerReport,
+}
+
+
+def header_constants():
+    out = {}
+    for m in re.finditer(r"^#define\s+(KB_[A-Z0-9_]+)\s+(0x[0-9a-fA-F]+|\d+)u?\b", open(HEADER).read(), re.M):
+        out[m.group(1)] = int(m.group(2), 0)
+    return out
+
+
+def test_every_header_constant_is_mirrored():
+    consts = header_constants()
+    assert len(consts) >= 25
+    for name, value in consts.items():
+        assert getattr(L, name, None) == value, name
+
+
+@pytest.fixture(scope="module")
+def c_layout(tmp_path_factory):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    d = tmp_path_factory.mktemp("abi")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "krabgpu.h"', "int main(void) {",
+             '  printf("{");']
+    first = True
+    for sname, cls in STRUCTS.items():
+        parts = [f'\\"size\\": %zu']
+        args = [f"sizeof({sname})"]
+        for fname, _ in cls._fields_:
+            parts.append(f'\\"{fname}\\": %zu')
+            args.append(f"offsetof({sname}, {fname})")
+        sep = "" if first else ", "
+        first = False
+        lines.append(f'  printf("{sep}\\"{sname}\\": {{{", ".join(parts)}}}", {", ".join(args)});')
+    lines += ['  printf("}\\n");', "  return 0;", "}"]
+    src = d / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = d / "layout"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    return json.loads(subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout)
+
+
+@pytest.mark.parametrize("sname", sorted(STRUCTS))
+def test_struct_layout_matches_ctypes(c_layout, sname):
+    cls = STRUCTS[sname]
+    got = c_layout[sname]
+    assert got["size"] == C.sizeof(cls), sname
+    for fname, _ in cls._fields_:
+        assert got[fname] == getattr(cls, fname).offset, (sname, fname)
