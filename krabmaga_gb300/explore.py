@@ -186,6 +186,18 @@ def write_csv(name: str, rows: Sequence[dict]) -> str:
     return path
 
 
+def _run_batch(replicas: List[Replica], nstep: int, device: int) -> np.ndarray:
+    """Run every replica nstep steps as one device batch (CUDA graphs of
+    100 steps) and return their heading moments, one row per replica: the
+    one device call of each search iteration, generation or evaluation."""
+    b = Batch(replicas, device=device)
+    try:
+        b.step(0, nstep, 1, 100)
+        return b.moments()
+    finally:
+        b.close()
+
+
 def _observables(m: np.ndarray) -> dict:
     return {name: fn(m) for name, fn in OUTPUTS.items()}
 
@@ -216,12 +228,7 @@ def random_search(init: FlockerConfig, n_iter: int, target: float,
             for _ in range(int(reps)):
                 reps_list.append(_replica(smp, init.init_seed + run))
                 run += 1
-        b = Batch(reps_list, device=device)
-        try:
-            b.step(0, int(step), 1, 100)
-            mom = b.moments()
-        finally:
-            b.close()
+        mom = _run_batch(reps_list, int(step), device)
         costs = [float(np.mean([cost_function(_observables(mom[i * reps + r])) for r in range(reps)]))
                  for i in range(len(samples))]
         k = int(np.argmin(costs))
@@ -267,12 +274,7 @@ def evolutionary_search(init_population: Callable[[], List],
             for r in range(int(reps)):
                 reps_list.append(_replica(make_config(ind, r), init_seed + run))
                 run += 1
-        b = Batch(reps_list, device=device)
-        try:
-            b.step(0, int(step), 1, 100)
-            mom = b.moments()
-        finally:
-            b.close()
+        mom = _run_batch(reps_list, int(step), device)
         pop_fitness = []
         reached = False
         for i, ind in enumerate(population):
@@ -438,12 +440,7 @@ def flock_objective(base: FlockerConfig, names: Sequence[str],
         for _ in range(int(reps)):
             reps_list.append(_replica(cfg, init_seed + counter[0]))
             counter[0] += 1
-        b = Batch(reps_list, device=device)
-        try:
-            b.step(0, int(step), 1, 100)
-            mom = b.moments()
-        finally:
-            b.close()
+        mom = _run_batch(reps_list, int(step), device)
         return float(value_of([_observables(mom[r]) for r in range(int(reps))]))
 
     return f

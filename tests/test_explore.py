@@ -145,3 +145,119 @@ def test_load_csv_columns_by_position(tmp_path):
     p.write_text("cohesion,jump,n\n0.5,0.7,100\n1.5,0.9,200\n")
     coh, jump, n = ex.load_csv(str(p), ("cohesion", float), ("jump", float), ("n", int))
     assert coh == [0.5, 1.5] and jump == [0.7, 0.9] and n == [100, 200]
+
+
+# ---------------------------------------------------------------- search loops
+# The drivers' host loops against the reference's, with the device batch
+# replaced by a fake: each run's moments row is a function of its replica's
+# parameters and seed ({boids, n*jump, 0, n*jump}: order 1, mean_speed jump).
+class FakeRunner:
+    def __init__(self):
+        self.calls = []  # one list of (jump, cohesion, seed) per device batch
+
+    def __call__(self, replicas, nstep, device):
+        import numpy as np
+        self.calls.append([(r.params.jump, r.params.cohesion, r.params.seed) for r in replicas])
+        rows = []
+        for r in replicas:
+            n = float(r.state[0].shape[0])
+            rows.append([n, n * r.params.jump, 0.0, n * r.params.jump])
+        return np.array(rows, np.float64)
+
+
+@pytest.fixture
+def fake_runner(monkeypatch):
+    fake = FakeRunner()
+    monkeypatch.setattr(ex, "_run_batch", fake)
+    return fake
+
+
+def test_random_search_loop_as_the_macro(fake_runner):
+    # random_search.rs:44-118: batch_size samples from the best so far, each
+    # run reps times; the mean cost per sample; keep the lowest; stop at target
+    import numpy as np
+    base = kg.FlockerConfig(initial_flockers=40, dim=30.0, init_seed=100)
+    jumps = iter([0.9, 0.8, 0.95, 0.61, 0.7, 0.59, 0.9, 0.9, 0.9])
+
+    def gen(best, rng):
+        return ex._apply(best, "jump", next(jumps))
+
+    def cost(obs):
+        return abs(obs["mean_speed"] - 0.6)
+
+    best, c, hist = kg.random_search(base, 5, 0.015, cost, gen, batch_size=3, step=7, reps=2)
+    # iteration 1: best 0.8 (0.2); iteration 2: 0.61 (0.01 <= target): stop
+    assert len(fake_runner.calls) == 2 and len(hist) == 2
+    assert best.params.jump == 0.61 and c == pytest.approx(0.01, abs=1e-6)
+    assert hist[0] == pytest.approx(0.2, abs=1e-6) and hist[1] == c
+    # one device batch per iteration, batch_size * reps runs; run k seeded init_seed + k
+    seeds = [s for call in fake_runner.calls for (_, _, s) in call]
+    assert seeds == list(range(100, 100 + 12))
+    assert [j for (j, _, _) in fake_runner.calls[0]] == [0.9, 0.9, 0.8, 0.8, 0.95, 0.95]
+    # an unreachable target runs every iteration and the history never rises
+    jumps = iter(np.linspace(1.0, 0.3, 12).tolist())
+    _, _, hist = kg.random_search(base, 4, -1.0, cost, gen, batch_size=3, step=7, reps=1)
+    assert len(hist) == 4 and all(b <= a for a, b in zip(hist, hist[1:]))
+
+
+def _ga(fake_runner, desired, generations, survivors=2):
+    base = kg.FlockerConfig(initial_flockers=30, dim=25.0, init_seed=5)
+    log = []
+
+    def init_population():
+        return [0.3, 0.5, 0.7, 0.9]
+
+    def make_config(ind, r):
+        return ex._apply(base, "jump", ind)
+
+    def fitness(obs):
+        return float(sum(o["mean_speed"] for o in obs) / len(obs))
+
+    def selection(pop):
+        log.append(("selection", [i for i, _ in pop]))
+        pop.sort(key=lambda t: -t[1])
+        del pop[survivors:]
+
+    def crossover(population):
+        log.append(("crossover", list(population)))
+        population.append(round((population[0] + population[-1]) / 2, 6) if population else 0.0)
+
+    def mutation(ind):
+        log.append(("mutation", ind))
+        return round(min(1.0, ind + 0.01), 6)
+
+    rows = kg.evolutionary_search(init_population, make_config, fitness, selection, mutation,
+                                  crossover, lambda a, b: a >= b, desired, generations, step=3,
+                                  reps=2, init_seed=base.init_seed)
+    return rows, log
+
+
+def test_evolutionary_search_loop_as_the_macro(fake_runner):
+    # genetic.rs:626-826: evaluate, stop on the desired fitness, else
+    # selection, crossover of the survivors, then mutation of every individual
+    rows, log = _ga(fake_runner, 5.0, 3)
+    assert [r["generation"] for r in rows] == [1] * 4 + [2] * 3 + [3] * 3
+    assert [r["index"] for r in rows] == [0, 1, 2, 3, 0, 1, 2, 0, 1, 2]
+    assert [r["individual"] for r in rows[:4]] == [0.3, 0.5, 0.7, 0.9]
+    assert [r["fitness"] for r in rows[:4]] == pytest.approx([0.3, 0.5, 0.7, 0.9], abs=1e-6)
+    # selection keeps the two fittest; crossover appends their mean; each is mutated
+    assert log[0] == ("selection", [0.3, 0.5, 0.7, 0.9])
+    assert log[1] == ("crossover", [0.9, 0.7])
+    assert [e for e in log[2:5]] == [("mutation", 0.9), ("mutation", 0.7), ("mutation", 0.8)]
+    assert [r["individual"] for r in rows[4:7]] == [0.91, 0.71, 0.81]
+    # the generation limit is checked at the top of the loop (genetic.rs:674-678), so
+    # selection runs after the last generation too; runs seeded init_seed + k in order
+    assert sum(1 for e in log if e[0] == "selection") == 3
+    seeds = [s for call in fake_runner.calls for (_, _, s) in call]
+    assert seeds == list(range(5, 5 + 2 * 10))
+
+
+def test_evolutionary_search_stops_on_the_desired_fitness(fake_runner):
+    rows, log = _ga(fake_runner, 0.85, 0)  # generation_num 0: no limit
+    assert {r["generation"] for r in rows} == {1} and len(rows) == 4 and log == []
+
+
+def test_evolutionary_search_stops_when_selection_empties_the_population(fake_runner):
+    rows, log = _ga(fake_runner, 5.0, 4, survivors=0)
+    assert {r["generation"] for r in rows} == {1}
+    assert [e[0] for e in log] == ["selection"]
