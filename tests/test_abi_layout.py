@@ -74,3 +74,26 @@ def test_struct_layout_matches_ctypes(c_layout, sname):
     assert got["size"] == C.sizeof(cls), sname
     for fname, _ in cls._fields_:
         assert got[fname] == getattr(cls, fname).offset, (sname, fname)
+
+
+def _header_arities():
+    h = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(kb_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", h):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_rust_binding_covers_the_header():
+    # the extern "C" blocks a maintainer would add to the reference's crate name
+    # every entry point of the header, each with the header's parameter count
+    hdr = _header_arities()
+    md = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    bound = {}
+    for m in re.finditer(r"pub fn (kb_[a-z0-9_]+)\s*\(([^;]*?)\)\s*(->[^;]*)?;", md, flags=re.S):
+        args = re.sub(r"//[^\n]*", "", m.group(2)).strip().rstrip(",")
+        bound[m.group(1)] = 0 if not args else args.count(",") + 1
+    assert set(bound) == set(hdr), (set(hdr) - set(bound), set(bound) - set(hdr))
+    for name, n in bound.items():
+        assert hdr[name] == n, name
