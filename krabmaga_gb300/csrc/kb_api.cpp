@@ -1488,6 +1488,10 @@ kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_s
         cand = defaults;
         ncand = (int32_t)(sizeof(defaults) / sizeof(defaults[0]) / 2);
     }
+    for (int32_t i = 0; i < ncand; ++i)  // the bounds of kb_field_set_step_options
+        if (cand[2 * i] < 0 || cand[2 * i + 1] < 0 || cand[2 * i] > 64 || cand[2 * i + 1] > 128)
+            return fail(KB_ERR_ARG, "candidate " + std::to_string(i) +
+                                        ": tile shape out of range (tx <= 64, ty <= 128)");
     cudaEvent_t e0, e1;
     KB_CUDA(cudaEventCreate(&e0));
     KB_CUDA(cudaEventCreate(&e1));
@@ -1543,6 +1547,8 @@ kb_status kb_field_autotune(kb_field* f, const kb_flock_params* p, uint64_t firs
                             uint32_t steps_per_trial, const int32_t* candidates, int32_t ncand,
                             int32_t best[3], float* ms_per_step) {
     if (!f || !p || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
+    std::string why;
+    if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
     DeviceGuard g(f->device);
     set_rep_params(&f->rep, p);
     f->reps[0] = f->rep;

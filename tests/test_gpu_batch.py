@@ -67,6 +67,22 @@ def test_batch_graphs_follow_a_tile_change(gpu, mode):
         assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
 
 
+def test_batch_autotune_refuses_tiles_out_of_range(gpu):
+    # candidates obey the bounds of set_step_options; a refused call runs no step
+    reps = small_sweep(kg.KB_ARITH_STRICT)[:3]
+    b = kg.Batch(reps)
+    b.set_step_options(1)
+    for bad in [(8, 16), (65, 8)], [(4, 129)], [(-1, 8)]:
+        with pytest.raises(kg.KbError) as e:
+            b.autotune(0, 2, candidates=bad)
+        assert e.value.status == L.KB_ERR_ARG
+    b.step(0, 6, 1, 0)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, 6)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
 def test_batch_exact_query_matches_oracle(gpu):
     reps = small_sweep(kg.KB_ARITH_STRICT, kg.KB_QUERY_EXACT)[:4]
     b = kg.Batch(reps)
