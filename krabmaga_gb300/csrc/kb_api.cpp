@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <utility>
 #include <vector>
@@ -21,6 +23,31 @@ thread_local std::string g_last_error;
 kb_status fail(kb_status code, const std::string& msg) {
     g_last_error = msg;
     return code;
+}
+// Set the message without letting an allocation failure escape.
+static void note_error(const char* head, const char* what) noexcept {
+    try {
+        g_last_error = std::string(head) + what;
+    } catch (...) {
+        g_last_error.clear();
+    }
+}
+kb_status exception_status() noexcept {
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        note_error("host allocation failed", "");
+        return KB_ERR_OOM;
+    } catch (const std::length_error& e) {
+        note_error("host allocation too large: ", e.what());
+        return KB_ERR_OOM;
+    } catch (const std::exception& e) {
+        note_error("host exception: ", e.what());
+        return KB_ERR_STATE;
+    } catch (...) {
+        note_error("unknown host exception", "");
+        return KB_ERR_STATE;
+    }
 }
 kb_status cuda_fail(cudaError_t e, const char* what) {
     std::string m = std::string(what) + ": " + cudaGetErrorString(e);
@@ -998,7 +1025,7 @@ kb_status field_query_view(kb_field* f, int32_t kind, float dist, QueryArgs* a, 
 
 extern "C" {
 
-kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
+kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) try {
     if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
     *out = nullptr;
     Rep R;
@@ -1007,33 +1034,41 @@ kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) {
                            desc->cell_wrap))
         return fail(KB_ERR_ARG, why);
     return field_new(desc->device, std::vector<Rep>{R}, false, desc->capacity_hint, out);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_destroy(kb_field* f) {
+kb_status kb_field_destroy(kb_field* f) try {
     if (!f) return KB_OK;
     DeviceGuard g(f->device);
     cudaStreamSynchronize(f->stream);
     delete f;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_dims(const kb_field* f, int32_t out4[4]) {
+kb_status kb_field_dims(const kb_field* f, int32_t out4[4]) try {
     if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
     out4[0] = f->rep.dw;
     out4[1] = f->rep.dh;
     out4[2] = f->rep.max_x;
     out4[3] = f->rep.max_y;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_cuda_stream(kb_field* f, void** stream) {
+kb_status kb_field_cuda_stream(kb_field* f, void** stream) try {
     if (!f || !stream) return fail(KB_ERR_ARG, "null argument");
     *stream = (void*)f->stream;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_set_object_location(kb_field* f, uint32_t id, const float pos[2],
-                                       const float last_d[2], const float loc[2]) {
+                                       const float last_d[2], const float loc[2]) try {
     if (!f || !pos || !last_d || !loc) return fail(KB_ERR_ARG, "null argument");
     if (!(std::isfinite(pos[0]) && std::isfinite(pos[1]) && std::isfinite(last_d[0]) &&
           std::isfinite(last_d[1]) && std::isfinite(loc[0]) && std::isfinite(loc[1])))
@@ -1047,10 +1082,12 @@ kb_status kb_field_set_object_location(kb_field* f, uint32_t id, const float pos
     if (!f->density_check) f->nagents += 1;
     f->w_from_compute = false;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_set_locations(kb_field* f, size_t n, const uint32_t* ids, const float* xy,
-                                 const float* dxy) {
+                                 const float* dxy) try {
     if (!f || (n && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
     if (n == 0) return KB_OK;
     if ((uint64_t)f->wn + f->p_id.size() + n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many objects");
@@ -1086,9 +1123,11 @@ kb_status kb_field_set_locations(kb_field* f, size_t n, const uint32_t* ids, con
     if (!f->density_check) f->nagents += n;
     f->w_from_compute = false;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float loc[2]) {
+kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float loc[2]) try {
     if (!f || !loc) return fail(KB_ERR_ARG, "null argument");
     int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
     if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
@@ -1105,24 +1144,32 @@ kb_status kb_field_remove_object_location(kb_field* f, uint32_t id, const float 
         if (!f->density_check) f->nagents -= removed;
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_lazy_update(kb_field* f) {
+kb_status kb_field_lazy_update(kb_field* f) try {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     return field_lazy_update(f);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_num_agents(kb_field* f, size_t* out) {
+kb_status kb_field_num_agents(kb_field* f, size_t* out) try {
     if (!f || !out) return fail(KB_ERR_ARG, "null argument");
     *out = f->nagents;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_num_objects(kb_field* f, size_t* out) {
+kb_status kb_field_num_objects(kb_field* f, size_t* out) try {
     if (!f || !out) return fail(KB_ERR_ARG, "null argument");
     *out = f->rn;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 static kb_status query_points(kb_field* f, int kind, float dist, size_t nq, const float* qxy,
@@ -1192,38 +1239,46 @@ static kb_status query_points(kb_field* f, int kind, float dist, size_t nq, cons
 
 kb_status kb_field_get_neighbors_within_relax_distance(kb_field* f, const float loc[2], float dist,
                                                        uint32_t* ids, float* states, size_t cap,
-                                                       size_t* n) {
+                                                       size_t* n) try {
     if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
     return query_points(f, KB_QUERY_RELAX, dist, 1, loc, nullptr, nullptr, ids, states, cap, n);
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_get_neighbors_within_distance(kb_field* f, const float loc[2], float dist,
                                                  uint32_t* ids, float* states, size_t cap,
-                                                 size_t* n) {
+                                                 size_t* n) try {
     if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
     return query_points(f, KB_QUERY_EXACT, dist, 1, loc, nullptr, nullptr, ids, states, cap, n);
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_neighbor_lists(kb_field* f, int32_t kind, float dist, size_t nq,
                                   const float* qxy, uint32_t* counts, uint32_t* ids, size_t cap,
-                                  size_t* total) {
+                                  size_t* total) try {
     if (!f || (nq && (!qxy || !counts))) return fail(KB_ERR_ARG, "null argument");
     if (kind != KB_QUERY_RELAX && kind != KB_QUERY_EXACT) return fail(KB_ERR_ARG, "bad query kind");
     size_t t = 0;
     kb_status st = query_points(f, kind, dist, nq, qxy, counts, nullptr, ids, nullptr, cap, &t);
     if (total) *total = t;
     return st;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_neighbor_digest(kb_field* f, int32_t kind, float dist, size_t nq,
-                                   const float* qxy, uint32_t* counts, uint32_t* digest) {
+                                   const float* qxy, uint32_t* counts, uint32_t* digest) try {
     if (!f || (nq && (!qxy || !counts || !digest))) return fail(KB_ERR_ARG, "null argument");
     if (kind != KB_QUERY_RELAX && kind != KB_QUERY_EXACT) return fail(KB_ERR_ARG, "bad query kind");
     return query_points(f, kind, dist, nq, qxy, counts, digest, nullptr, nullptr, 0, nullptr);
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_get_objects(kb_field* f, const float loc[2], uint32_t* ids, float* states,
-                               size_t cap, size_t* n) {
+                               size_t cap, size_t* n) try {
     if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
     int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
     if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
@@ -1243,10 +1298,12 @@ kb_status kb_field_get_objects(kb_field* f, const float loc[2], uint32_t* ids, f
         KB_CUDA(cudaStreamSynchronize(f->stream));
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_get_objects_unbuffered(kb_field* f, const float loc[2], uint32_t* ids,
-                                          float* states, size_t cap, size_t* n) {
+                                          float* states, size_t cap, size_t* n) try {
     if (!f || !loc || !n) return fail(KB_ERR_ARG, "null argument");
     int64_t idx = host_bag_index(f->rep, loc[0], loc[1]);
     if (idx < 0) return fail(KB_ERR_RANGE, "location outside the bag matrix (the reference panics)");
@@ -1272,13 +1329,17 @@ kb_status kb_field_get_objects_unbuffered(kb_field* f, const float loc[2], uint3
         KB_CUDA(cudaStreamSynchronize(f->stream));
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_num_objects_at_location(kb_field* f, const float loc[2], size_t* n) {
+kb_status kb_field_num_objects_at_location(kb_field* f, const float loc[2], size_t* n) try {
     return kb_field_get_objects(f, loc, nullptr, nullptr, 0, n);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_get_empty_bags(kb_field* f, float* xy, size_t cap, size_t* n) {
+kb_status kb_field_get_empty_bags(kb_field* f, float* xy, size_t cap, size_t* n) try {
     if (!f || !n || (cap && !xy)) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     DevBuf<float2> dxy;
@@ -1298,9 +1359,11 @@ kb_status kb_field_get_empty_bags(kb_field* f, float* xy, size_t cap, size_t* n)
         KB_CUDA(cudaStreamSynchronize(f->stream));
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_get_random_empty_bag(kb_field* f, uint64_t seed, float xy[2], int32_t* found) {
+kb_status kb_field_get_random_empty_bag(kb_field* f, uint64_t seed, float xy[2], int32_t* found) try {
     if (!f || !xy || !found) return fail(KB_ERR_ARG, "null argument");
     size_t n = 0;
     kb_status st = kb_field_get_empty_bags(f, nullptr, 0, &n);
@@ -1318,10 +1381,12 @@ kb_status kb_field_get_random_empty_bag(kb_field* f, uint64_t seed, float xy[2],
     xy[1] = all[2 * pick + 1];
     *found = 1;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, uint32_t* ids,
-                                float* states, size_t cap, size_t* n) {
+                                float* states, size_t cap, size_t* n) try {
     if (!f || !n) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     const float4* src_st;
@@ -1382,9 +1447,11 @@ kb_status kb_field_iter_objects(kb_field* f, int32_t buffered, float* cell_xy, u
     }
     KB_CUDA(cudaStreamSynchronize(f->stream));
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n) {
+kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n) try {
     if (!f || !n) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     if (kb_status st0 = materialize(f)) return st0;
@@ -1396,9 +1463,11 @@ kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t c
     }
     KB_CUDA(cudaStreamSynchronize(f->stream));
     return check_flags(f);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear) {
+kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear) try {
     if (!f || !flags) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     kb_status st = read_u32(f, f->err.p, flags);
@@ -1408,16 +1477,20 @@ kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear) {
         KB_CUDA(cudaStreamSynchronize(f->stream));
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_synchronize(kb_field* f) {
+kb_status kb_field_synchronize(kb_field* f) try {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     KB_CUDA(cudaStreamSynchronize(f->stream));
     return check_flags(f);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty) {
+kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx, int32_t tile_ty) try {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     if (tile_tx < 0 || tile_ty < 0 || tile_tx > 64 || tile_ty > 128)
         return fail(KB_ERR_ARG, "tile shape out of range (tx <= 64, ty <= 128)");
@@ -1427,9 +1500,11 @@ kb_status kb_field_set_step_options(kb_field* f, int32_t fused, int32_t tile_tx,
     f->tile_ty = tile_ty;
     f->fused.ready = false;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode) {
+kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode) try {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     if (mode != KB_DENSE_AUTO && mode != KB_DENSE_OFF && mode != KB_DENSE_ON)
         return fail(KB_ERR_ARG, "dense mode must be KB_DENSE_AUTO, KB_DENSE_OFF or KB_DENSE_ON");
@@ -1438,9 +1513,11 @@ kb_status kb_field_set_dense_mode(kb_field* f, int32_t mode) {
     set_dense(f, f->dense);
     if (mode == KB_DENSE_AUTO) f->steps_since_occ = DENSE_REFRESH;  // measure at the next step
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_step_path(kb_field* f, int32_t* path) {
+kb_status kb_field_step_path(kb_field* f, int32_t* path) try {
     if (!f || !path) return fail(KB_ERR_ARG, "null argument");
     occ_poll(f);
     kb_flock_params q{};
@@ -1449,16 +1526,20 @@ kb_status kb_field_step_path(kb_field* f, int32_t* path) {
     else if (small_eligible(f)) *path = KB_PATH_SMALL;
     else *path = f->dense ? KB_PATH_DENSE : KB_PATH_SEPARATE;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_dense_active(kb_field* f, int32_t* active) {
+kb_status kb_field_dense_active(kb_field* f, int32_t* active) try {
     if (!f || !active) return fail(KB_ERR_ARG, "null argument");
     occ_poll(f);
     *active = f->dense ? 1 : 0;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long* out16) {
+kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long* out16) try {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     f->fused.profile = enable != 0;
@@ -1473,6 +1554,8 @@ kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long*
         }
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 }  // extern "C"
@@ -1545,7 +1628,7 @@ static kb_status run_field_steps(void* ctx, uint64_t first, uint32_t n) {
 
 kb_status kb_field_autotune(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                             uint32_t steps_per_trial, const int32_t* candidates, int32_t ncand,
-                            int32_t best[3], float* ms_per_step) {
+                            int32_t best[3], float* ms_per_step) try {
     if (!f || !p || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
     std::string why;
     if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
@@ -1556,9 +1639,11 @@ kb_status kb_field_autotune(kb_field* f, const kb_flock_params* p, uint64_t firs
     FieldTuneCtx ctx{f, p};
     return autotune_tiles(f, p, first_step, steps_per_trial, candidates, ncand, best, ms_per_step,
                           run_field_steps, &ctx);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]) {
+kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]) try {
     if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     out4[0] = out4[1] = out4[2] = out4[3] = 0;
@@ -1570,9 +1655,11 @@ kb_status kb_field_step_stats(kb_field* f, uint32_t out4[4]) {
         out4[3] = (uint32_t)f->fused.cfg.tx << 16 | (uint32_t)f->fused.cfg.ty;
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step) {
+kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step) try {
     if (!f || !p) return fail(KB_ERR_ARG, "null argument");
     std::string why;
     if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
@@ -1591,10 +1678,12 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
     f->w_from_compute = true;
     f->w_has_dead = false;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_t step, size_t n,
-                                  const uint32_t* ids, const float* states) {
+                                  const uint32_t* ids, const float* states) try {
     if (!f || !p || (n && (!ids || !states))) return fail(KB_ERR_ARG, "null argument");
     if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: agents join a batch with kb_batch_add_replica");
     std::string why;
@@ -1640,10 +1729,12 @@ kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_
     f->w_from_compute = false;  // the write list is no longer one pass over the read buffer
     if (!f->density_check) f->nagents += m;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_field_get_locations(kb_field* f, int32_t buffered, size_t n, const uint32_t* ids,
-                                 float* states, int32_t* found) {
+                                 float* states, int32_t* found) try {
     if (!f || (n && (!ids || !states || !found))) return fail(KB_ERR_ARG, "null argument");
     if (n == 0) return KB_OK;
     if (n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many ids");
@@ -1677,9 +1768,11 @@ kb_status kb_field_get_locations(kb_field* f, int32_t buffered, size_t n, const 
         states[4 * q + 3] = out[j].w;
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t* removed) {
+kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t* removed) try {
     if (!f || (n && !ids)) return fail(KB_ERR_ARG, "null argument");
     if (removed) *removed = 0;
     if (n == 0) return KB_OK;
@@ -1705,6 +1798,8 @@ kb_status kb_field_remove_ids(kb_field* f, size_t n, const uint32_t* ids, size_t
     }
     if (removed) *removed = cnt;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 // Enqueue nsteps steps (force + rebuild) directly on the stream.
@@ -1860,13 +1955,15 @@ static kb_status flock_step_impl(kb_field* f, const kb_flock_params* p, uint64_t
     return KB_OK;
 }
 
-kb_status kb_field_set_kernel_timing(kb_field* f, int32_t enable) {
+kb_status kb_field_set_kernel_timing(kb_field* f, int32_t enable) try {
     if (!f) return fail(KB_ERR_ARG, "null argument");
     f->ktime = enable != 0;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_kernel_times(kb_field* f, double ms[3], uint64_t* steps) {
+kb_status kb_field_kernel_times(kb_field* f, double ms[3], uint64_t* steps) try {
     if (!f || !ms || !steps) return fail(KB_ERR_ARG, "null argument");
     DeviceGuard g(f->device);
     ms[0] = ms[1] = ms[2] = 0.0;
@@ -1887,13 +1984,17 @@ kb_status kb_field_kernel_times(kb_field* f, double ms[3], uint64_t* steps) {
     }
     f->kt_pending.clear();
     return st;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_flock_step(kb_field* f, const kb_flock_params* p, uint64_t first_step,
-                        uint32_t nsteps) {
+                        uint32_t nsteps) try {
     kb_status st = flock_step_impl(f, p, first_step, nsteps);
     if (f) f->dstep_host = st ? ~0ull : first_step + nsteps;  // unknown after a failure
     return st;
+} catch (...) {
+    return kb::exception_status();
 }
 
 }  // extern "C"

@@ -49,7 +49,7 @@ struct kb_batch {
 extern "C" {
 
 kb_status kb_batch_create(int32_t device, uint32_t nrep, const kb_replica_desc* reps,
-                          kb_batch** out) {
+                          kb_batch** out) try {
     if (!reps || !out || nrep == 0) return fail(KB_ERR_ARG, "null argument or no replicas");
     *out = nullptr;
     std::vector<Rep> table(nrep);
@@ -80,17 +80,21 @@ kb_status kb_batch_create(int32_t device, uint32_t nrep, const kb_replica_desc* 
     b->have.assign(nrep, 0);
     *out = b;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_batch_destroy(kb_batch* b) {
+kb_status kb_batch_destroy(kb_batch* b) try {
     if (!b) return KB_OK;
     DeviceGuard g(b->f->device);
     delete b;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_batch_set_replica(kb_batch* b, uint32_t r, size_t n, const uint32_t* ids,
-                               const float* xy, const float* dxy) {
+                               const float* xy, const float* dxy) try {
     if (!b || (n && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
     kb_field* f = b->f;
     if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
@@ -115,10 +119,12 @@ kb_status kb_batch_set_replica(kb_batch* b, uint32_t r, size_t n, const uint32_t
     }
     b->have[r] = 1;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 // Build the packed read buffer (every replica must be set).
-kb_status kb_batch_commit(kb_batch* b) {
+kb_status kb_batch_commit(kb_batch* b) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     for (size_t r = 0; r < b->have.size(); ++r)
         if (!b->have[r]) return fail(KB_ERR_STATE, "replica " + std::to_string(r) + " not set");
@@ -130,6 +136,8 @@ kb_status kb_batch_commit(kb_batch* b) {
     for (const Rep& R : f->reps) expect += R.nboids;
     if (f->rn != expect) return fail(KB_ERR_STATE, "packed boid count mismatch");
     return upload_rep(f);
+} catch (...) {
+    return kb::exception_status();
 }
 
 // nsteps steps of every replica, each replica with its own parameters.
@@ -137,7 +145,7 @@ kb_status kb_batch_commit(kb_batch* b) {
 // graph_launches > 1 that many launches are captured into one CUDA graph
 // and replayed.
 kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint32_t steps_per_launch,
-                        uint32_t graph_launches) {
+                        uint32_t graph_launches) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     kb_field* f = b->f;
     if (f->wn || !f->p_id.empty()) return fail(KB_ERR_STATE, "batch not committed");
@@ -203,6 +211,8 @@ kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint3
         }
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 
@@ -212,16 +222,18 @@ static kb_status run_batch_steps(void* ctx, uint64_t first, uint32_t n) {
 
 kb_status kb_batch_autotune(kb_batch* b, uint64_t first_step, uint32_t steps_per_trial,
                             const int32_t* candidates, int32_t ncand, int32_t best[3],
-                            float* ms_per_step) {
+                            float* ms_per_step) try {
     if (!b || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
     DeviceGuard g(b->f->device);
     if (!fused_eligible(b->f, &b->common)) return fail(KB_ERR_STATE, "batch not eligible for the fused step");
     return autotune_tiles(b->f, &b->common, first_step, steps_per_trial, candidates, ncand, best,
                           ms_per_step, run_batch_steps, b);
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* states, size_t cap,
-                               size_t* n) {
+                               size_t* n) try {
     if (!b || !n) return fail(KB_ERR_ARG, "null argument");
     kb_field* f = b->f;
     if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
@@ -241,6 +253,8 @@ kb_status kb_batch_get_replica(kb_batch* b, uint32_t r, uint32_t* ids, float* st
     }
     KB_CUDA(cudaStreamSynchronize(f->stream));
     return check_flags(f);
+} catch (...) {
+    return kb::exception_status();
 }
 
 // Moments of every replica's headings, reduced on the device.
@@ -259,15 +273,19 @@ static kb_status field_moments(kb_field* f, double* out) {
     return check_flags(f);
 }
 
-kb_status kb_batch_moments(kb_batch* b, double* out) {
+kb_status kb_batch_moments(kb_batch* b, double* out) try {
     if (!b || !out) return fail(KB_ERR_ARG, "null argument");
     return field_moments(b->f, out);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_field_moments(kb_field* f, double out4[4]) {
+kb_status kb_field_moments(kb_field* f, double out4[4]) try {
     if (!f || !out4) return fail(KB_ERR_ARG, "null argument");
     if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: use kb_batch_moments");
     return field_moments(f, out4);
+} catch (...) {
+    return kb::exception_status();
 }
 
 // Rebuild a committed batch with a new replica table: slot i of `reps`
@@ -347,7 +365,7 @@ static kb_status batch_repack(kb_batch* b, std::vector<Rep> reps, const std::vec
     return check_flags(f);
 }
 
-kb_status kb_batch_remove_replica(kb_batch* b, uint32_t r) {
+kb_status kb_batch_remove_replica(kb_batch* b, uint32_t r) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     kb_field* f = b->f;
     if (r >= f->reps.size()) return fail(KB_ERR_ARG, "replica index out of range");
@@ -362,11 +380,13 @@ kb_status kb_batch_remove_replica(kb_batch* b, uint32_t r) {
             src.push_back(i);
         }
     return batch_repack(b, reps, src, 0, nullptr, nullptr, nullptr);
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_batch_add_replica(kb_batch* b, const kb_replica_desc* d, const uint32_t* ids,
                                const float* xy, const float* dxy, uint64_t origin_step,
-                               uint32_t* index) {
+                               uint32_t* index) try {
     if (!b || !d || !index || (d->nboids && (!ids || !xy || !dxy))) return fail(KB_ERR_ARG, "null argument");
     kb_field* f = b->f;
     if (f->wn || !f->p_id.empty() || std::find(b->have.begin(), b->have.end(), 0) != b->have.end())
@@ -399,31 +419,43 @@ kb_status kb_batch_add_replica(kb_batch* b, const kb_replica_desc* d, const uint
     if (st) return st;
     *index = (uint32_t)(reps.size() - 1);
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_batch_synchronize(kb_batch* b) {
+kb_status kb_batch_synchronize(kb_batch* b) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     return kb_field_synchronize(b->f);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_batch_cuda_stream(kb_batch* b, void** stream) {
+kb_status kb_batch_cuda_stream(kb_batch* b, void** stream) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     return kb_field_cuda_stream(b->f, stream);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty) {
+kb_status kb_batch_set_step_options(kb_batch* b, int32_t fused, int32_t tile_tx, int32_t tile_ty) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     return kb_field_set_step_options(b->f, fused, tile_tx, tile_ty);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_batch_step_stats(kb_batch* b, uint32_t out4[4]) {
+kb_status kb_batch_step_stats(kb_batch* b, uint32_t out4[4]) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     return kb_field_step_stats(b->f, out4);
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_batch_device_flags(kb_batch* b, uint32_t* flags, int32_t clear) {
+kb_status kb_batch_device_flags(kb_batch* b, uint32_t* flags, int32_t clear) try {
     if (!b) return fail(KB_ERR_ARG, "null argument");
     return kb_field_device_flags(b->f, flags, clear);
+} catch (...) {
+    return kb::exception_status();
 }
 
 }  // extern "C"

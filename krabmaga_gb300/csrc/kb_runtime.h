@@ -47,6 +47,10 @@ struct DevBuf {
 // Record a failure message for kb_last_error() and return the code.
 kb_status fail(kb_status code, const std::string& msg);
 kb_status cuda_fail(cudaError_t e, const char* what);
+// The status of the exception being handled, for the catch block of an entry
+// point: host allocation failures are KB_ERR_OOM, anything else KB_ERR_STATE,
+// and no exception crosses the C ABI.
+kb_status exception_status() noexcept;
 
 // Stream-ordered writes of small device state (values travel as kernel
 // arguments, so no host staging buffer has to outlive the call).

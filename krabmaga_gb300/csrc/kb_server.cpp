@@ -139,7 +139,11 @@ void srv_fail_all(kb_server* S, std::vector<SrvReq*>& act, const std::string& wh
     std::lock_guard<std::mutex> lk(S->mu);
     for (SrvReq* q : act) {
         q->state = 3;
-        q->error = why;
+        try {
+            q->error = why;
+        } catch (...) {
+            q->error.clear();
+        }
         q->t_done = Clock::now();
         S->used_bytes -= q->bytes;
         S->failed++;
@@ -148,123 +152,141 @@ void srv_fail_all(kb_server* S, std::vector<SrvReq*>& act, const std::string& wh
     S->cv_done.notify_all();
 }
 
-void srv_loop(kb_server* S) {
-    cudaSetDevice(S->desc.device);
+// One pass of the request loop: admit what fits, run one epoch, copy out the
+// finished requests.  Returns false once the server is stopping.
+bool srv_epoch(kb_server* S, std::vector<SrvReq*>& act, bool& changed) {
     kb_field* f = S->f;
-    std::vector<SrvReq*> act;
-    bool changed = false;
-    for (;;) {
-        {
-            std::unique_lock<std::mutex> lk(S->mu);
-            while (!S->stop && S->queue.empty() && act.empty()) S->cv.wait(lk);
-            if (S->stop) break;
-            while (!S->queue.empty() && act.size() < S->desc.max_slots &&
-                   S->used_bytes + S->queue.front()->bytes <= S->desc.hbm_budget_bytes) {
-                SrvReq* q = S->queue.front();
-                S->queue.pop_front();
-                q->state = 1;
-                q->t_admit = Clock::now();
-                q->fresh = true;
-                S->used_bytes += q->bytes;
-                act.push_back(q);
-                changed = true;
-            }
-            S->active = act;
-            S->max_active = std::max<uint64_t>(S->max_active, act.size());
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        while (!S->stop && S->queue.empty() && act.empty()) S->cv.wait(lk);
+        if (S->stop) return false;
+        while (!S->queue.empty() && act.size() < S->desc.max_slots &&
+               S->used_bytes + S->queue.front()->bytes <= S->desc.hbm_budget_bytes) {
+            SrvReq* q = S->queue.front();
+            S->queue.pop_front();
+            q->state = 1;
+            q->t_admit = Clock::now();
+            q->fresh = true;
+            S->used_bytes += q->bytes;
+            act.push_back(q);
+            changed = true;
         }
-        if (act.empty()) continue;
-        const auto t0 = Clock::now();
-        kb_status st = KB_OK;
-        if (changed) st = srv_repack(S, act);
-        changed = false;
-        uint32_t K = S->desc.quantum_steps ? S->desc.quantum_steps : 100;
-        for (SrvReq* q : act) K = std::min(K, q->remaining);
-        if (!st) {
-            st = launch_set_u64(f->dstep.p, S->global_step, f->stream) ? fail(KB_ERR_CUDA, "step") : KB_OK;
-            f->dstep_host = ~0ull;
+        S->active = act;
+        S->max_active = std::max<uint64_t>(S->max_active, act.size());
+    }
+    if (act.empty()) return true;
+    const auto t0 = Clock::now();
+    kb_status st = KB_OK;
+    if (changed) st = srv_repack(S, act);
+    changed = false;
+    uint32_t K = S->desc.quantum_steps ? S->desc.quantum_steps : 100;
+    for (SrvReq* q : act) K = std::min(K, q->remaining);
+    if (!st) {
+        st = launch_set_u64(f->dstep.p, S->global_step, f->stream) ? fail(KB_ERR_CUDA, "step") : KB_OK;
+        f->dstep_host = ~0ull;
+    }
+    if (!st && K > 0) {
+        if (fused_eligible(f, &S->common)) {
+            st = tiled_steps(f, &S->common, K);
+        } else {
+            if (!(st = materialize(f))) st = enqueue_steps(f, &S->common, K, all_fast_rebin_ok(f));
         }
-        if (!st && K > 0) {
-            if (fused_eligible(f, &S->common)) {
-                st = tiled_steps(f, &S->common, K);
-            } else {
-                if (!(st = materialize(f))) st = enqueue_steps(f, &S->common, K, all_fast_rebin_ok(f));
+        S->launches++;
+    }
+    if (st) {
+        srv_fail_all(S, act, g_last_error);
+        changed = true;
+        return true;
+    }
+    S->global_step += K;
+    double upd = 0.0;
+    for (SrvReq* q : act) {
+        q->remaining -= K;
+        upd += (double)q->r.nboids * K;
+    }
+    // copy out the finished requests
+    bool any_done = false;
+    for (SrvReq* q : act) any_done |= (q->remaining == 0);
+    if (any_done) {
+        if (!(st = materialize(f))) {
+            std::vector<uint32_t> lohi(2 * act.size());
+            for (size_t i = 0; i < act.size(); ++i) {
+                if (act[i]->remaining) continue;
+                const Rep& R = act[i]->geom;
+                cudaMemcpyAsync(&lohi[2 * i], f->start[f->cur].p + R.cell_off, 4, cudaMemcpyDeviceToHost, f->stream);
+                cudaMemcpyAsync(&lohi[2 * i + 1], f->start[f->cur].p + R.cell_off + R.ncells, 4, cudaMemcpyDeviceToHost, f->stream);
             }
-            S->launches++;
+            if (cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
+            for (size_t i = 0; i < act.size() && !st; ++i) {
+                SrvReq* q = act[i];
+                if (q->remaining) continue;
+                const uint32_t lo = lohi[2 * i], n = lohi[2 * i + 1] - lohi[2 * i];
+                q->ids.resize(n);
+                q->st.resize((size_t)n * 4);
+                if (n) {
+                    cudaMemcpyAsync(q->ids.data(), f->rid.p + lo, 4ull * n, cudaMemcpyDeviceToHost, f->stream);
+                    cudaMemcpyAsync(q->st.data(), f->rst.p + lo, 16ull * n, cudaMemcpyDeviceToHost, f->stream);
+                }
+            }
+            if (!st && cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
+            uint32_t flags = 0;
+            if (!st) {
+                cudaMemcpy(&flags, f->err.p, 4, cudaMemcpyDeviceToHost);
+                if (flags) {
+                    st = fail(KB_ERR_DEVICE_FLAG, "device error word set during serving");
+                    // the word belongs to the failed batch: later requests start clean
+                    cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream);
+                }
+            }
         }
         if (st) {
             srv_fail_all(S, act, g_last_error);
             changed = true;
-            continue;
+            return true;
         }
-        S->global_step += K;
-        double upd = 0.0;
+    }
+    const auto t1 = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->busy_s += std::chrono::duration<double>(t1 - t0).count();
+        S->updates += upd;
+        std::vector<SrvReq*> keep;
         for (SrvReq* q : act) {
-            q->remaining -= K;
-            upd += (double)q->r.nboids * K;
-        }
-        // copy out the finished requests
-        bool any_done = false;
-        for (SrvReq* q : act) any_done |= (q->remaining == 0);
-        if (any_done) {
-            if (!(st = materialize(f))) {
-                std::vector<uint32_t> lohi(2 * act.size());
-                for (size_t i = 0; i < act.size(); ++i) {
-                    if (act[i]->remaining) continue;
-                    const Rep& R = act[i]->geom;
-                    cudaMemcpyAsync(&lohi[2 * i], f->start[f->cur].p + R.cell_off, 4, cudaMemcpyDeviceToHost, f->stream);
-                    cudaMemcpyAsync(&lohi[2 * i + 1], f->start[f->cur].p + R.cell_off + R.ncells, 4, cudaMemcpyDeviceToHost, f->stream);
-                }
-                if (cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
-                for (size_t i = 0; i < act.size() && !st; ++i) {
-                    SrvReq* q = act[i];
-                    if (q->remaining) continue;
-                    const uint32_t lo = lohi[2 * i], n = lohi[2 * i + 1] - lohi[2 * i];
-                    q->ids.resize(n);
-                    q->st.resize((size_t)n * 4);
-                    if (n) {
-                        cudaMemcpyAsync(q->ids.data(), f->rid.p + lo, 4ull * n, cudaMemcpyDeviceToHost, f->stream);
-                        cudaMemcpyAsync(q->st.data(), f->rst.p + lo, 16ull * n, cudaMemcpyDeviceToHost, f->stream);
-                    }
-                }
-                if (!st && cudaStreamSynchronize(f->stream) != cudaSuccess) st = fail(KB_ERR_CUDA, "copy-out");
-                uint32_t flags = 0;
-                if (!st) {
-                    cudaMemcpy(&flags, f->err.p, 4, cudaMemcpyDeviceToHost);
-                    if (flags) {
-                        st = fail(KB_ERR_DEVICE_FLAG, "device error word set during serving");
-                        // the word belongs to the failed batch: later requests start clean
-                        cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream);
-                    }
-                }
-            }
-            if (st) {
-                srv_fail_all(S, act, g_last_error);
+            if (q->remaining == 0) {
+                q->state = 2;
+                q->t_done = t1;
+                S->used_bytes -= q->bytes;
+                S->latencies.push_back(std::chrono::duration<double>(q->t_done - q->t_arrive).count());
+                S->completed++;
+                S->t_last = t1;
                 changed = true;
-                continue;
+            } else {
+                keep.push_back(q);
             }
         }
-        const auto t1 = Clock::now();
-        {
-            std::lock_guard<std::mutex> lk(S->mu);
-            S->busy_s += std::chrono::duration<double>(t1 - t0).count();
-            S->updates += upd;
-            std::vector<SrvReq*> keep;
-            for (SrvReq* q : act) {
-                if (q->remaining == 0) {
-                    q->state = 2;
-                    q->t_done = t1;
-                    S->used_bytes -= q->bytes;
-                    S->latencies.push_back(std::chrono::duration<double>(q->t_done - q->t_arrive).count());
-                    S->completed++;
-                    S->t_last = t1;
-                    changed = true;
-                } else {
-                    keep.push_back(q);
-                }
-            }
-            act.swap(keep);
-            S->active = act;
-            if (changed) S->cv_done.notify_all();
+        act.swap(keep);
+        S->active = act;
+        if (changed) S->cv_done.notify_all();
+    }
+    return true;
+}
+
+void srv_loop(kb_server* S) {
+    cudaSetDevice(S->desc.device);
+    std::vector<SrvReq*> act;
+    try {
+        act.reserve(S->desc.max_slots);  // admission then never reallocates
+    } catch (...) {
+    }
+    bool changed = false;
+    for (;;) {
+        try {
+            if (!srv_epoch(S, act, changed)) break;
+        } catch (...) {
+            // a host exception (an allocation) fails the running requests as a CUDA error does
+            exception_status();
+            srv_fail_all(S, act, g_last_error);
+            changed = true;
         }
     }
 }
@@ -273,7 +295,7 @@ void srv_loop(kb_server* S) {
 
 extern "C" {
 
-kb_status kb_server_create(const kb_server_desc* desc, kb_server** out) {
+kb_status kb_server_create(const kb_server_desc* desc, kb_server** out) try {
     if (!desc || !out) return fail(KB_ERR_ARG, "null argument");
     if (desc->max_slots == 0 || desc->max_request_boids == 0)
         return fail(KB_ERR_ARG, "max_slots and max_request_boids must be positive");
@@ -301,9 +323,11 @@ kb_status kb_server_create(const kb_server_desc* desc, kb_server** out) {
     S->loop = std::thread(srv_loop, S);
     *out = S;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_server_destroy(kb_server* S) {
+kb_status kb_server_destroy(kb_server* S) try {
     if (!S) return KB_OK;
     {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -319,9 +343,11 @@ kb_status kb_server_destroy(kb_server* S) {
     for (auto& kv : S->all) delete kv.second;
     delete S;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_server_submit(kb_server* S, const kb_request* r, uint64_t* ticket) {
+kb_status kb_server_submit(kb_server* S, const kb_request* r, uint64_t* ticket) try {
     if (!S || !r || !ticket) return fail(KB_ERR_ARG, "null argument");
     std::string why;
     if (!params_ok(&r->params, &why)) return fail(KB_ERR_ARG, why);
@@ -360,9 +386,11 @@ kb_status kb_server_submit(kb_server* S, const kb_request* r, uint64_t* ticket) 
     S->cv.notify_all();
     *ticket = q->ticket;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_server_poll(kb_server* S, uint64_t ticket, int32_t* state, double* latency_s) {
+kb_status kb_server_poll(kb_server* S, uint64_t ticket, int32_t* state, double* latency_s) try {
     if (!S || !state) return fail(KB_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     auto it = S->all.find(ticket);
@@ -374,10 +402,12 @@ kb_status kb_server_poll(kb_server* S, uint64_t ticket, int32_t* state, double* 
                          : 0.0;
     if (it->second->state == 3) return fail(KB_ERR_STATE, it->second->error);
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 kb_status kb_server_result(kb_server* S, uint64_t ticket, uint32_t* ids, float* states, size_t cap,
-                           size_t* n) {
+                           size_t* n) try {
     if (!S || !n) return fail(KB_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     auto it = S->all.find(ticket);
@@ -389,9 +419,11 @@ kb_status kb_server_result(kb_server* S, uint64_t ticket, uint32_t* ids, float* 
     if (ids && take) std::memcpy(ids, q->ids.data(), 4 * take);
     if (states && take) std::memcpy(states, q->st.data(), 16 * take);
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_server_release(kb_server* S, uint64_t ticket) {
+kb_status kb_server_release(kb_server* S, uint64_t ticket) try {
     if (!S) return fail(KB_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     auto it = S->all.find(ticket);
@@ -400,9 +432,11 @@ kb_status kb_server_release(kb_server* S, uint64_t ticket) {
     delete it->second;
     S->all.erase(it);
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_server_wait_idle(kb_server* S, double timeout_s) {
+kb_status kb_server_wait_idle(kb_server* S, double timeout_s) try {
     if (!S) return fail(KB_ERR_ARG, "null argument");
     std::unique_lock<std::mutex> lk(S->mu);
     const auto until = Clock::now() + std::chrono::duration<double>(timeout_s);
@@ -412,9 +446,11 @@ kb_status kb_server_wait_idle(kb_server* S, double timeout_s) {
             return fail(KB_ERR_TIMEOUT, "requests still pending");
     }
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
-kb_status kb_server_stats(kb_server* S, kb_server_report* out) {
+kb_status kb_server_stats(kb_server* S, kb_server_report* out) try {
     if (!S || !out) return fail(KB_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     std::vector<double> v = S->latencies;
@@ -439,6 +475,8 @@ kb_status kb_server_stats(kb_server* S, kb_server_report* out) {
     out->repacks = S->repacks;
     out->max_active = S->max_active;
     return KB_OK;
+} catch (...) {
+    return kb::exception_status();
 }
 
 }  // extern "C"
