@@ -105,7 +105,7 @@ using namespace kb;
 
 extern "C" kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind, float dist,
                                                       size_t nq, const float* qxy,
-                                                      uint32_t* counts, uint32_t* digest) {
+                                                      uint32_t* counts, uint32_t* digest) try {
     if (!f || (nq && (!qxy || !counts || !digest))) return fail(KB_ERR_ARG, "null argument");
     if (kind != KB_QUERY_RELAX && kind != KB_QUERY_EXACT) return fail(KB_ERR_ARG, "bad query kind");
     if (nq > NA_MAX)
@@ -138,4 +138,6 @@ extern "C" kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind,
     NA_CUDA(cudaMemcpyAsync(digest, ddig, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
     NA_CUDA(cudaStreamSynchronize(s));
     return KB_OK;
+} catch (...) {
+    return exception_status();
 }
