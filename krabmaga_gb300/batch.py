@@ -74,6 +74,12 @@ class Batch:
         except Exception:
             pass
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
     @property
     def handle(self):
         return self._h

@@ -83,6 +83,12 @@ class Field2D:
         except Exception:
             pass
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
     @property
     def handle(self):
         return self._h

@@ -55,6 +55,12 @@ class Server:
         except Exception:
             pass
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
     def submit(self, req: Request) -> int:
         t = C.c_uint64()
         L.call("kb_server_submit", self._h, C.byref(req.to_c()), C.byref(t))

@@ -208,3 +208,13 @@ def test_batch_add_replica_errors_leave_the_batch_unchanged(gpu):
     with pytest.raises(L.KbError) as err:
         b.remove_replica(0)                          # the last replica stays
     assert err.value.status == L.KB_ERR_STATE
+
+
+def test_batch_closes_as_a_context_manager(gpu):
+    reps = small_sweep(kg.KB_ARITH_STRICT)[:2]
+    with kg.Batch(reps) as b:
+        b.step(0, 3)
+        ids, st = b.get_replica(1)
+    oids, ost = oracle_run(reps[1], 3)
+    assert np.array_equal(ids, oids) and same_bits(st, ost)
+    assert b.handle is None

@@ -308,3 +308,14 @@ def test_lookups_by_object_read_and_write_buffers(gpu):
     order = {int(i): k for k, i in enumerate(sid)}
     want = sst[[order[int(i)] for i in q[:-2]]]
     assert np.array_equal(st[:-2].view(np.uint32), want.view(np.uint32))
+
+
+def test_handles_close_as_context_managers(gpu):
+    with kg.Field2D(W, H, D, True) as f:
+        f.set_locations(np.array([4], np.uint32), np.array([[1.0, 2.0]], np.float32),
+                        np.zeros((1, 2), np.float32))
+        f.lazy_update()
+        ids, _ = f.get_state()
+        assert ids.tolist() == [4]
+    assert f.handle is None
+    f.close()  # closing twice is harmless

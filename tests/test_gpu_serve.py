@@ -115,3 +115,13 @@ def test_device_generator_matches_host_generator(gpu):
     ai, a_s = alone(r)
     assert np.array_equal(ids, ai) and same_bits(s, a_s)
     srv.close()
+
+
+def test_server_closes_with_requests_pending(gpu):
+    # leaving the block stops the loop after its current epoch and frees the
+    # queued and running requests
+    reqs = small_stream(kg.KB_ARITH_FAST, 6)
+    with kg.Server(max_slots=1, quantum_steps=8, max_request_boids=8000) as srv:
+        for r in reqs:
+            srv.submit(r)
+    assert srv._h is None
