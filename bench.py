@@ -57,6 +57,24 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def bag_count(side, d=D_C):
+    """Bags of a square field: (ceil(side/d) + 1)^2 in f32, the bag matrix of
+    Field2D::new (field_2d.rs:304-322)."""
+    return (int(np.ceil(np.float32(side) / np.float32(d))) + 1) ** 2
+
+
+def algorithmic_bytes(n, ncells):
+    """Algorithmic bytes of one step and of each of its kernels: every record,
+    key and bag offset touched once.  The step figure is n * 32 + ncells * 8
+    (state read and written per boid, one bag offset written and read)."""
+    return {
+        "step": n * 32 + ncells * 8,
+        "force": n * 44 + ncells * 8,  # record in 20, record + key out 24; offsets in, counts out
+        "scan": ncells * 8,            # counts in, offsets out
+        "rebin": n * 44 + ncells * 8,  # key + record in 24, record out 20; two offset arrays
+    }
+
+
 def ncu_traffic(kernel):
     """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
     summary of the same workload (profiles/<kernel>_flock1m.md, a line
@@ -473,12 +491,8 @@ def run_ours(args, wl):
     if rank != 0:
         return
     hbm, peak_kind = peaks()
-    ncells = (int(np.ceil(np.float32(side) / np.float32(D_C))) + 1) ** 2
-    # algorithmic bytes (each record, key and offset touched once)
-    step_bytes = n * 32 + ncells * 8  # whole step: state read+write per boid, bag offsets
-    force_bytes = n * 44 + ncells * 8  # record in 20, record + key out 24; offsets in, counts out
-    scan_bytes = ncells * 8            # counts in, offsets out
-    rebin_bytes = n * 44 + ncells * 8  # key + record in 24, record out 20; two offset arrays
+    ab = algorithmic_bytes(n, bag_count(side))
+    step_bytes, force_bytes, scan_bytes, rebin_bytes = ab["step"], ab["force"], ab["scan"], ab["rebin"]
     kernels = None
     if kernel_ms is not None and kernel_steps == K:
         fm, sm, rm = (v / K for v in kernel_ms)
