@@ -130,16 +130,7 @@ def explore(nstep: int, rep_conf: int, inputs: Dict[str, Sequence], outputs: Seq
         conf_list.append(cfg)
     reps = [_replica(conf_list[i], base.init_seed + i * rep_conf + j)
             for i in range(n_conf) for j in range(rep_conf)]
-    b = Batch(reps, device=device)
-    try:
-        b.synchronize()
-        t0 = time.perf_counter()
-        b.step(0, nstep, 1, 100)
-        b.synchronize()
-        secs = time.perf_counter() - t0
-        mom = b.moments()
-    finally:
-        b.close()
+    mom, secs = _run_batch_timed(reps, nstep, device)
     rows = []
     for i in range(n_conf):
         for j in range(rep_conf):
@@ -194,6 +185,21 @@ def _run_batch(replicas: List[Replica], nstep: int, device: int) -> np.ndarray:
     try:
         b.step(0, nstep, 1, 100)
         return b.moments()
+    finally:
+        b.close()
+
+
+def _run_batch_timed(replicas: List[Replica], nstep: int, device: int) -> Tuple[np.ndarray, float]:
+    """_run_batch, also returning the wall seconds of the steps alone (the
+    batch is synchronised on both sides of them)."""
+    b = Batch(replicas, device=device)
+    try:
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.step(0, nstep, 1, 100)
+        b.synchronize()
+        secs = time.perf_counter() - t0
+        return b.moments(), secs
     finally:
         b.close()
 

@@ -261,3 +261,34 @@ def test_evolutionary_search_stops_when_selection_empties_the_population(fake_ru
     rows, log = _ga(fake_runner, 5.0, 4, survivors=0)
     assert {r["generation"] for r in rows} == {1}
     assert [e[0] for e in log] == ["selection"]
+
+
+def test_explore_rows_as_the_macro(monkeypatch):
+    # every run of every configuration in one device batch (faked here); the
+    # rows in configuration order (first input slowest), runs 0-based, run k
+    # of configuration i seeded init_seed + i * rep_conf + k
+    import numpy as np
+    seen = []
+
+    def fake(replicas, nstep, device):
+        seen.append([(r.params.jump, r.n, r.params.seed) for r in replicas])
+        m = np.array([[r.n, r.n * r.params.jump, 0.0, r.n * r.params.jump] for r in replicas], float)
+        return m, 0.5
+
+    monkeypatch.setattr(ex, "_run_batch_timed", fake)
+    base = kg.FlockerConfig(initial_flockers=20, dim=30.0, init_seed=9)
+    rows = kg.explore(40, 2, {"jump": [0.3, 0.6], "initial_flockers": [10, 20, 30]},
+                      ["mean_speed", "boids"], base=base)
+    assert len(seen) == 1 and len(seen[0]) == 12 and len(rows) == 12
+    assert [(r["Simulation"], r["Run"], r["jump"], r["initial_flockers"]) for r in rows[:4]] == \
+        [(0, 0, 0.3, 10), (0, 1, 0.3, 10), (1, 0, 0.3, 20), (1, 1, 0.3, 20)]
+    assert (rows[-1]["Simulation"], rows[-1]["jump"], rows[-1]["initial_flockers"]) == (5, 0.6, 30)
+    for r in rows:
+        assert r["mean_speed"] == pytest.approx(r["jump"]) and r["boids"] == r["initial_flockers"]
+        assert r["Run Duration"] == 0.5 and r["Step per sec"] == 80.0
+        assert list(r)[:2] == ["Simulation", "Run"]
+    assert [s for (_, _, s) in seen[0]] == list(range(9, 21))
+    # the matched mode pairs the inputs by position
+    rows = kg.explore(5, 1, {"jump": [0.3, 0.6], "initial_flockers": [10, 20]}, ["boids"],
+                      mode=ex.ExploreMode.Matched, base=base)
+    assert [(r["jump"], r["initial_flockers"], r["boids"]) for r in rows] == [(0.3, 10, 10), (0.6, 20, 20)]
