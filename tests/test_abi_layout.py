@@ -97,3 +97,48 @@ def test_rust_binding_covers_the_header():
     assert set(bound) == set(hdr), (set(hdr) - set(bound), set(bound) - set(hdr))
     for name, n in bound.items():
         assert hdr[name] == n, name
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "krabgpu.h"
+
+int main(void) {
+    uint32_t ids[64];
+    float xy[128], dxy[128];
+    kb_field* f = NULL;
+    kb_field_desc desc = {10.0f, 10.0f, 0.5f, 1, 0, 0, KB_CELL_WRAP_CLAMP};
+    if (strstr(kb_version(), "sm_103a") == NULL) return 1;
+    if (kb_gen_uniform(64, 50.0f, 40.0f, 7, 1.0f, ids, xy, dxy) != KB_OK) return 2;
+    if (kb_field_create(NULL, &f) != KB_ERR_ARG || f != NULL) return 3;
+    if (strlen(kb_last_error()) == 0) return 4;
+    if (kb_device_count() == 0 && kb_field_create(&desc, &f) != KB_ERR_NO_DEVICE) return 5;
+    for (int i = 0; i < 64; ++i) printf("%u %a %a %a %a\n", ids[i], xy[2 * i], xy[2 * i + 1], dxy[2 * i], dxy[2 * i + 1]);
+    return 0;
+}
+"""
+
+
+def test_plain_c_caller_links_and_agrees_with_ctypes(tmp_path):
+    # the library as a C program links it: header compiled as C99, no C++ name
+    # mangling; the host generator gives the same bits through either caller
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(L.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.dirname(HEADER), str(src),
+                    "-L", libdir, "-lkrabgpu", "-Wl,-rpath," + libdir, "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.returncode
+    import numpy as np
+    import krabmaga_gb300 as kg
+    ids, xy, dxy = kg.gen_uniform(64, 50.0, 40.0, 7, 1.0)
+    rows = [ln.split() for ln in out.stdout.strip().splitlines()]
+    assert [int(r[0]) for r in rows] == ids.tolist()
+    got = np.array([[float.fromhex(v) for v in r[1:]] for r in rows], np.float32)
+    assert np.array_equal(got[:, :2], xy) and np.array_equal(got[:, 2:], dxy)
