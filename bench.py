@@ -146,12 +146,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def gen(wl):
-    import krabmaga_gb300 as kg
-
+def gen(wl, src):
+    """The workload's seeded flock from `src`: the library (krabmaga_gb300) for
+    the GPU arm, the oracle for the CPU arms, so that those never load the GPU
+    library.  Both give the same bits (tests/test_workload_gen.py)."""
     if wl["gen"] == "uniform":
-        return kg.gen_uniform(wl["n"], wl["side"], wl["side"], wl["seed"], 1.0)
-    return kg.gen_clustered(wl["n"], wl["side"], wl["side"], 256, 40.0, 0.3, wl["seed"])
+        return src.gen_uniform(wl["n"], wl["side"], wl["side"], wl["seed"], 1.0)
+    return src.gen_clustered(wl["n"], wl["side"], wl["side"], 256, 40.0, 0.3, wl["seed"])
 
 
 def dist_setup():
@@ -187,7 +188,7 @@ def cpu_reference(wl, steps):
     """The oracle's reference-equivalent run: returns (boid-updates/s, sample text)."""
     import oracle
 
-    ids, xy, dxy = gen(wl)
+    ids, xy, dxy = gen(wl, oracle)
     p = oracle.params(seed=wl["seed"], query_mode=0)
     secs, _ = oracle.simulate_timed(wl["side"], wl["side"], D_C, p, ids, xy, dxy, steps)
     return wl["n"] * steps / secs, (f"{wl['desc']}, {steps} steps through the priority-queue "
@@ -201,7 +202,7 @@ def cpu_reference_threads(wl, steps):
     import oracle
 
     threads = max(1, os.cpu_count() or 1)
-    ids, xy, dxy = gen(wl)
+    ids, xy, dxy = gen(wl, oracle)
     p = oracle.params(seed=wl["seed"], query_mode=0)
     secs, _ = oracle.simulate_timed_threads(wl["side"], wl["side"], D_C, p, ids, xy, dxy, steps,
                                             threads)
@@ -335,8 +336,10 @@ def run_reference(args, wl):
     steps = max(1, min(args.steps, args.ref_steps))
     value, sample = cpu_reference(wl, steps)
     pv, threads, psample = cpu_reference_threads(wl, steps)
+    # rank 0 alone runs the CPU arm (one core), whatever the number of ranks
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "ranks": ws,
         "steps": steps, "warmup": 0, "ms_per_step": 1e3 * wl["n"] / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox uniform flock)",
@@ -362,7 +365,7 @@ def run_ours(args, wl):
     dev = local
     torch.cuda.set_device(dev)
     n, side = wl["n"], wl["side"]
-    ids, xy, dxy = gen(wl)
+    ids, xy, dxy = gen(wl, kg)
     params = kg.FlockParams(seed=wl["seed"], query_mode=kg.KB_QUERY_RELAX,
                             arith=kg.KB_ARITH_FAST if args.arith == "fast" else kg.KB_ARITH_STRICT)
     pc = params.to_c()
@@ -576,7 +579,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile", default="0x0", help="fused tile shape TXxTY in bags (0x0: automatic)")
     ap.add_argument("--mode", type=int, default=0,
-                    help="step path: 2 tiled split (default), 1 persistent, 0 separate kernels")
+                    help="step path: 0 the default choice (separate kernels on this workload), "
+                         "1 persistent tiled, 2 split tiled, 3 separate kernels whatever the size")
     ap.add_argument("--profile", action="store_true", help="short plain run for ncu, no timing")
     ap.add_argument("--profile-call-steps", type=int, default=1,
                     help="with --profile: steps per kb_flock_step call (runs of 2 or more take "

@@ -288,10 +288,18 @@ kb_status kb_field_neighbor_digest(kb_field* f, int32_t kind, float dist, size_t
  * KB_NOALLOC_MAX_QUERIES returns KB_ERR_ARG.  Calls whose GPU work overlaps
  * (two host threads, fields on the same device) race on that array.  The
  * first call on a device sets the array up for that device
- * (cudaGetSymbolAddress); make it before any stream capture on the device. */
+ * (cudaGetSymbolAddress); make it before any stream capture on the device.
+ * The array's address is kept for the life of the process: a reset of the
+ * device's primary context (cudaDeviceReset) invalidates it, as it
+ * invalidates every field on that device. */
 #define KB_NOALLOC_MAX_QUERIES 65536
 kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind, float dist, size_t nq,
                                            const float* qxy, uint32_t* counts, uint32_t* digest);
+
+/* No counterpart in the reference.  Device allocations and frees the library
+ * has made so far in this process (all devices), for checking that a call
+ * allocates nothing. */
+kb_status kb_debug_allocation_counts(uint64_t* allocs, uint64_t* frees);
 
 /* ------------------------------------------------------ batched replicas */
 /* Many independent Flockers simulations (the model-exploration workload of

@@ -195,6 +195,7 @@ _SIGS = {
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
     "kb_field_neighbor_digest_noalloc": (
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
+    "kb_debug_allocation_counts": (C.c_int32, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "kb_batch_create": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(ReplicaDesc), C.POINTER(_P)]),
     "kb_batch_destroy": (C.c_int32, [_P]),
     "kb_batch_set_replica": (C.c_int32, [_P, C.c_uint32, C.c_size_t, _U32, _F, _F]),
@@ -255,3 +256,10 @@ def fptr(a):
 
 def uptr(a):
     return a.ctypes.data_as(_U32) if a is not None else None
+
+
+def allocation_counts():
+    """(device allocations, device frees) the library has made in this process."""
+    a, f = C.c_uint64(), C.c_uint64()
+    call("kb_debug_allocation_counts", C.byref(a), C.byref(f))
+    return int(a.value), int(f.value)

@@ -20,6 +20,8 @@ namespace kb {
 
 thread_local std::string g_last_error;
 
+std::atomic<unsigned long long> g_dev_allocs{0}, g_dev_frees{0};
+
 kb_status fail(kb_status code, const std::string& msg) {
     g_last_error = msg;
     return code;
@@ -478,11 +480,14 @@ uint32_t* buf_ids(kb_field* f, int i) { return i == 0 ? f->rid.p : (i == 1 ? f->
 uint32_t* buf_key(kb_field* f, int i) { return i == 0 ? f->rkey.p : (i == 1 ? f->wkey.p : f->tkey.p); }
 
 // Rebuild the read buffer from a virtual state (the stencil gather of the
-// last write list into canonical order).
+// last write list into canonical order).  The read buffer keeps its device
+// address (a write list held in rst is gathered into the third buffer and
+// copied back), so graphs captured over the field's buffers stay valid and
+// the query entry points that materialise drop none.
 kb_status materialize(kb_field* f) {
     if (!f->virt) return KB_OK;
     int dst = 0;
-    if (f->a_last == 0) dst = 1;  // the write list sits in rst: gather into wst, then swap roles
+    if (f->a_last == 0) dst = 2;  // the write list sits in rst: gather into tst, then copy back
     RebinArgs r{};
     r.reps = f->d_rep.p;
     r.nrep = nrep(f);
@@ -501,10 +506,9 @@ kb_status materialize(kb_field* f) {
     r.step = nullptr;
     r.err = f->err.p;
     KB_CUDA(launch_rebin(r, f->stream));
-    if (dst == 1) {
-        f->rst.swap(f->wst);
-        f->rid.swap(f->wid);
-        f->drop_graphs();
+    if (dst == 2 && f->rn) {
+        KB_CUDA(cudaMemcpyAsync(f->rst.p, f->tst.p, sizeof(float4) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
+        KB_CUDA(cudaMemcpyAsync(f->rid.p, f->tid.p, sizeof(uint32_t) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
     }
     f->virt = false;
     return KB_OK;
@@ -1024,6 +1028,15 @@ kb_status field_query_view(kb_field* f, int32_t kind, float dist, QueryArgs* a, 
 }  // namespace kb
 
 extern "C" {
+
+kb_status kb_debug_allocation_counts(uint64_t* allocs, uint64_t* frees) try {
+    if (!allocs || !frees) return fail(KB_ERR_ARG, "null argument");
+    *allocs = g_dev_allocs.load(std::memory_order_relaxed);
+    *frees = g_dev_frees.load(std::memory_order_relaxed);
+    return KB_OK;
+} catch (...) {
+    return kb::exception_status();
+}
 
 kb_status kb_field_create(const kb_field_desc* desc, kb_field** out) try {
     if (!desc || !out) return fail(KB_ERR_ARG, "null argument");

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <atomic>
 #include <string>
 #include <utility>
 
@@ -12,6 +13,10 @@
 #include "kb_common.h"
 
 namespace kb {
+
+// Device allocations and frees made by the library (every one goes through
+// DevBuf), for kb_debug_allocation_counts.
+extern std::atomic<unsigned long long> g_dev_allocs, g_dev_frees;
 
 template <typename T>
 struct DevBuf {
@@ -24,6 +29,7 @@ struct DevBuf {
     cudaError_t alloc(size_t count) {
         release();
         if (count == 0) return cudaSuccess;
+        g_dev_allocs.fetch_add(1, std::memory_order_relaxed);
         cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
         if (e != cudaSuccess) {
             p = nullptr;
@@ -34,7 +40,10 @@ struct DevBuf {
         return cudaSuccess;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            g_dev_frees.fetch_add(1, std::memory_order_relaxed);
+            cudaFree(p);
+        }
         p = nullptr;
         n = 0;
     }

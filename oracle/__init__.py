@@ -67,6 +67,10 @@ _SIGS = {
                                          C.c_size_t]),
     "orc_simulate_timed": (C.c_double, [C.c_float, C.c_float, C.c_float, C.POINTER(Params),
                                         C.c_size_t, _U32, _F, _F, C.c_uint32, C.POINTER(_P)]),
+    "orc_gen_uniform": (C.c_int, [C.c_size_t, C.c_float, C.c_float, C.c_uint64, C.c_float, _U32,
+                                  _F, _F]),
+    "orc_gen_clustered": (C.c_int, [C.c_size_t, C.c_float, C.c_float, C.c_uint32, C.c_float,
+                                    C.c_float, C.c_uint64, _U32, _F, _F]),
 }
 for _n, (_r, _a) in _SIGS.items():
     _fn = getattr(lib, _n)
@@ -92,6 +96,27 @@ def params_from(fp) -> Params:
     """From a krabmaga_gb300.FlockParams-like object."""
     return Params(fp.cohesion, fp.avoidance, fp.consistency, fp.randomness, fp.momentum,
                   fp.jump, fp.neighbor_radius, fp.query_mode, fp.seed)
+
+
+def gen_uniform(n, w, h, seed, heading_scale=1.0):
+    """The uniform workload flock (workload_gen.cpp): (ids, xy[n,2], dxy[n,2])."""
+    ids = np.zeros(n, np.uint32)
+    xy = np.zeros((n, 2), np.float32)
+    dxy = np.zeros((n, 2), np.float32)
+    if lib.orc_gen_uniform(n, w, h, seed, heading_scale, _u(ids), _f(xy), _f(dxy)) != 0:
+        raise ValueError("bad workload arguments")
+    return ids, xy, dxy
+
+
+def gen_clustered(n, w, h, nclusters, sigma, angle_sigma, seed):
+    """The clustered workload flock (workload_gen.cpp): (ids, xy[n,2], dxy[n,2])."""
+    ids = np.zeros(n, np.uint32)
+    xy = np.zeros((n, 2), np.float32)
+    dxy = np.zeros((n, 2), np.float32)
+    if lib.orc_gen_clustered(n, w, h, nclusters, sigma, angle_sigma, seed, _u(ids), _f(xy),
+                             _f(dxy)) != 0:
+        raise ValueError("bad workload arguments")
+    return ids, xy, dxy
 
 
 def philox(ctr, key):

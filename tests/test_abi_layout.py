@@ -85,18 +85,56 @@ def _header_arities():
     return out
 
 
-def test_rust_binding_covers_the_header():
-    # the extern "C" blocks a maintainer would add to the reference's crate name
-    # every entry point of the header, each with the header's parameter count
-    hdr = _header_arities()
-    md = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+RUST_SYS = os.path.join(ROOT, "rust", "krabgpu-sys", "src", "lib.rs")
+
+
+def _rust_externs():
+    src = open(RUST_SYS).read()
     bound = {}
-    for m in re.finditer(r"pub fn (kb_[a-z0-9_]+)\s*\(([^;]*?)\)\s*(->[^;]*)?;", md, flags=re.S):
+    for m in re.finditer(r"pub fn (kb_[a-z0-9_]+)\s*\(([^;]*?)\)\s*(->[^;]*)?;", src, flags=re.S):
         args = re.sub(r"//[^\n]*", "", m.group(2)).strip().rstrip(",")
         bound[m.group(1)] = 0 if not args else args.count(",") + 1
+    return src, bound
+
+
+def test_rust_binding_covers_the_header():
+    # the extern "C" block of the Rust crate a maintainer adds to the reference
+    # names every entry point of the header, each with the header's parameter count
+    hdr = _header_arities()
+    _, bound = _rust_externs()
     assert set(bound) == set(hdr), (set(hdr) - set(bound), set(bound) - set(hdr))
     for name, n in bound.items():
         assert hdr[name] == n, name
+
+
+def test_rust_structs_and_constants_match_the_header():
+    # every #[repr(C)] struct lists the ctypes mirror's fields in the same order,
+    # and every constant the crate defines has the header's value
+    src, _ = _rust_externs()
+    for sname, cls in STRUCTS.items():
+        m = re.search(r"pub struct " + sname + r"\s*\{(.*?)\n\}", src, flags=re.S)
+        assert m, sname
+        fields = re.findall(r"pub ([a-z0-9_]+)\s*:", m.group(1))
+        assert fields == [f for f, _ in cls._fields_], sname
+    consts = header_constants()
+    found = re.findall(r"pub const (KB_[A-Z0-9_]+)\s*:\s*[a-z0-9_]+\s*=\s*(0x[0-9a-fA-F]+|\d+)\s*;", src)
+    assert {n for n, _ in found} == set(consts), set(consts) ^ {n for n, _ in found}
+    for name, v in found:
+        assert consts[name] == int(v, 0), name
+
+
+def test_rust_facade_keeps_the_reference_names():
+    # the safe crate implements the reference's State and Field traits and keeps
+    # Field2D's method names
+    src = open(os.path.join(ROOT, "rust", "krabmaga-gpu", "src", "lib.rs")).read()
+    assert "impl State for GpuFlocker" in src and "impl Field for GpuField2D" in src
+    for name in ["set_object_location", "lazy_update", "get_neighbors_within_relax_distance",
+                 "get_neighbors_within_distance", "get_objects", "num_objects_at_location",
+                 "get_empty_bags", "iter_objects", "remove_object_location", "get_location"]:
+        assert re.search(r"fn " + name + r"\b", src), name
+    hdr = _header_arities()
+    for fn in re.findall(r"sys::(kb_[a-z0-9_]+)\s*\(", src):
+        assert fn in hdr, fn
 
 
 C_CALLER = r"""

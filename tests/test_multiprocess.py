@@ -61,6 +61,19 @@ def test_reference_arm_under_torchrun_prints_once():
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
     line = json.loads(lines[0])
-    assert line["impl"] == "reference" and line["n_gpus"] == 2
+    # rank 0 alone runs the one-core CPU arm: one GPU's worth of work
+    assert line["impl"] == "reference" and line["n_gpus"] == 1 and line["ranks"] == 2
     assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_does_not_load_the_gpu_library():
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'flock1k', "
+            "'--steps', '2', '--warmup', '0']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('GPU_LIB_LOADED' if 'libkrabgpu' in maps else 'GPU_LIB_ABSENT'); "
+            "print('ORACLE_LOADED' if 'libkrab_oracle' in maps else 'ORACLE_ABSENT')")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "GPU_LIB_ABSENT" in r.stdout and "ORACLE_LOADED" in r.stdout

@@ -94,3 +94,46 @@ def test_noalloc_rejects_more_than_its_staging_array(gpu):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     finally:
         f.close()
+
+
+def test_noalloc_call_makes_no_device_allocation(gpu):
+    """The promise itself: no device allocation or free by the library (its
+    own counter of every cudaMalloc / cudaFree it makes), none by torch's
+    allocator, and the device's free memory unchanged.  The first call here
+    also materialises a read buffer left virtual by tiled steps."""
+    import torch
+
+    f = _flock(steps=0)
+    g = _flock(steps=0)
+    try:
+        # tiled steps leave the read buffer virtual (the last write list plus offsets)
+        f.set_step_options(2)
+        p = kg.FlockParams(seed=5)
+        L.call("kb_flock_step", f.handle, C.byref(p.to_c()), C.c_uint64(1), C.c_uint32(4))
+        f.synchronize()
+        q = np.random.default_rng(8).uniform(0, SIDE, (20_000, 2)).astype(np.float32)
+        torch.cuda.synchronize()
+        a0 = L.allocation_counts()
+        t0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+        n1, d1 = _noalloc(f, L.KB_QUERY_RELAX, 10.0, q)
+        assert L.allocation_counts() == a0
+        # a second field's queries, once the array and both query kernels are
+        # loaded on this device (module loading is not an allocation of the call)
+        _noalloc(g, L.KB_QUERY_RELAX, 10.0, q)
+        _noalloc(g, L.KB_QUERY_EXACT, 10.0, q)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        a1 = L.allocation_counts()
+        n2, d2 = _noalloc(g, L.KB_QUERY_EXACT, 10.0, q)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
+        assert L.allocation_counts() == a1 == a0
+        assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == t0
+        # and the results are still those of the allocating entry point
+        e1, g1 = f.neighbor_digest(L.KB_QUERY_RELAX, 10.0, q)
+        e2, g2 = g.neighbor_digest(L.KB_QUERY_EXACT, 10.0, q)
+        assert np.array_equal(n1, e1) and np.array_equal(d1, g1)
+        assert np.array_equal(n2, e2) and np.array_equal(d2, g2)
+    finally:
+        f.close()
+        g.close()
