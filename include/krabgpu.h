@@ -257,6 +257,25 @@ kb_status kb_field_autotune(kb_field* f, const kb_flock_params* p, uint64_t firs
 kb_status kb_field_get_state(kb_field* f, uint32_t* ids, float* states, size_t cap, size_t* n);
 /* Error word raised by this handle's kernels since the last clear (KB_FLAG_*). */
 kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear);
+
+/* No counterpart in the reference (it has no device waits; it panics on its
+ * errors, src/engine/schedule.rs:374).  Every wait of this library's kernels
+ * on another block (the look-back scan of large bag matrices, the grid
+ * barrier and TMA waits of the tiled steps) is bounded: after spin_limit
+ * iterations (0: each kernel's default) it gives up, raises
+ * KB_FLAG_SPIN_TIMEOUT and the kernel returns; the results of that call are
+ * invalid, and kb_field_synchronize reports KB_ERR_DEVICE_FLAG.  Clearing the
+ * flag (kb_field_device_flags with clear) resets the kernels' control words
+ * and empties the field's read buffer, which the failed call left invalid (a
+ * batch's replicas are set anew with kb_batch_set_replica); the field is then
+ * used again once its state is set anew.  withhold (KB_WITHHOLD_*) is the test
+ * hook that makes a wait run out on purpose, without any fault: the
+ * look-back scan tile, or the block of the persistent step, numbered `index`
+ * does not publish its signal. */
+#define KB_WITHHOLD_NONE 0
+#define KB_WITHHOLD_SCAN_PUBLISH 1
+#define KB_WITHHOLD_GRID_ARRIVAL 2
+kb_status kb_field_set_wait_test(kb_field* f, uint32_t spin_limit, int32_t withhold, uint32_t index);
 /* Wait for the handle's stream; returns KB_ERR_DEVICE_FLAG if a kernel
  * raised the error word. */
 kb_status kb_field_synchronize(kb_field* f);

@@ -43,6 +43,9 @@ KB_PATH_FUSED = 1
 KB_PATH_TILED = 2
 KB_PATH_SMALL = 3
 KB_PATH_DENSE = 4
+KB_WITHHOLD_NONE = 0
+KB_WITHHOLD_SCAN_PUBLISH = 1
+KB_WITHHOLD_GRID_ARRIVAL = 2
 
 STATUS_NAMES = {
     0: "KB_OK", 1: "KB_ERR_ARG", 2: "KB_ERR_OOM", 3: "KB_ERR_CUDA", 4: "KB_ERR_TIMEOUT",
@@ -188,6 +191,7 @@ _SIGS = {
     "kb_flock_step": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_uint32]),
     "kb_field_get_state": (C.c_int32, [_P, _U32, _F, C.c_size_t, _SZ]),
     "kb_field_device_flags": (C.c_int32, [_P, _U32, C.c_int32]),
+    "kb_field_set_wait_test": (C.c_int32, [_P, C.c_uint32, C.c_int32, C.c_uint32]),
     "kb_field_synchronize": (C.c_int32, [_P]),
     "kb_field_neighbor_lists": (
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32, C.c_size_t, _SZ]),

@@ -399,6 +399,43 @@ kb_status ensure_aux_scan(kb_field* f, uint32_t n) {
     return KB_OK;
 }
 
+// Bounded-wait settings of the field's kernels (kb_field_set_wait_test).
+WaitCfg scan_wait(const kb_field* f) {
+    return WaitCfg{f->wait_spins, f->withhold_kind == KB_WITHHOLD_SCAN_PUBLISH ? f->withhold_index : ~0u};
+}
+WaitCfg fused_wait(const kb_field* f) {
+    return WaitCfg{f->wait_spins, f->withhold_kind == KB_WITHHOLD_GRID_ARRIVAL ? f->withhold_index : ~0u};
+}
+
+// After a bounded wait gave up, the control words of the waiting kernels can
+// be left mid-protocol (a grid barrier's arrival count, a tile counter, look-
+// back words): reset them all, with the epochs restarting at zero.  The step
+// that gave up left the read buffer invalid: a plain field is emptied (its
+// state is set anew), a batch's replicas are set anew by the caller.
+kb_status reset_wait_state(kb_field* f) {
+    cudaStream_t s = f->stream;
+    if (f->scan_ctl.p) KB_CUDA(cudaMemsetAsync(f->scan_ctl.p, 0, sizeof(ScanCtl) * f->scan_ctl.n, s));
+    if (f->tstate.p) KB_CUDA(cudaMemsetAsync(f->tstate.p, 0, sizeof(unsigned long long) * f->tstate.n, s));
+    if (f->aux_ctl.p) KB_CUDA(cudaMemsetAsync(f->aux_ctl.p, 0, sizeof(ScanCtl) * f->aux_ctl.n, s));
+    if (f->aux_tstate.p)
+        KB_CUDA(cudaMemsetAsync(f->aux_tstate.p, 0, sizeof(unsigned long long) * f->aux_tstate.n, s));
+    if (f->hist.p) KB_CUDA(cudaMemsetAsync(f->hist.p, 0, sizeof(uint32_t) * f->hist.n, s));
+    f->hist_counted = false;
+    auto& F = f->fused;
+    if (F.ctl.p) KB_CUDA(cudaMemsetAsync(F.ctl.p, 0, sizeof(uint32_t) * F.ctl.n, s));
+    if (F.scan_state.p)
+        KB_CUDA(cudaMemsetAsync(F.scan_state.p, 0, sizeof(unsigned long long) * F.scan_state.n, s));
+    f->virt = false;
+    if (!f->is_batch) {
+        f->rn = 0;
+        if (f->start[f->cur].p)
+            KB_CUDA(cudaMemsetAsync(f->start[f->cur].p, 0, sizeof(uint32_t) * (f->ncells_total + 1), s));
+    }
+    f->dstep_host = ~0ull;
+    KB_CUDA(cudaStreamSynchronize(s));
+    return KB_OK;
+}
+
 // The general stable sort: write list -> read buffer.  hist already holds
 // the key counts when counted == true.
 kb_status general_rebuild(kb_field* f, bool counted) {
@@ -411,7 +448,8 @@ kb_status general_rebuild(kb_field* f, bool counted) {
         KB_CUDA(launch_hist_list(f->wkey.p, f->wdead.p, f->wn, f->hist.p, s));
     }
     f->hist_counted = false;  // the scan below zeroes it
-    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s,
+                        scan_wait(f)));
     KB_CUDA(launch_scatter_list(f->wkey.p, f->wdead.p, f->wst.p, f->wid.p, f->wn, f->start[nxt].p, f->cursor.p, f->tst.p, f->tid.p, f->tsrc.p, s));
     KB_CUDA(launch_canon(f->start[nxt].p, f->ncells_total, f->tst.p, f->tid.p, f->tsrc.p, f->cursor.p, f->rst.p, f->rid.p, s));
     f->cur = nxt;
@@ -421,7 +459,8 @@ kb_status general_rebuild(kb_field* f, bool counted) {
 kb_status fast_rebuild(kb_field* f, bool bump_step) {
     cudaStream_t s = f->stream;
     const int nxt = 1 - f->cur;
-    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s));
+    KB_CUDA(launch_scan(f->hist.p, f->start[nxt].p, f->ncells_total, f->scan_ctl.p, f->tstate.p, f->err.p, true, s,
+                        scan_wait(f)));
     f->hist_counted = false;
     if (f->kt_cur >= 0) KB_CUDA(cudaEventRecord(f->kt_pending[f->kt_cur].ev[2], s));
     RebinArgs a{};
@@ -441,6 +480,7 @@ kb_status fast_rebuild(kb_field* f, bool bump_step) {
     a.s_ids = f->rid.p;
     a.step = bump_step ? f->dstep.p : nullptr;
     a.err = f->err.p;
+    a.n = f->rn;
     KB_CUDA(launch_rebin(a, s));
     f->cur = nxt;
     return KB_OK;
@@ -505,6 +545,7 @@ kb_status materialize(kb_field* f) {
     r.s_ids = buf_ids(f, dst);
     r.step = nullptr;
     r.err = f->err.p;
+    r.n = f->rn;
     KB_CUDA(launch_rebin(r, f->stream));
     if (dst == 2 && f->rn) {
         KB_CUDA(cudaMemcpyAsync(f->rst.p, f->tst.p, sizeof(float4) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
@@ -663,6 +704,7 @@ kb_status fused_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
     a.err = f->err.p;
     a.stats = F.ctl.p + 4;
     a.phase_cycles = nullptr;
+    a.wait = fused_wait(f);
     if (F.profile) {
         if (F.phase_cycles.n < (size_t)F.nctas * 16) {
             cudaError_t e = F.phase_cycles.alloc((size_t)F.nctas * 16);
@@ -698,6 +740,7 @@ FusedArgs fused_args(kb_field* f) {
     a.err = f->err.p;
     a.stats = F.ctl.p + 4;
     a.phase_cycles = nullptr;
+    a.wait = fused_wait(f);
     if (F.profile) {
         if (F.phase_cycles.n < 16) {
             if (F.phase_cycles.alloc(16)) return a;
@@ -733,7 +776,7 @@ kb_status split_steps(kb_field* f, const kb_flock_params* p, uint32_t nsteps) {
                                  f->start[1 - cur].p, f->start[cur].p, k, F.strict != 0, F.qmode, s));
         in_keys = true;
         KB_CUDA(launch_scan(f->hist.p, f->start[1 - cur].p, f->ncells_total, f->scan_ctl.p,
-                            f->tstate.p, f->err.p, true, s));
+                            f->tstate.p, f->err.p, true, s, scan_wait(f)));
         cur = 1 - cur;
         in = out;
     }
@@ -1486,9 +1529,24 @@ kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear) try
     kb_status st = read_u32(f, f->err.p, flags);
     if (st) return st;
     if (clear) {
+        if ((*flags & ERR_SPIN_TIMEOUT) && (st = reset_wait_state(f))) return st;
         KB_CUDA(cudaMemsetAsync(f->err.p, 0, sizeof(uint32_t), f->stream));
         KB_CUDA(cudaStreamSynchronize(f->stream));
     }
+    return KB_OK;
+} catch (...) {
+    return kb::exception_status();
+}
+
+kb_status kb_field_set_wait_test(kb_field* f, uint32_t spin_limit, int32_t withhold, uint32_t index) try {
+    if (!f) return fail(KB_ERR_ARG, "null argument");
+    if (withhold != KB_WITHHOLD_NONE && withhold != KB_WITHHOLD_SCAN_PUBLISH &&
+        withhold != KB_WITHHOLD_GRID_ARRIVAL)
+        return fail(KB_ERR_ARG, "withhold must be one of KB_WITHHOLD_*");
+    f->wait_spins = spin_limit;
+    f->withhold_kind = withhold;
+    f->withhold_index = withhold == KB_WITHHOLD_NONE ? 0u : index;
+    f->drop_graphs();  // captured launches hold the previous settings
     return KB_OK;
 } catch (...) {
     return kb::exception_status();

@@ -116,6 +116,12 @@ struct kb_field {
     // 0 separate kernels (small fields: one block, kb_small.cu), 1 persistent
     // fused, 2 split tile step, 3 separate kernels whatever the size
     int fused_mode = 0;
+    // Bounded device waits (kb_field_set_wait_test): iterations before a wait
+    // gives up (0: each kernel's default), and the test hook that makes one
+    // publisher withhold its signal (KB_WITHHOLD_*, at index withhold_index).
+    uint32_t wait_spins = 0;
+    int32_t withhold_kind = KB_WITHHOLD_NONE;
+    uint32_t withhold_index = 0;
     // Per-kernel timing of ungraphed separate-kernel steps: four events per
     // step (force | scan | rebin), read and recycled by kb_field_kernel_times.
     bool ktime = false;
@@ -231,6 +237,8 @@ kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_s
 // Whether every replica's ids are distinct (checked on the device) / set it.
 kb_status check_unique_ids(kb_field* f);
 void set_ids_unique(kb_field* f, bool u);
+// Reset the control words of the bounded-wait protocols (after a timeout).
+kb_status reset_wait_state(kb_field* f);
 // Synchronous reads: one device word; the device error word as a status.
 kb_status read_u32(kb_field* f, const uint32_t* dptr, uint32_t* out);
 kb_status check_flags(kb_field* f);

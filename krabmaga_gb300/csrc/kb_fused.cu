@@ -161,8 +161,12 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* s_warp
     return excl;
 }
 
+__device__ __forceinline__ uint32_t limit_or(uint32_t runtime, uint32_t dflt) {
+    return runtime ? runtime : dflt;
+}
+
 // Grid barrier for a cooperative launch; false if the wait expired.
-__device__ bool grid_sync(uint32_t* bar, uint32_t* err) {
+__device__ bool grid_sync(uint32_t* bar, uint32_t* err, uint32_t spin_limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -177,7 +181,7 @@ __device__ bool grid_sync(uint32_t* bar, uint32_t* err) {
         } else {
             uint32_t spins = 0;
             while (*gen == g) {
-                if (++spins > BAR_SPINS) {
+                if (++spins > limit_or(spin_limit, BAR_SPINS)) {
                     atomicOr(err, ERR_SPIN_TIMEOUT);
                     s_ok = 0;
                     break;
@@ -227,7 +231,7 @@ __device__ void scan_phase(const FusedArgs& a, uint32_t* start_next, uint32_t ep
                         w = *((volatile unsigned long long*)&a.scan_state[j]);
                         if ((uint32_t)(w >> 34) == (epoch & 0x3FFFFFFFu) && ((w >> 32) & 3ull))
                             break;
-                        if (++spins > LB_SPINS) {
+                        if (++spins > limit_or(a.wait.spin_limit, LB_SPINS)) {
                             atomicOr(a.err, ERR_SPIN_TIMEOUT);
                             w = lb_pack(epoch, LB_INC, 0u);
                             break;
@@ -312,6 +316,7 @@ struct Smem {
     uint8_t* srcy;    // [maxqy][4][2] staged row runs feeding each canonical row
     uint8_t* nsrcy;
     uint16_t* sord_cell;  // region-local bag (iq * nqy + jq) of each canonical record
+    uint32_t* abort;      // set when a bounded wait of this block gave up (beside mbar)
 };
 
 struct StepBufs {
@@ -559,7 +564,7 @@ __device__ __forceinline__ void force_boid(const FusedArgs& a, const Rep& R, con
 }
 
 template <bool STRICT, int QMODE>
-__device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, const Smem& S,
+__device__ bool process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, const Smem& S,
                              const StepBufs& B, unsigned long long step, uint32_t* phase,
                              PhaseClock& pc) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -716,15 +721,30 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
         // one warp waits on the transaction barrier; the rest block at the
         // CTA barrier, then observe the completed phase once
         if (warp == 0) {
+            const uint32_t lim = limit_or(a.wait.spin_limit, TMA_SPINS);
             uint32_t spins = 0;
+            bool done = true;
             while (!mbar_try_wait(S.mbar, *phase & 1u)) {
-                if (++spins > TMA_SPINS) {
-                    atomicOr(a.err, ERR_SPIN_TIMEOUT);
+                if (++spins > lim) {
+                    done = false;
                     break;
+                }
+            }
+            if (!done) {
+                // the copies of this phase did not land in time: give them one
+                // more bounded wait (they write this block's shared memory), then
+                // the whole block stops without reading the staged records
+                spins = 0;
+                while (!mbar_try_wait(S.mbar, *phase & 1u) && ++spins <= lim) {
+                }
+                if (lane == 0) {
+                    atomicOr(a.err, ERR_SPIN_TIMEOUT);
+                    *S.abort = 1u;
                 }
             }
         }
         __syncthreads();
+        if (*S.abort) return false;
         if (warp != 0) {
             uint32_t spins = 0;
             while (!mbar_try_wait(S.mbar, *phase & 1u) && ++spins < 64u) {
@@ -766,11 +786,13 @@ __device__ void process_tile(const FusedArgs& a, const Tile tile, TileCtx& c, co
     }
     __syncthreads();
     pc.mark(7);
+    return true;
 }
 
 __device__ __forceinline__ Smem smem_view(unsigned char* smem, const FusedLayout& L) {
     Smem S;
     S.mbar = reinterpret_cast<unsigned long long*>(smem + L.off_mbar);
+    S.abort = reinterpret_cast<uint32_t*>(smem + L.off_mbar + 8);
     S.stage_st = reinterpret_cast<float4*>(smem + L.off_stage_st);
     S.sord_st = reinterpret_cast<float4*>(smem + L.off_sord_st);
     S.stage_ids = reinterpret_cast<uint32_t*>(smem + L.off_stage_ids);
@@ -803,6 +825,7 @@ __global__ void __launch_bounds__(FT, 4) k_tile_step(FusedArgs a, StepBufs B, ui
     if (tid == 0) {
         mbar_init(S.mbar, 1);
         fence_proxy_async();
+        *S.abort = 0u;
     }
     for (int t = tid; t < L.maxhx * L.maxhy; t += FT) S.hist[t] = 0u;
     __syncthreads();
@@ -822,6 +845,7 @@ __global__ void __launch_bounds__(FT, 2) k_fused(FusedArgs a) {
     const FusedLayout L = fused_layout(a.cfg);
     Smem S;
     S.mbar = reinterpret_cast<unsigned long long*>(smem + L.off_mbar);
+    S.abort = reinterpret_cast<uint32_t*>(smem + L.off_mbar + 8);
     S.stage_st = reinterpret_cast<float4*>(smem + L.off_stage_st);
     S.sord_st = reinterpret_cast<float4*>(smem + L.off_sord_st);
     S.stage_ids = reinterpret_cast<uint32_t*>(smem + L.off_stage_ids);
@@ -843,6 +867,7 @@ __global__ void __launch_bounds__(FT, 2) k_fused(FusedArgs a) {
     if (tid == 0) {
         mbar_init(S.mbar, 1);
         fence_proxy_async();
+        *S.abort = 0u;
     }
     for (int t = tid; t < L.maxhx * L.maxhy; t += FT) S.hist[t] = 0u;
     __syncthreads();
@@ -869,14 +894,16 @@ __global__ void __launch_bounds__(FT, 2) k_fused(FusedArgs a) {
             __syncthreads();
             pc.mark(8);
             if (t >= a.ntiles) break;
-            process_tile<STRICT, QMODE>(a, a.tiles[t], ctx, S, B, step, &phase, pc);
+            if (!process_tile<STRICT, QMODE>(a, a.tiles[t], ctx, S, B, step, &phase, pc)) return;
         }
-        if (!grid_sync(a.bar, a.err)) return;
+        // test hook: this block leaves before the barrier, so the others' wait runs out
+        if (s == 0 && blockIdx.x == a.wait.withhold) return;
+        if (!grid_sync(a.bar, a.err, a.wait.spin_limit)) return;
         pc.mark(9);
         if (blockIdx.x == 0 && tid == 0) atomicExch(a.tile_counter, 0u);
         scan_phase(a, a.start_b[s & 1], epoch0 + s + 1);
         pc.mark(10);
-        if (!grid_sync(a.bar, a.err)) return;
+        if (!grid_sync(a.bar, a.err, a.wait.spin_limit)) return;
         pc.mark(11);
     }
     if (blockIdx.x == 0 && tid == 0) {

@@ -23,6 +23,7 @@
 #include <stdint.h>
 
 #include "kb_common.h"
+#include "kb_launch.h"
 
 namespace kb {
 
@@ -114,6 +115,10 @@ struct FusedArgs {
     uint32_t* err;
     uint32_t* stats;  // [0] tiles that ran through the global scratch path
     unsigned long long* phase_cycles;  // optional [gridDim][16] cycle counters per phase
+    // bounded waits: iterations before a wait gives up (0: the defaults), and
+    // the test hook: block `withhold` of the persistent kernel leaves before
+    // its first grid barrier (~0u: none)
+    WaitCfg wait;
 };
 
 // Largest CTA count that can be co-resident for this layout (0 if none).

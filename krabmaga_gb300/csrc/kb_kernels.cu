@@ -111,8 +111,8 @@ __device__ __forceinline__ void columns_runs(const ForceArgs& a, const Rep& R, i
     for (int k = 0; k < NC; ++k) {
         if (mi + k <= Mi) {
             const uint32_t colbase = R.cell_off + (uint32_t)(mi + k) * (uint32_t)R.dh;
-            s[k] = __ldg(a.start + colbase + mj);
-            e[k] = __ldg(a.start + colbase + Mj + 1);
+            e[k] = min(__ldg(a.start + colbase + Mj + 1), a.n);
+            s[k] = min(__ldg(a.start + colbase + mj), e[k]);
         }
     }
 #pragma unroll
@@ -137,8 +137,8 @@ __device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, 
         s[k] = e[k] = 0u;
         if (mi + k <= Mi) {
             const uint32_t colbase = R.cell_off + (uint32_t)(mi + k) * (uint32_t)R.dh;
-            s[k] = __ldg(a.start + colbase + mj);
-            e[k] = __ldg(a.start + colbase + Mj + 1);
+            e[k] = min(__ldg(a.start + colbase + Mj + 1), a.n);
+            s[k] = min(__ldg(a.start + colbase + mj), e[k]);
         }
     }
     const uint32_t P1 = e[0] - s[0], P2 = P1 + (e[1] - s[1]), T = P2 + (e[2] - s[2]);
@@ -216,14 +216,16 @@ __device__ __forceinline__ void gather_candidates(const ForceArgs& a, const Rep&
                 const uint32_t colbase = R.cell_off + (uint32_t)bx * (uint32_t)R.dh;
                 if (QMODE == 0 && clamped) {
                     if (mj > Mj) continue;
-                    accumulate_run(R, a.st, a.ids, __ldg(a.start + colbase + mj),
-                                   __ldg(a.start + colbase + Mj + 1), me, my_id, acc);
+                    const uint32_t e = min(__ldg(a.start + colbase + Mj + 1), a.n);
+                    accumulate_run(R, a.st, a.ids, min(__ldg(a.start + colbase + mj), e), e, me,
+                                   my_id, acc);
                     continue;
                 }
                 for (int cj = mj; cj <= Mj; ++cj) {
                     const int by = t_transform(cj, R.max_y);
                     const uint32_t c = colbase + (uint32_t)by;
-                    const uint32_t s = __ldg(a.start + c), e = __ldg(a.start + c + 1);
+                    const uint32_t e = min(__ldg(a.start + c + 1), a.n);
+                    const uint32_t s = min(__ldg(a.start + c), e);
                     if (s == e) continue;
                     if (QMODE == 0) {
                         accumulate_run(R, a.st, a.ids, s, e, me, my_id, acc);
@@ -399,8 +401,9 @@ __device__ __forceinline__ unsigned long long pack_tile(uint32_t epoch, unsigned
 
 __global__ void __launch_bounds__(SCAN_THREADS)
     k_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n, ScanCtl* ctl,
-           unsigned long long* tstate, uint32_t* err, int zero_in, uint32_t ntiles) {
+           unsigned long long* tstate, uint32_t* err, int zero_in, uint32_t ntiles, WaitCfg wait) {
     pdl_enter();
+    const uint32_t spin_limit = wait.spin_limit ? wait.spin_limit : SPIN_LIMIT;
     __shared__ uint32_t s_tile, s_epoch, s_prefix;
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -460,14 +463,15 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     // decoupled look-back across tiles, 256 predecessors per round trip
     __shared__ int s_jinc;
     __shared__ uint32_t s_sum[SCAN_THREADS / 32];
+    const bool publish = tile != wait.withhold;  // the test hook withholds one tile's words
     if (tile == 0) {
         if (tid == 0) {
-            atomicExch(&tstate[0], pack_tile(epoch, FLAG_INC, agg));
+            if (publish) atomicExch(&tstate[0], pack_tile(epoch, FLAG_INC, agg));
             s_prefix = 0;
         }
     } else {
         if (tid == 0) {
-            atomicExch(&tstate[tile], pack_tile(epoch, FLAG_AGG, agg));
+            if (publish) atomicExch(&tstate[tile], pack_tile(epoch, FLAG_AGG, agg));
             s_jinc = -0x7fffffff;
         }
         __syncthreads();
@@ -482,7 +486,7 @@ __global__ void __launch_bounds__(SCAN_THREADS)
                     word = *((volatile unsigned long long*)&tstate[j]);
                     if ((uint32_t)(word >> 34) == (epoch & 0x3FFFFFFFu) && ((word >> 32) & 3ull) != 0ull)
                         break;
-                    if (++spins > SPIN_LIMIT) {
+                    if (++spins > spin_limit) {
                         atomicOr(err, ERR_SPIN_TIMEOUT);
                         word = pack_tile(epoch, FLAG_INC, 0u);
                         break;
@@ -512,7 +516,7 @@ __global__ void __launch_bounds__(SCAN_THREADS)
             __syncthreads();
         }
         if (tid == 0) {
-            atomicExch(&tstate[tile], pack_tile(epoch, FLAG_INC, prefix + agg));
+            if (publish) atomicExch(&tstate[tile], pack_tile(epoch, FLAG_INC, prefix + agg));
             s_prefix = prefix;
         }
     }
@@ -575,8 +579,8 @@ __device__ __forceinline__ void rebin_run(const RebinArgs& a, const Rep& R, uint
 }
 
 __device__ __forceinline__ void rebin_cell(const RebinArgs& a, const Rep& R, uint32_t c) {
-    uint32_t dst = __ldg(a.start_next + c);
-    const uint32_t end = __ldg(a.start_next + c + 1);
+    const uint32_t end = min(__ldg(a.start_next + c + 1), a.n);
+    uint32_t dst = min(__ldg(a.start_next + c), end);
     if (dst == end) return;
     const uint32_t local = c - R.cell_off;
     const uint32_t Xu = div_dh(local, R);
@@ -587,8 +591,8 @@ __device__ __forceinline__ void rebin_cell(const RebinArgs& a, const Rep& R, uin
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const uint32_t base = R.cell_off + (uint32_t)(X - 1 + k) * (uint32_t)R.dh + (uint32_t)Y;
-            s[k] = __ldg(a.start_cur + base - 1);
-            e[k] = __ldg(a.start_cur + base + 2);
+            e[k] = min(__ldg(a.start_cur + base + 2), a.n);
+            s[k] = min(__ldg(a.start_cur + base - 1), e[k]);
         }
         if (a.key) {
             // the first keys of every run in flight together
@@ -630,8 +634,8 @@ __device__ __forceinline__ void rebin_cell(const RebinArgs& a, const Rep& R, uin
                 const int sy = src_line(ky, Y, R.max_y, R.seam);
                 if (sy < 0 || sy > R.max_y || sy <= lasty) continue;
                 lasty = sy;
-                rebin_run(a, R, c, __ldg(a.start_cur + colbase + sy),
-                          __ldg(a.start_cur + colbase + sy + 1), dst, end);
+                const uint32_t re = min(__ldg(a.start_cur + colbase + sy + 1), a.n);
+                rebin_run(a, R, c, min(__ldg(a.start_cur + colbase + sy), re), re, dst, end);
             }
         }
     }
@@ -860,12 +864,12 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
     // source runs, in one round trip
     uint32_t lo = 0, hi = 0, b = 0;
     if ((int)lane < nb) {
-        lo = __ldg(a.start_next + c0 + lane);
-        hi = __ldg(a.start_next + c0 + lane + 1);
+        hi = min(__ldg(a.start_next + c0 + lane + 1), a.n);
+        lo = min(__ldg(a.start_next + c0 + lane), hi);
     }
     if (interior && lane < 6u) {
         const uint32_t cb = R.cell_off + (uint32_t)(X - 1 + (int)(lane % 3u)) * (uint32_t)R.dh;
-        b = __ldg(a.start_cur + cb + (lane < 3u ? (uint32_t)(Y0 - 1) : (uint32_t)(Y1 + 2)));
+        b = min(__ldg(a.start_cur + cb + (lane < 3u ? (uint32_t)(Y0 - 1) : (uint32_t)(Y1 + 2))), a.n);
     }
     if (__shfl_sync(FULL_MASK, lo, 0) == __shfl_sync(FULL_MASK, hi, nb - 1)) return;  // no arrivals
     cnt[lane] = 0u;
@@ -877,7 +881,8 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
         const uint32_t s0 = __shfl_sync(FULL_MASK, b, 0), s1 = __shfl_sync(FULL_MASK, b, 1);
         const uint32_t s2 = __shfl_sync(FULL_MASK, b, 2), e0 = __shfl_sync(FULL_MASK, b, 3);
         const uint32_t e1 = __shfl_sync(FULL_MASK, b, 4), e2 = __shfl_sync(FULL_MASK, b, 5);
-        const uint32_t P1 = e0 - s0, P2 = P1 + (e1 - s1), T = P2 + (e2 - s2);
+        // run bounds out of order (only after a failed step) read as empty runs
+        const uint32_t P1 = e0 - min(s0, e0), P2 = P1 + (e1 - min(s1, e1)), T = P2 + (e2 - min(s2, e2));
         for (uint32_t f = 0; f < T; f += 32u) {
             const uint32_t ff = f + lane;
             const uint32_t p = ff < P1 ? s0 + ff : (ff < P2 ? s1 + (ff - P1) : s2 + (ff - P2));
@@ -903,8 +908,8 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
             }
 #pragma unroll 1
             for (int r = 0; r < nr; ++r) {
-                const uint32_t s = __ldg(a.start_cur + cb + (uint32_t)ra[r]);
-                const uint32_t e = __ldg(a.start_cur + cb + (uint32_t)rb[r] + 1u);
+                const uint32_t e = min(__ldg(a.start_cur + cb + (uint32_t)rb[r] + 1u), a.n);
+                const uint32_t s = min(__ldg(a.start_cur + cb + (uint32_t)ra[r]), e);
 #pragma unroll 1
                 for (uint32_t f = s; f < e; f += 32u)
                     seg_batch(a, f + lane < e, f + lane, c0, nb, lo, hi, cnt, lane_lt, bad);
@@ -1332,7 +1337,7 @@ cudaError_t launch_add_u64(unsigned long long* dst, unsigned long long v, cudaSt
 // ====================================================================== launchers
 cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* ctl,
                         unsigned long long* tile_state, uint32_t* err, bool zero_in,
-                        cudaStream_t s) {
+                        cudaStream_t s, WaitCfg wait) {
     const uint32_t nt = scan_tiles(n);
     if (nt == 0) {
         return cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
@@ -1345,7 +1350,8 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
         return launch_pdl(k_scan_tiles, nt2, SCAN_THREADS, s, const_cast<uint32_t*>(in), out, n,
                           tile_state, zero_in ? 1 : 0, nt2);
     }
-    return launch_pdl(k_scan, nt, SCAN_THREADS, s, in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt);
+    return launch_pdl(k_scan, nt, SCAN_THREADS, s, in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt,
+                      wait);
 }
 
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s) {

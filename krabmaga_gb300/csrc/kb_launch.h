@@ -35,11 +35,22 @@ inline uint32_t scan_state_words(uint32_t n) {
     return (a > b ? a : b) + 1u;
 }
 
+// Bounded device waits: the iterations a wait makes before it gives up and
+// raises ERR_SPIN_TIMEOUT (0: the kernel's default), and a test hook that
+// makes one publisher (a look-back scan tile, a persistent block at its first
+// grid barrier) withhold its signal so that a wait runs out on purpose
+// (~0u: none).
+struct WaitCfg {
+    uint32_t spin_limit;
+    uint32_t withhold;
+};
+constexpr WaitCfg WAIT_DEFAULT = {0u, 0xFFFFFFFFu};
+
 // Exclusive scan of in[0..n) into out[0..n]; out[n] = total.  When zero_in,
 // in[] is cleared as it is read (the histogram is ready for the next step).
 cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* ctl,
                         unsigned long long* tile_state, uint32_t* err, bool zero_in,
-                        cudaStream_t s);
+                        cudaStream_t s, WaitCfg wait = WAIT_DEFAULT);
 
 // Flock step agent pass: reads the canonical read buffer (st, ids, start),
 // writes next states into the write list in the same order plus each one's
@@ -129,6 +140,7 @@ struct RebinArgs {
     uint32_t* s_ids;
     unsigned long long* step;
     uint32_t* err;
+    uint32_t n;  // records (every slot index is below it)
 };
 // Bag segments of the segment rebin: SEG_ROWS consecutive bags of one column.
 constexpr int SEG_ROWS = 32;

@@ -387,5 +387,12 @@ class Field2D:
         L.call("kb_field_device_flags", self._h, C.byref(v), C.c_int32(1 if clear else 0))
         return v.value
 
+    def set_wait_test(self, spin_limit: int = 0, withhold: int = 0, index: int = 0) -> None:
+        """Bounded device waits: iterations before a wait gives up (0: the
+        kernels' defaults), and the test hook KB_WITHHOLD_* that makes the
+        look-back tile or persistent block `index` withhold its signal."""
+        L.call("kb_field_set_wait_test", self._h, C.c_uint32(spin_limit), C.c_int32(withhold),
+               C.c_uint32(index))
+
     def synchronize(self) -> None:
         L.call("kb_field_synchronize", self._h)

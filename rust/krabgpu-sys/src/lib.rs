@@ -40,6 +40,9 @@ pub const KB_PATH_TILED: i32 = 2;
 pub const KB_PATH_SMALL: i32 = 3;
 pub const KB_PATH_DENSE: i32 = 4;
 pub const KB_NOALLOC_MAX_QUERIES: usize = 65536;
+pub const KB_WITHHOLD_NONE: i32 = 0;
+pub const KB_WITHHOLD_SCAN_PUBLISH: i32 = 1;
+pub const KB_WITHHOLD_GRID_ARRIVAL: i32 = 2;
 
 #[repr(C)]
 pub struct kb_field {
@@ -216,6 +219,9 @@ extern "C" {
     pub fn kb_field_get_state(f: *mut kb_field, ids: *mut u32, states: *mut f32, cap: usize,
                               n: *mut usize) -> kb_status;
     pub fn kb_field_device_flags(f: *mut kb_field, flags: *mut u32, clear: i32) -> kb_status;
+    // bounded device waits: iteration limit, and the test hook that withholds one signal
+    pub fn kb_field_set_wait_test(f: *mut kb_field, spin_limit: u32, withhold: i32,
+                                  index: u32) -> kb_status;
     pub fn kb_field_synchronize(f: *mut kb_field) -> kb_status;
     // heading moments {boids, sum dx, sum dy, sum |d|}, reduced on the device
     pub fn kb_field_moments(f: *mut kb_field, out4: *mut f64) -> kb_status;
