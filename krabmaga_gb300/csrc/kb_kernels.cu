@@ -834,6 +834,10 @@ __device__ __forceinline__ uint32_t seg_rank(uint32_t k, uint32_t c0, int nb, ui
 }
 
 // One batch of 32 write-list entries (p, valid per lane): rank and copy.
+#ifndef KB_REBIN_BATCHES
+#define KB_REBIN_BATCHES 2
+#endif
+
 __device__ __forceinline__ void seg_batch(const RebinArgs& a, bool valid, uint32_t p, uint32_t c0,
                                           int nb, uint32_t lo, uint32_t hi, uint32_t* cnt,
                                           uint32_t lane_lt, bool& bad) {
@@ -883,10 +887,36 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
         const uint32_t e1 = __shfl_sync(FULL_MASK, b, 4), e2 = __shfl_sync(FULL_MASK, b, 5);
         // run bounds out of order (only after a failed step) read as empty runs
         const uint32_t P1 = e0 - min(s0, e0), P2 = P1 + (e1 - min(s1, e1)), T = P2 + (e2 - min(s2, e2));
-        for (uint32_t f = 0; f < T; f += 32u) {
-            const uint32_t ff = f + lane;
-            const uint32_t p = ff < P1 ? s0 + ff : (ff < P2 ? s1 + (ff - P1) : s2 + (ff - P2));
-            seg_batch(a, ff < T, p, c0, nb, lo, hi, cnt, lane_lt, bad);
+        // KB_REBIN_BATCHES batches of 32 list entries per round: every key of
+        // the round in flight at once, then the ranks in list order, then every
+        // record of the round in flight at once
+        for (uint32_t f0 = 0; f0 < T; f0 += 32u * KB_REBIN_BATCHES) {
+            uint32_t p[KB_REBIN_BATCHES], dst[KB_REBIN_BATCHES];
+#pragma unroll
+            for (int b = 0; b < KB_REBIN_BATCHES; ++b) {
+                const uint32_t ff = f0 + 32u * b + lane;
+                p[b] = ff < P1 ? s0 + ff : (ff < P2 ? s1 + (ff - P1) : s2 + (ff - P2));
+                dst[b] = ff < T ? __ldg(a.key + p[b]) : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for (int b = 0; b < KB_REBIN_BATCHES; ++b)
+                dst[b] = seg_rank(dst[b], c0, nb, lo, hi, cnt, lane_lt, bad);
+            float4 rec[KB_REBIN_BATCHES];
+            uint32_t rid[KB_REBIN_BATCHES];
+#pragma unroll
+            for (int b = 0; b < KB_REBIN_BATCHES; ++b) {
+                if (dst[b] != 0xFFFFFFFFu) {
+                    rec[b] = __ldg(a.a_st + p[b]);
+                    rid[b] = __ldg(a.a_ids + p[b]);
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < KB_REBIN_BATCHES; ++b) {
+                if (dst[b] != 0xFFFFFFFFu) {
+                    a.s_st[dst[b]] = rec[b];
+                    a.s_ids[dst[b]] = rid[b];
+                }
+            }
         }
     } else {
         // a segment at the seam or the field's edge: the source lines of
@@ -921,7 +951,7 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
 }
 
 #ifndef KB_REBIN_MINB
-#define KB_REBIN_MINB 8
+#define KB_REBIN_MINB 6
 #endif
 
 template <bool MULTI, int ROWS = SEG_ROWS>
