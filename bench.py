@@ -229,12 +229,10 @@ def run_sweep(args, dev):
     def batched(mode):
         b = kg.Batch(reps, device=dev)
         b.set_step_options(mode)
-        tx = ty = 0
-        tune_ms = None
-        step = 0
-        if mode in (1, 2):
-            tx, ty, used, tune_ms = b.autotune(0, 4)
-            step = used
+        # the autotuner's trials are real steps of the sweep: the tile shape of
+        # the tiled modes, the force block size of the separate kernels
+        tx, ty, used, tune_ms = b.autotune(0, 4)
+        step = used
         b.step(step, 10, 1, 0)
         step += 10
         b.synchronize()
@@ -256,7 +254,9 @@ def run_sweep(args, dev):
         stats = b.step_stats()
         b.close()
         return {"mode": mode, "value": total * steps / bs, "ms_per_step": 1e3 * bs / steps,
-                "autotuned_tile": [tx, ty], "autotune_ms_per_step": tune_ms, "fused": stats,
+                "autotuned": ({"tile": [tx, ty]} if mode in (1, 2)
+                              else {"force_block_threads": tx, "replicas_per_block": ty}),
+                "autotune_ms_per_step": tune_ms, "fused": stats,
                 "one_launch_value": one}
 
     runs = [batched(m) for m in (2, 0)]
@@ -286,8 +286,9 @@ def run_sweep(args, dev):
         "batched_value": bv, "plain_replica_by_replica_value": pv, "speedup": bv / pv,
         "unit": UNIT, "batched_ms_per_step": best["ms_per_step"], "best_mode": best["mode"],
         "modes": runs,
-        "launch": "mode 2: tile step + scan per step; mode 0: force + scan + rebin per step over "
-                  "all replicas; CUDA graphs of 100 steps",
+        "launch": "mode 2: tile step + scan per step, CUDA graphs of 100 steps; mode 0: force + "
+                  "offsets scan (two launches) + rebin per step over all replicas, launched per "
+                  "step with programmatic dependent launch",
         "data": "synthetic (seeded)", "l2": "working set larger than L2 (no flush)",
     }
 

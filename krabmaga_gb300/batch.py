@@ -141,8 +141,12 @@ class Batch:
         return ids[: n.value], st[: n.value]
 
     def autotune(self, first_step: int, steps_per_trial: int = 5, candidates=None):
-        """Pick the fastest tile shape by timing real steps; returns
-        (tx, ty, steps consumed, ms per step)."""
+        """Pick the fastest launch shape by timing real steps.  Tiled step
+        modes (1, 2): the tile shape, candidates (tx, ty), returns (tx, ty,
+        steps consumed, ms per step).  Separate kernels (modes 0, 3): the force
+        pass's threads per block over the packed replicas, candidates
+        (threads, 1) with threads 128, 256 or 512 and one replica per block,
+        returns (threads, 1, steps consumed, ms per step)."""
         cand = None
         nc = 0
         if candidates:

@@ -221,7 +221,7 @@ kb_status build_rep_blocks(kb_field* f) {
     bs.clear();
     for (uint32_t r = 0; r < (uint32_t)f->reps.size(); ++r) {
         const Rep& R = f->reps[r];
-        for (uint64_t i = 0; i < R.nboids; i += FORCE_THREADS) bf.push_back(make_uint2(r, R.boid_off + (uint32_t)i));
+        for (uint64_t i = 0; i < R.nboids; i += f->force_block) bf.push_back(make_uint2(r, R.boid_off + (uint32_t)i));
         const uint32_t ns = rep_segments(R);
         for (uint32_t g = 0; g < ns; g += REBIN_SEG_WARPS) bs.push_back(make_uint2(r, R.seg_off + g));
     }
@@ -510,6 +510,7 @@ kb_status enqueue_force(kb_field* f, const kb_flock_params* p) {
     a.nblk = f->nblk_force;
     a.self_by_slot = f->ids_unique ? 1 : 0;
     a.dense = f->dense ? 1 : 0;
+    a.block_threads = f->force_block;
     KB_CUDA(launch_flock_force(a, p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
     f->hist_counted = true;
     return KB_OK;
@@ -563,7 +564,12 @@ FusedCfg fused_config(const kb_field* f, int dd) {
     c.tx = f->tile_tx > 0 ? f->tile_tx : 16;
     c.ty = f->tile_ty > 0 ? f->tile_ty : 32;
     c.dd = dd;
-    const double rho = (double)f->rn / (double)f->ncells_total;
+    // mean bag occupancy of the densest replica: every tile's capacity must hold
+    // the densest replica's tiles (replicas of one sweep differ several-fold)
+    double rho = (double)f->rn / (double)f->ncells_total;  // a plain field: its mean
+    if (f->is_batch)
+        for (const Rep& R : f->reps)
+            if (R.ncells) rho = std::max(rho, (double)R.nboids / (double)R.ncells);
     const double staged_cells = (double)(c.tx + 2 * dd + 2) * (c.ty + 2 * dd + 2);
     const double sord_cells = (double)(c.tx + 2 * dd) * (c.ty + 2 * dd);
     auto cap = [](double mean) {
@@ -1633,6 +1639,63 @@ kb_status kb_field_phase_clocks(kb_field* f, int32_t enable, unsigned long long*
 
 // Time `steps` fused steps under each candidate tile shape (real steps of
 // the simulation, numbered from first_step) and keep the fastest shape.
+kb_status autotune_force_block(kb_field* f, uint64_t first_step, uint32_t steps,
+                               const int32_t* cand, int32_t ncand, int32_t* best_out,
+                               float* best_ms_out, kb_status (*run)(void*, uint64_t, uint32_t),
+                               void* ctx) {
+    static const int32_t defaults[] = {128, 1, 256, 1, 512, 1};
+    if (!cand || ncand <= 0) {
+        cand = defaults;
+        ncand = 3;
+    }
+    for (int32_t i = 0; i < ncand; ++i) {
+        const int32_t t = cand[2 * i];
+        if ((t != 128 && t != 256 && t != 512) || cand[2 * i + 1] != 1)
+            return fail(KB_ERR_ARG, "candidate " + std::to_string(i) +
+                                        ": force blocks of 128, 256 or 512 threads, one replica per block");
+    }
+    cudaEvent_t e0, e1;
+    KB_CUDA(cudaEventCreate(&e0));
+    KB_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_i = -1;
+    uint64_t step = first_step;
+    kb_status st = KB_OK;
+    auto use = [&](int32_t t) -> kb_status {
+        if (f->force_block == (uint32_t)t) return KB_OK;
+        f->force_block = (uint32_t)t;
+        f->drop_graphs();  // the block table's length is baked into captured launches
+        return build_rep_blocks(f);
+    };
+    for (int32_t i = 0; i < ncand && !st; ++i) {
+        if ((st = use(cand[2 * i]))) break;
+        if ((st = run(ctx, step, 1))) break;  // warms up
+        step += 1;
+        if (cudaEventRecord(e0, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        if ((st = run(ctx, step, steps))) break;
+        step += steps;
+        if (cudaEventRecord(e1, f->stream) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        if (cudaEventSynchronize(e1) != cudaSuccess) { st = fail(KB_ERR_CUDA, "event"); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            best_i = i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    if ((st = use(cand[2 * best_i]))) return st;
+    if (best_out) {
+        best_out[0] = (int32_t)f->force_block;
+        best_out[1] = 1;
+        best_out[2] = (int32_t)(step - first_step);  // steps consumed
+    }
+    if (best_ms_out) *best_ms_out = best / (float)steps;
+    return KB_OK;
+}
+
 kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_step,
                                 uint32_t steps, const int32_t* cand, int32_t ncand,
                                 int32_t* best_out, float* best_ms_out,

@@ -225,9 +225,15 @@ kb_status kb_batch_autotune(kb_batch* b, uint64_t first_step, uint32_t steps_per
                             float* ms_per_step) try {
     if (!b || steps_per_trial == 0) return fail(KB_ERR_ARG, "null argument or zero steps");
     DeviceGuard g(b->f->device);
-    if (!fused_eligible(b->f, &b->common)) return fail(KB_ERR_STATE, "batch not eligible for the fused step");
-    return autotune_tiles(b->f, &b->common, first_step, steps_per_trial, candidates, ncand, best,
-                          ms_per_step, run_batch_steps, b);
+    if (b->f->fused_mode == 1 || b->f->fused_mode == 2) {
+        if (!fused_eligible(b->f, &b->common))
+            return fail(KB_ERR_STATE, "batch not eligible for the fused step");
+        return autotune_tiles(b->f, &b->common, first_step, steps_per_trial, candidates, ncand,
+                              best, ms_per_step, run_batch_steps, b);
+    }
+    // the separate kernels: the force pass's block size over the packed replicas
+    return autotune_force_block(b->f, first_step, steps_per_trial, candidates, ncand, best,
+                                ms_per_step, run_batch_steps, b);
 } catch (...) {
     return kb::exception_status();
 }

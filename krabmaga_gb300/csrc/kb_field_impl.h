@@ -62,6 +62,7 @@ struct kb_field {
     DevBuf<uint2> blk_force, blk_seg;
     std::vector<uint2> blk_force_h, blk_seg_h;
     uint32_t nblk_force = 0, nblk_seg = 0;
+    uint32_t force_block = FORCE_THREADS;  // threads per force block over packed replicas
     DevBuf<float4> tst;
     DevBuf<ScanCtl> scan_ctl, aux_ctl;
     DevBuf<unsigned long long> tstate, aux_tstate;
@@ -234,6 +235,13 @@ kb_status autotune_tiles(kb_field* f, const kb_flock_params* p, uint64_t first_s
                          uint32_t steps, const int32_t* cand, int32_t ncand, int32_t* best_out,
                          float* best_ms_out, kb_status (*run)(void*, uint64_t, uint32_t),
                          void* ctx);
+// The same over the force pass's block size of packed replicas (separate
+// kernels): candidates are pairs {threads, replicas per block}, threads one of
+// FORCE_BLOCK_SIZES and one replica per block (nullptr: every block size).
+kb_status autotune_force_block(kb_field* f, uint64_t first_step, uint32_t steps,
+                               const int32_t* cand, int32_t ncand, int32_t* best_out,
+                               float* best_ms_out, kb_status (*run)(void*, uint64_t, uint32_t),
+                               void* ctx);
 // Whether every replica's ids are distinct (checked on the device) / set it.
 kb_status check_unique_ids(kb_field* f);
 void set_ids_unique(kb_field* f, bool u);

@@ -307,8 +307,10 @@ __device__ __forceinline__ void load_rep_shared(Rep* dst, const Rep* src) {
         reinterpret_cast<uint32_t*>(dst)[threadIdx.x] = __ldg(reinterpret_cast<const uint32_t*>(src) + threadIdx.x);
 }
 
-template <bool STRICT, int QMODE, bool MULTI, bool DENSE = false>
-__global__ void __launch_bounds__(KB_FORCE_THREADS, MULTI ? KB_FORCE_MINB_MULTI : KB_FORCE_MINB)
+// BT: threads per block (the packed-replica block table's granularity); the
+// same 48 warps per SM at every block size.
+template <bool STRICT, int QMODE, bool MULTI, bool DENSE = false, int BT = KB_FORCE_THREADS>
+__global__ void __launch_bounds__(BT, (MULTI ? KB_FORCE_MINB_MULTI : KB_FORCE_MINB) * KB_FORCE_THREADS / BT)
     k_flock_force(ForceArgs a) {
     pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1389,7 +1391,16 @@ cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaS
     const bool multi = a.nrep > 1;
     if (multi && a.blk == nullptr) return cudaErrorInvalidValue;
     const unsigned g = multi ? a.nblk : grid_for(a.n, KB_FORCE_THREADS);
-#define KB_FORCE(S, Q, MU) return launch_pdl(k_flock_force<S, Q, MU>, g, KB_FORCE_THREADS, s, a)
+#define KB_FORCE(S, Q, MU)                                                                      \
+    do {                                                                                        \
+        if constexpr (MU) {                                                                     \
+            if (a.block_threads == 128)                                                         \
+                return launch_pdl(k_flock_force<S, Q, MU, false, 128>, g, 128, s, a);           \
+            if (a.block_threads == 512)                                                         \
+                return launch_pdl(k_flock_force<S, Q, MU, false, 512>, g, 512, s, a);           \
+        }                                                                                       \
+        return launch_pdl(k_flock_force<S, Q, MU>, g, KB_FORCE_THREADS, s, a);                  \
+    } while (0)
     if (a.dense && qmode == 0 && !multi) {
         if (strict) return launch_pdl(k_flock_force<true, 0, false, true>, g, KB_FORCE_THREADS, s, a);
         return launch_pdl(k_flock_force<false, 0, false, true>, g, KB_FORCE_THREADS, s, a);

@@ -81,8 +81,13 @@ struct ForceArgs {
     // run with a plain pointer instead of the flat index formula (the same
     // visiting order, fewer instructions per candidate)
     int32_t dense;
+    // several replicas: threads per block of the block table (FORCE_BLOCKS_*;
+    // 0: FORCE_THREADS), the launch shape the batch autotuner picks
+    uint32_t block_threads;
 };
 constexpr int FORCE_THREADS = 256;  // the force kernel's block (one replica per block)
+// Block sizes of the force pass over packed replicas (one replica per block).
+constexpr int FORCE_BLOCK_SIZES[3] = {128, 256, 512};
 cudaError_t launch_flock_force(const ForceArgs& a, bool strict, int qmode, cudaStream_t s);
 // Whole steps of a small single-replica field in one cluster of SMALL_CTAS
 // blocks (kb_small.cu): every block loads the read buffer (st, ids, start

@@ -218,3 +218,31 @@ def test_batch_closes_as_a_context_manager(gpu):
     oids, ost = oracle_run(reps[1], 3)
     assert np.array_equal(ids, oids) and same_bits(st, ost)
     assert b.handle is None
+
+
+@pytest.mark.parametrize("threads", [128, 256, 512])
+def test_mode0_force_block_sizes_match_oracle(gpu, threads):
+    # the separate-kernel step over packed replicas at each force block size
+    # the autotuner may pick (one candidate: the autotuner keeps it)
+    reps = small_sweep(kg.KB_ARITH_STRICT)
+    b = kg.Batch(reps)
+    b.set_step_options(0)
+    t, per_block, used, ms = b.autotune(0, 2, candidates=[(threads, 1)])
+    assert (t, per_block) == (threads, 1) and used == 3 and ms > 0
+    b.step(used, 9, 1, 0)
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, used + 9)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
+
+
+def test_mode0_autotune_picks_a_block_size_and_refuses_others(gpu):
+    reps = small_sweep(kg.KB_ARITH_FAST)
+    b = kg.Batch(reps)
+    b.set_step_options(0)
+    t, per_block, used, ms = b.autotune(0, 2)
+    assert t in (128, 256, 512) and per_block == 1 and used == 9
+    for bad in [[(64, 1)], [(256, 2)]]:
+        with pytest.raises(kg.KbError) as e:
+            b.autotune(used, 2, candidates=bad)
+        assert e.value.status == L.KB_ERR_ARG
