@@ -293,6 +293,54 @@ def run_sweep(args, dev):
     }
 
 
+def run_configs(args, dev):
+    """The other configurations of the workload table at their own sizes,
+    fast arithmetic: C1 (1,000 boids, torus 200, seed 42, 200 steps: one call,
+    whole steps on the thread-block cluster path; and end to end from host
+    arrays) and C3 (4,194,304 boids in 256 Gaussian clusters, torus 12952,
+    seed 11: graph-replayed steps on inputs larger than L2)."""
+    import torch
+
+    import krabmaga_gb300 as kg
+    from krabmaga_gb300 import _lib as L
+
+    out = {}
+    for name, steps in (("flock1k", 200), ("clustered4m", args.c3_steps)):
+        wl = WORKLOADS[name]
+        ids, xy, dxy = gen(wl, kg)
+        p = kg.FlockParams(seed=wl["seed"], arith=kg.KB_ARITH_FAST).to_c()
+        f = kg.Field2D(wl["side"], wl["side"], D_C, True, device=dev, capacity_hint=wl["n"])
+        f.set_locations(ids, xy, dxy)
+        f.lazy_update()
+        L.call("kb_flock_step", f.handle, C.byref(p), C.c_uint64(0), C.c_uint32(steps))  # warm-up
+        f.synchronize()
+        stream = torch.cuda.ExternalStream(f.cuda_stream(), device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.call("kb_flock_step", f.handle, C.byref(p), C.c_uint64(steps), C.c_uint32(steps))
+        e1.record(stream)
+        f.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        entry = {"workload": wl["desc"], "steps": steps, "value": wl["n"] * steps / sec,
+                 "unit": UNIT, "ms_per_step": 1e3 * sec / steps, "path": f.step_path(),
+                 "candidate_walk": "per-run (dense)" if f.dense_active() else "flat"}
+        f.close()
+        if name == "flock1k":
+            t0 = time.perf_counter()
+            g = kg.Field2D(wl["side"], wl["side"], D_C, True, device=dev, capacity_hint=wl["n"])
+            g.set_locations(ids, xy, dxy)
+            g.lazy_update()
+            L.call("kb_flock_step", g.handle, C.byref(p), C.c_uint64(0), C.c_uint32(steps))
+            g.get_state()
+            t1 = time.perf_counter()
+            g.close()
+            entry["e2e"] = {"value": wl["n"] * steps / (t1 - t0), "unit": UNIT,
+                            "call": f"create + set_locations + lazy_update + {steps} steps + "
+                                    f"get_state, host arrays in and out"}
+        out[name] = entry
+    return out
+
+
 def run_serving(args, dev):
     """Served request stream: Poisson arrivals (`serve_rate` per second for
     `serve_seconds`), each a Flockers simulation with N log-uniform over
@@ -517,6 +565,7 @@ def run_ours(args, wl):
     traffic = ncu_traffic(kname) if kernels else None
     clocks = clk.summary()
 
+    configs = run_configs(args, dev) if (args.c3_steps > 0 and ws == 1) else None
     sweep = run_sweep(args, dev) if (args.sweep_reps > 0 and ws == 1) else None
     serving = run_serving(args, dev) if (args.serve_seconds > 0 and ws == 1) else None
 
@@ -559,6 +608,7 @@ def run_ours(args, wl):
         # bag-occupancy measurement that the field launches every 64 steps
         "gpu_launches": K * ({2: 3, 1: 1}.get(args.mode) or (1 + len(kernels) if kernels else 3))
                         + (((args.warmup + K) // 64 - args.warmup // 64) if args.mode == 0 else 0),
+        "configs": configs,
         "sweep": sweep,
         "serving": serving,
     }
@@ -586,6 +636,8 @@ def main():
     ap.add_argument("--profile-call-steps", type=int, default=1,
                     help="with --profile: steps per kb_flock_step call (runs of 2 or more take "
                          "the cluster path on fields of at most 4096 boids)")
+    ap.add_argument("--c3-steps", type=int, default=20,
+                    help="steps of the C1/C3 configuration runs (0: skip them)")
     ap.add_argument("--sweep-reps", type=int, default=512)
     ap.add_argument("--sweep-steps", type=int, default=500)
     ap.add_argument("--serve-seconds", type=float, default=60.0)

@@ -320,6 +320,14 @@ kb_status kb_field_neighbor_digest_noalloc(kb_field* f, int32_t kind, float dist
  * allocates nothing. */
 kb_status kb_debug_allocation_counts(uint64_t* allocs, uint64_t* frees);
 
+/* No counterpart in the reference.  Allocation-failure injection for testing
+ * failure handling on the host: the next `count` device allocations the
+ * library attempts fail as if the device were out of memory (no cudaMalloc
+ * is made for them); 0 ends the injection.  Calls that need an allocation
+ * then return KB_ERR_OOM, and the request server fails the requests of the
+ * epoch that met it and carries on with the next ones. */
+kb_status kb_debug_fail_allocations(uint32_t count);
+
 /* ------------------------------------------------------ batched replicas */
 /* Many independent Flockers simulations (the model-exploration workload of
  * explore_parallel!, src/explore/model_exploration.rs:354-432: one

@@ -200,6 +200,7 @@ _SIGS = {
     "kb_field_neighbor_digest_noalloc": (
         C.c_int32, [_P, C.c_int32, C.c_float, C.c_size_t, _F, _U32, _U32]),
     "kb_debug_allocation_counts": (C.c_int32, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "kb_debug_fail_allocations": (C.c_int32, [C.c_uint32]),
     "kb_batch_create": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(ReplicaDesc), C.POINTER(_P)]),
     "kb_batch_destroy": (C.c_int32, [_P]),
     "kb_batch_set_replica": (C.c_int32, [_P, C.c_uint32, C.c_size_t, _U32, _F, _F]),
@@ -267,3 +268,9 @@ def allocation_counts():
     a, f = C.c_uint64(), C.c_uint64()
     call("kb_debug_allocation_counts", C.byref(a), C.byref(f))
     return int(a.value), int(f.value)
+
+
+def fail_allocations(count: int) -> None:
+    """The next `count` device allocations of the library fail as if the device
+    were out of memory (testing failure handling); 0 ends it."""
+    call("kb_debug_fail_allocations", C.c_uint32(count))

@@ -21,6 +21,7 @@ namespace kb {
 thread_local std::string g_last_error;
 
 std::atomic<unsigned long long> g_dev_allocs{0}, g_dev_frees{0};
+std::atomic<long long> g_fail_allocs{0};
 
 kb_status fail(kb_status code, const std::string& msg) {
     g_last_error = msg;
@@ -1082,6 +1083,13 @@ kb_status kb_debug_allocation_counts(uint64_t* allocs, uint64_t* frees) try {
     if (!allocs || !frees) return fail(KB_ERR_ARG, "null argument");
     *allocs = g_dev_allocs.load(std::memory_order_relaxed);
     *frees = g_dev_frees.load(std::memory_order_relaxed);
+    return KB_OK;
+} catch (...) {
+    return kb::exception_status();
+}
+
+kb_status kb_debug_fail_allocations(uint32_t count) try {
+    g_fail_allocs.store((long long)count, std::memory_order_relaxed);
     return KB_OK;
 } catch (...) {
     return kb::exception_status();

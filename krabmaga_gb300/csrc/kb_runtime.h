@@ -17,6 +17,10 @@ namespace kb {
 // Device allocations and frees made by the library (every one goes through
 // DevBuf), for kb_debug_allocation_counts.
 extern std::atomic<unsigned long long> g_dev_allocs, g_dev_frees;
+// Allocation-failure injection (kb_debug_fail_allocations): while positive,
+// each device allocation fails as if the device were out of memory, without
+// calling cudaMalloc, and takes one off the count.
+extern std::atomic<long long> g_fail_allocs;
 
 template <typename T>
 struct DevBuf {
@@ -29,6 +33,9 @@ struct DevBuf {
     cudaError_t alloc(size_t count) {
         release();
         if (count == 0) return cudaSuccess;
+        if (g_fail_allocs.load(std::memory_order_relaxed) > 0 &&
+            g_fail_allocs.fetch_sub(1, std::memory_order_relaxed) > 0)
+            return cudaErrorMemoryAllocation;
         g_dev_allocs.fetch_add(1, std::memory_order_relaxed);
         cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
         if (e != cudaSuccess) {

@@ -149,6 +149,7 @@ void srv_fail_all(kb_server* S, std::vector<SrvReq*>& act, const std::string& wh
         S->failed++;
     }
     act.clear();
+    S->active.clear();  // the snapshot wait_idle reads: nothing runs until the next admission
     S->cv_done.notify_all();
 }
 

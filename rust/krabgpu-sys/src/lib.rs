@@ -241,6 +241,8 @@ extern "C" {
                                             digest: *mut u32) -> kb_status;
     // device allocations and frees the library has made in this process
     pub fn kb_debug_allocation_counts(allocs: *mut u64, frees: *mut u64) -> kb_status;
+    // allocation-failure injection: the next `count` device allocations fail
+    pub fn kb_debug_fail_allocations(count: u32) -> kb_status;
 
     // ---- batched replicas: the runs of explore_parallel! (model_exploration.rs:354-432)
     pub fn kb_batch_create(device: i32, nrep: u32, reps: *const kb_replica_desc,

@@ -125,3 +125,49 @@ def test_server_closes_with_requests_pending(gpu):
         for r in reqs:
             srv.submit(r)
     assert srv._h is None
+
+
+def test_allocation_failure_fails_an_epoch_and_the_server_carries_on(gpu):
+    """Allocation-failure injection on the host (no GPU fault): the device
+    allocations of the server's first repack fail as if HBM were exhausted,
+    so the requests of that epoch fail (their poll reports the error) while the server keeps
+    running; once the injection ends, later requests complete and equal the
+    same simulations run alone."""
+    reqs = small_stream(kg.KB_ARITH_FAST, 6)
+    srv = kg.Server(max_slots=2, quantum_steps=16, max_request_boids=8000,
+                    arith=kg.KB_ARITH_FAST)
+    try:
+        L.fail_allocations(1000)
+        first = [srv.submit(r) for r in reqs[:2]]
+        srv.wait_idle(60.0)
+        L.fail_allocations(0)
+        for t in first:  # a failed request's poll reports its error
+            with pytest.raises(kg.KbError) as e:
+                srv.poll(t)
+            assert e.value.status == L.KB_ERR_STATE and "out of memory" in str(e.value)
+        st = srv.stats()
+        assert st["failed"] == 2 and st["completed"] == 0
+        later = [srv.submit(r) for r in reqs[2:]]
+        srv.wait_idle(120.0)
+        st = srv.stats()
+        assert st["completed"] == len(reqs) - 2 and st["failed"] == 2
+        for t, r in zip(later, reqs[2:]):
+            assert srv.poll(t)[0] == 2
+            ids, s = srv.result(t, r.nboids)
+            ai, a_s = alone(r)
+            assert np.array_equal(ids, ai) and same_bits(s, a_s), f"request {t}"
+    finally:
+        L.fail_allocations(0)
+        srv.close()
+
+
+def test_allocation_failure_reaches_a_field_call_as_oom(gpu):
+    L.fail_allocations(1000)
+    try:
+        with pytest.raises(kg.KbError) as e:
+            kg.Field2D(100.0, 100.0, 6.0, True, capacity_hint=1000)
+        assert e.value.status == L.KB_ERR_OOM
+    finally:
+        L.fail_allocations(0)
+    f = kg.Field2D(100.0, 100.0, 6.0, True, capacity_hint=1000)  # fine again
+    f.close()
