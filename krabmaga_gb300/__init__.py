@@ -13,8 +13,8 @@ from .field import Bird, Field2D, Real2D
 from .batch import Batch, Replica, sweep_replicas
 from .serve import Request, Server, request_stream
 from .explore import (ExploreMode, FlockerConfig, bayesian_search, build_configurations,
-                      evolutionary_search, explore, flock_objective, gen_param, load_csv,
-                      random_search, write_csv)
+                      evolutionary_search, explore, explore_distributed, flock_objective,
+                      gen_param, load_csv, random_search, write_csv)
 from .model import (Agent, AgentImpl, FlockParams, Flocker, Schedule, State, gen_clustered,
                     gen_uniform, simulate, simulate_old)
 
@@ -27,7 +27,8 @@ __all__ = [
     "KB_PATH_SEPARATE", "KB_PATH_FUSED", "KB_PATH_TILED", "KB_PATH_SMALL", "KB_PATH_DENSE",
     "KB_FLAG_KEY_RANGE", "KB_FLAG_REBIN_MISS", "KB_FLAG_SPIN_TIMEOUT", "KB_FLAG_NONFINITE",
     "Batch", "Replica", "sweep_replicas", "Request", "Server", "request_stream",
-    "ExploreMode", "FlockerConfig", "build_configurations", "explore", "random_search",
+    "ExploreMode", "FlockerConfig", "build_configurations", "explore", "explore_distributed",
+    "random_search",
     "evolutionary_search", "write_csv", "bayesian_search", "flock_objective", "gen_param",
     "load_csv",
 ]

@@ -95,16 +95,10 @@ def _replica(cfg: FlockerConfig, seed: int) -> Replica:
     return Replica(side, side, float(d), params, state)
 
 
-def explore(nstep: int, rep_conf: int, inputs: Dict[str, Sequence], outputs: Sequence[str],
-            mode: ExploreMode = ExploreMode.Exaustive, base: Optional[FlockerConfig] = None,
-            device: int = 0) -> List[dict]:
-    """Run every configuration rep_conf times for nstep steps, all runs as one
-    device batch, and return the dataframe rows: "Simulation" (configuration
-    index), "Run" (0-based, as explore_parallel!), the inputs, the outputs,
-    "Run Duration" (seconds of the whole batch) and "Step per sec".
-
-    With ExploreMode.Matched every input must have the same length."""
-    base = base or FlockerConfig()
+def _configurations(inputs: Dict[str, Sequence], outputs: Sequence[str], mode: ExploreMode,
+                    base: FlockerConfig) -> Tuple[List[str], List[list], List[FlockerConfig]]:
+    """The input names, each configuration's input values and its
+    FlockerConfig, in the reference's configuration order."""
     names = list(inputs)
     values = [list(inputs[k]) for k in names]
     for o in outputs:
@@ -120,28 +114,99 @@ def explore(nstep: int, rep_conf: int, inputs: Dict[str, Sequence], outputs: Seq
             raise ValueError("ExploreMode.Matched needs inputs of equal length")
         n_conf = lens.pop() if lens else 1
         conf_values = [[v[i] for v in values] for i in range(n_conf)]
-    if n_conf == 0 or rep_conf <= 0:
-        return []
     conf_list = []
     for vals in conf_values:
         cfg = base
         for k, v in zip(names, vals):
             cfg = _apply(cfg, k, v)
         conf_list.append(cfg)
-    reps = [_replica(conf_list[i], base.init_seed + i * rep_conf + j)
-            for i in range(n_conf) for j in range(rep_conf)]
-    mom, secs = _run_batch_timed(reps, nstep, device)
+    return names, conf_values, conf_list
+
+
+def _rows(confs: Sequence[int], labels: Sequence[int], rep_conf: int, names: Sequence[str],
+          conf_values: Sequence[list], conf_list: Sequence[FlockerConfig], outputs: Sequence[str],
+          nstep: int, base: FlockerConfig, device: int, runner: Optional[Callable]) -> List[dict]:
+    """Run rep_conf runs of each configuration in confs as one batch; row k
+    of configuration confs[i] is labelled Simulation labels[i], Run k.  Run
+    k of configuration g starts from Philox(init_seed + g * rep_conf + k)."""
+    if not confs:
+        return []
+    reps = [_replica(conf_list[g], base.init_seed + g * rep_conf + j)
+            for g in confs for j in range(rep_conf)]
+    mom, secs = (runner or _run_batch_timed)(reps, nstep, device)
     rows = []
-    for i in range(n_conf):
+    for i, g in enumerate(confs):
         for j in range(rep_conf):
-            row = {"Simulation": i, "Run": j}
-            row.update({k: v for k, v in zip(names, conf_values[i])})
+            row = {"Simulation": labels[i], "Run": j}
+            row.update({k: v for k, v in zip(names, conf_values[g])})
             m = mom[i * rep_conf + j]
             row.update({o: OUTPUTS[o](m) for o in outputs})
             row["Run Duration"] = secs
             row["Step per sec"] = nstep / secs if secs > 0 else float("inf")
             rows.append(row)
     return rows
+
+
+def explore(nstep: int, rep_conf: int, inputs: Dict[str, Sequence], outputs: Sequence[str],
+            mode: ExploreMode = ExploreMode.Exaustive, base: Optional[FlockerConfig] = None,
+            device: int = 0, runner: Optional[Callable] = None) -> List[dict]:
+    """Run every configuration rep_conf times for nstep steps, all runs as one
+    device batch, and return the dataframe rows: "Simulation" (configuration
+    index), "Run" (0-based, as explore_parallel!), the inputs, the outputs,
+    "Run Duration" (seconds of the whole batch) and "Step per sec".
+
+    With ExploreMode.Matched every input must have the same length.
+    runner(replicas, nstep, device) -> (moments [nrep, 4], seconds) replaces
+    the device batch (tests run the oracle there)."""
+    base = base or FlockerConfig()
+    names, conf_values, conf_list = _configurations(inputs, outputs, mode, base)
+    n_conf = len(conf_list)
+    if n_conf == 0 or rep_conf <= 0:
+        return []
+    return _rows(list(range(n_conf)), list(range(n_conf)), rep_conf, names, conf_values,
+                 conf_list, outputs, nstep, base, device, runner)
+
+
+def explore_distributed(nstep: int, rep_conf: int, inputs: Dict[str, Sequence],
+                        outputs: Sequence[str], mode: ExploreMode = ExploreMode.Exaustive,
+                        base: Optional[FlockerConfig] = None, group=None,
+                        device: Optional[int] = None,
+                        runner: Optional[Callable] = None) -> List[dict]:
+    """explore_distributed_mpi! (src/explore/mpi/model_exploration.rs:120-300)
+    over the ranks of a torch.distributed group, one GPU per rank: the
+    replicas-only sharding of an exploration.
+
+    As in the reference, rank r takes configurations r, r + P, r + 2P, ...
+    (P ranks; the first n_conf % P ranks take one more), runs each of them
+    rep_conf times (rep_conf <= 0 counts as 1), here all as one device batch
+    on its GPU, and rank 0 gathers every rank's rows in rank order (the
+    gather_varcount_into_root of the reference).  Rank 0 returns the whole
+    dataframe, the other ranks an empty list.  "Simulation" is the
+    configuration's index among its rank's configurations, as the reference
+    writes it (conf_num = i); the input columns name the configuration.  A
+    run starts from the same Philox stream as in explore, so every row equals
+    the single-process row of the same configuration and run.
+
+    device: this rank's GPU (default: LOCAL_RANK); runner as in explore."""
+    import os
+
+    import torch.distributed as dist
+
+    base = base or FlockerConfig()
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    if device is None:
+        device = int(os.environ.get("LOCAL_RANK", "0"))
+    rep_conf = max(int(rep_conf), 1)
+    names, conf_values, conf_list = _configurations(inputs, outputs, mode, base)
+    mine = list(range(rank, len(conf_list), world))
+    rows = _rows(mine, list(range(len(mine))), rep_conf, names, conf_values, conf_list, outputs,
+                 nstep, base, device, runner)
+    root = dist.get_global_rank(group, 0) if group is not None else 0
+    parts = [None] * world if rank == 0 else None
+    dist.gather_object(rows, parts, dst=root, group=group)
+    if rank != 0:
+        return []
+    return [r for part in parts for r in part]
 
 
 def _debug(v) -> str:

@@ -172,3 +172,64 @@ def test_bayesian_search_over_flock_runs(gpu):
 
     x, y = ex.bayesian_search(lambda: [[0.1], [2.0]], f, gen, 4)
     assert 0.0 <= x[0] <= 3.0 and 0.0 <= y <= 1.0
+
+
+def _dist_rank(rank, world, port, q):
+    import os
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world),
+                      RANK=str(rank))
+    sys.path.insert(0, root)
+    import torch.distributed as dist
+
+    import krabmaga_gb300 as kg
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        rows = kg.explore_distributed(*_dist_args(), device=0)
+        q.put((rank, rows))
+    finally:
+        dist.destroy_process_group()
+
+
+def _dist_args():
+    base = kg.FlockerConfig(initial_flockers=300, dim=110.0, init_seed=21,
+                            params=kg.FlockParams(arith=kg.KB_ARITH_STRICT))
+    return (15, 2, {"cohesion": [0.5, 1.0, 1.5], "jump": [0.4, 0.9]}, ["order", "mean_speed", "boids"],
+            kg.ExploreMode.Exaustive, base)
+
+
+def test_distributed_exploration_equals_the_single_process_rows(gpu):
+    """explore_distributed on two ranks (two processes sharing this GPU, each
+    running its own batch; a gloo group gathers the rows): rank 0's dataframe
+    holds every single-process row, regrouped by rank in the reference's
+    round-robin order, with the same outputs."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_dist_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=300) for _ in range(2))
+    for p in procs:
+        p.join(60)
+    assert all(p.exitcode == 0 for p in procs)
+    single = kg.explore(*_dist_args())
+    assert got[1] == [] and len(got[0]) == len(single) == 12
+    expect = []
+    for r in range(2):
+        for i, g in enumerate(range(r, 6, 2)):
+            for j in range(2):
+                expect.append(dict(single[2 * g + j], Simulation=i))
+    timing = ("Run Duration", "Step per sec")
+    for a, b in zip(got[0], expect):
+        assert {k: v for k, v in a.items() if k not in timing} == \
+            {k: v for k, v in b.items() if k not in timing}
