@@ -192,16 +192,19 @@ struct Acc {
     // toroidal_distance's first branch is taken for every pair when the
     // replica guarantees it (Rep::nowrap, hoisted out of the loops by the
     // callers): the same bits, no test
-    template <bool NOWRAP = false>
+    // COUNT = false: the caller sets count itself (a walk that knows how
+    // many of its candidates are not the boid itself)
+    template <bool NOWRAP = false, bool COUNT = true>
     __device__ __forceinline__ void add(const Rep& R, float sx, float sy, float4 o) {
         using M = F<STRICT>;
         const float dx = NOWRAP ? __fsub_rn(sx, o.x) : toroidal_distance(sx, o.x, R.w);
         const float dy = NOWRAP ? __fsub_rn(sy, o.y) : toroidal_distance(sy, o.y, R.h);
-        add_d(dx, dy, o);
+        add_d<COUNT>(dx, dy, o);
     }
+    template <bool COUNT = true>
     __device__ __forceinline__ void add_d(float dx, float dy, float4 o) {
         using M = F<STRICT>;
-        count += 1;
+        if (COUNT) count += 1;
         if (STRICT) {
             float sq = M::add(M::mul(dx, dx), M::mul(dy, dy));
             float q = M::add(M::mul(sq, sq), 1.0f);

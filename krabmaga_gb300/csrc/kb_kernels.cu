@@ -144,20 +144,26 @@ __device__ __forceinline__ void columns_flat3(const ForceArgs& a, const Rep& R, 
     const uint32_t P1 = e[0] - s[0], P2 = P1 + (e[1] - s[1]), T = P2 + (e[2] - s[2]);
     acc.vec += T;
     const uint32_t d1 = s[1] - P1, d2 = s[2] - P2;  // position = f + d (mod 2^32)
+    if (R.nowrap && my_slot != 0xFFFFFFFFu) {
+        // every candidate but the boid's own slot counts: no count per candidate
+        const bool self_in = (my_slot - s[0] < e[0] - s[0]) || (my_slot - s[1] < e[1] - s[1]) ||
+                             (my_slot - s[2] < e[2] - s[2]);
+        acc.count = (int)(T - (self_in ? 1u : 0u));
+    }
     if (DENSE && R.nowrap && my_slot != 0xFFFFFFFFu) {
 #pragma unroll 1
         for (int k = 0; k < 3; ++k) {
             const uint32_t ek = e[k];
             for (uint32_t q = s[k]; q < ek; ++q) {
                 const float4 o = __ldg(a.st + q);
-                if (q != my_slot) acc.template add<true>(R, me.x, me.y, o);
+                if (q != my_slot) acc.template add<true, false>(R, me.x, me.y, o);
             }
         }
     } else if (R.nowrap && my_slot != 0xFFFFFFFFu) {
         for (uint32_t f = 0; f < T; ++f) {
             const uint32_t p = f < P1 ? s[0] + f : (f < P2 ? f + d1 : f + d2);
             const float4 o = __ldg(a.st + p);
-            if (p != my_slot) acc.template add<true>(R, me.x, me.y, o);
+            if (p != my_slot) acc.template add<true, false>(R, me.x, me.y, o);
         }
     } else if (R.nowrap) {
         for (uint32_t f = 0; f < T; ++f) {
