@@ -102,8 +102,8 @@ class GpuStrip:
 class ShardedFlock:
     """A Flockers simulation on a w x w torus (bags of side d) split over the
     ranks of `group` by column strips.  `make_local(w, d, capacity)` builds the
-    local field (GpuStrip on this rank's GPU by default); `device` is where the
-    exchange tensors live ("cpu" for gloo, "cuda" for NCCL)."""
+    local field (GpuStrip on GPU `gpu` by default); `device` is where the
+    exchange tensors live ("cpu" for gloo, "cuda" for NCCL: then GPU `gpu`)."""
 
     def __init__(self, w: float, d: float, params: FlockParams, ids: np.ndarray, xy: np.ndarray,
                  dxy: np.ndarray, group=None, make_local: Optional[Callable] = None,
@@ -114,7 +114,11 @@ class ShardedFlock:
         self.group = group
         self.rank = dist.get_rank(group)
         self.world = dist.get_world_size(group)
-        self.w, self.d, self.params, self.device = float(w), float(d), params, device
+        import torch
+
+        self.w, self.d, self.params = float(w), float(d), params
+        # the exchange buffers: host memory for gloo, this rank's GPU for NCCL
+        self.device = torch.device("cuda", gpu) if device == "cuda" else torch.device(device)
         self.max_x, self.dw, self.dh = geometry(w, d)
         self.dd = max(query_reach(params.neighbor_radius, d), 0)
         self.strips = strips(self.dw, self.world)
