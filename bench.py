@@ -64,9 +64,12 @@ def bag_count(side, d=D_C):
 
 
 def algorithmic_bytes(n, ncells):
-    """Algorithmic bytes of one step and of each of its kernels: every record,
-    key and bag offset touched once.  The step figure is n * 32 + ncells * 8
-    (state read and written per boid, one bag offset written and read)."""
+    """Algorithmic bytes of one step: the metric's unit figure, 32 B per boid
+    (its float4 state read, its next state written) and 8 B per bag (one bag
+    offset written and read).  The dominant kernel's roofline divides this
+    step figure by its own launch time (one launch processes one step's
+    boids and bags).  The per-kernel "impl_bytes" count what each kernel of
+    this implementation touches once (ids, keys, counts included)."""
     return {
         "step": n * 32 + ncells * 8,
         "force": n * 44 + ncells * 8,  # record in 20, record + key out 24; offsets in, counts out
@@ -548,15 +551,18 @@ def run_ours(args, wl):
     kernels = None
     if kernel_ms is not None and kernel_steps == K:
         fm, sm, rm = (v / K for v in kernel_ms)
-        kernels = {"k_flock_force": {"ms_mean": fm, "bytes": force_bytes,
-                                     "gbs": force_bytes / fm / 1e6}}
+        kernels = {"k_flock_force": {"ms_mean": fm, "impl_bytes": force_bytes,
+                                     "impl_gbs": force_bytes / fm / 1e6}}
         if sm < 1e-3:  # the offsets scan runs inside the rebin launch
             ob = scan_bytes + rebin_bytes
-            kernels["k_offsets_rebin"] = {"ms_mean": sm + rm, "bytes": ob, "gbs": ob / (sm + rm) / 1e6}
+            kernels["k_offsets_rebin"] = {"ms_mean": sm + rm, "impl_bytes": ob,
+                                          "impl_gbs": ob / (sm + rm) / 1e6}
         else:
-            kernels["k_scan"] = {"ms_mean": sm, "bytes": scan_bytes, "gbs": scan_bytes / sm / 1e6}
-            kernels["k_rebin"] = {"ms_mean": rm, "bytes": rebin_bytes, "gbs": rebin_bytes / rm / 1e6}
-        kname, kbytes, kms = "k_flock_force", force_bytes, fm
+            kernels["k_scan"] = {"ms_mean": sm, "impl_bytes": scan_bytes,
+                                 "impl_gbs": scan_bytes / sm / 1e6}
+            kernels["k_rebin"] = {"ms_mean": rm, "impl_bytes": rebin_bytes,
+                                  "impl_gbs": rebin_bytes / rm / 1e6}
+        kname, kbytes, kms = "k_flock_force", step_bytes, fm
     else:  # tiled modes: the whole step is the measured unit
         kname = {2: "k_tile_step + k_scan (two launches per step)",
                  1: "k_fused (whole step, one launch)", 0: "whole step"}[args.mode]
