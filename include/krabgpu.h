@@ -193,6 +193,31 @@ kb_status kb_flock_compute(kb_field* f, const kb_flock_params* p, uint64_t step)
  * step.  The next lazy_update takes the general rebuild. */
 kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_t step, size_t n,
                                   const uint32_t* ids, const float* states);
+/* Device-resident record exchange (no reference counterpart: the halo and
+ * migration messages of the MPI field, kdtree_mpi.rs:705-795, without a
+ * host round trip).  Every pointer below is device memory on the field's
+ * device; records are {x, y, last_d.x, last_d.y} as four floats.  The
+ * caller's writes to input buffers must be complete before the call (e.g.
+ * its stream synchronised); the calls return with their own device work
+ * finished, so outputs can be read on any stream.
+ *
+ * kb_field_copy_read_buffer: the read buffer (bags ascending, insertion
+ * order inside a bag) into states_dev[4*cap] / ids_dev[cap]; *n = its
+ * length.  KB_ERR_ARG (with *n set) when cap < *n. */
+kb_status kb_field_copy_read_buffer(kb_field* f, float* states_dev, uint32_t* ids_dev, size_t cap,
+                                    size_t* n);
+/* kb_field_set_locations for records in device memory: the n records are
+ * appended to the write buffer in this order (set_object_location per
+ * record, field_2d.rs:838-846).  KB_ERR_RANGE / KB_ERR_ARG as
+ * kb_field_set_locations, with the write buffer left as it was. */
+kb_status kb_field_set_states_device(kb_field* f, size_t n, const uint32_t* ids_dev,
+                                     const float* states_dev);
+/* Bird::step (bird.rs:39-154) of n agents held in device memory against the
+ * read buffer, as kb_flock_compute_agents, but the next states go to
+ * out_dev[4*n] (agent order) and nothing is added to the write buffer. */
+kb_status kb_flock_next_states_device(kb_field* f, const kb_flock_params* p, uint64_t step,
+                                      size_t n, const uint32_t* ids_dev, const float* states_dev,
+                                      float* out_dev);
 /* nsteps full steps: compute + lazy_update each (schedule.rs:395-412), with
  * step numbers first_step ... first_step+nsteps-1.  The read buffer must
  * hold the flock and the write buffer must be empty (call lazy_update after

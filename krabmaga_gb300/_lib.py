@@ -180,6 +180,11 @@ _SIGS = {
     "kb_flock_compute": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64]),
     "kb_flock_compute_agents": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64, C.c_size_t,
                                             _U32, _F]),
+    # device-resident record exchange: device pointers as void*
+    "kb_field_copy_read_buffer": (C.c_int32, [_P, _P, _P, C.c_size_t, _SZ]),
+    "kb_field_set_states_device": (C.c_int32, [_P, C.c_size_t, _P, _P]),
+    "kb_flock_next_states_device": (C.c_int32, [_P, C.POINTER(FlockParamsC), C.c_uint64,
+                                                C.c_size_t, _P, _P, _P]),
     "kb_field_set_step_options": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "kb_field_set_dense_mode": (C.c_int32, [_P, C.c_int32]),
     "kb_field_dense_active": (C.c_int32, [_P, C.POINTER(C.c_int32)]),

@@ -1875,6 +1875,103 @@ kb_status kb_flock_compute_agents(kb_field* f, const kb_flock_params* p, uint64_
     return kb::exception_status();
 }
 
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+kb_status kb_field_copy_read_buffer(kb_field* f, float* states_dev, uint32_t* ids_dev, size_t cap,
+                                    size_t* n) try {
+    if (!f || !n) return fail(KB_ERR_ARG, "null argument");
+    DeviceGuard g(f->device);
+    kb_status st = materialize(f);
+    if (st) return st;
+    *n = f->rn;
+    if (cap < f->rn) return fail(KB_ERR_ARG, "output capacity below the read buffer's length");
+    if (f->rn == 0) return KB_OK;
+    if (!states_dev || !ids_dev) return fail(KB_ERR_ARG, "null argument");
+    KB_CUDA(cudaMemcpyAsync(states_dev, f->rst.p, sizeof(float4) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
+    KB_CUDA(cudaMemcpyAsync(ids_dev, f->rid.p, sizeof(uint32_t) * f->rn, cudaMemcpyDeviceToDevice, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return KB_OK;
+} catch (...) {
+    return kb::exception_status();
+}
+
+kb_status kb_field_set_states_device(kb_field* f, size_t n, const uint32_t* ids_dev,
+                                     const float* states_dev) try {
+    if (!f || (n && (!ids_dev || !states_dev))) return fail(KB_ERR_ARG, "null argument");
+    if (n == 0) return KB_OK;
+    if (!aligned16(states_dev)) return fail(KB_ERR_ARG, "states_dev is not 16-byte aligned");
+    if ((uint64_t)f->wn + f->p_id.size() + n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "too many objects");
+    DeviceGuard g(f->device);
+    kb_status st = flush_pending(f);  // earlier single writes first (insertion order)
+    if (st) return st;
+    if (f->virt && (st = materialize(f))) return st;
+    if ((st = grow(f, f->wn + (uint32_t)n))) return st;
+    const uint32_t m = (uint32_t)n;
+    KB_CUDA(cudaMemcpyAsync(f->wid.p + f->wn, ids_dev, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, f->stream));
+    KB_CUDA(cudaMemsetAsync(f->small.p, 0xFF, sizeof(uint32_t), f->stream));
+    KB_CUDA(launch_pack_states(f->rep, reinterpret_cast<const float4*>(states_dev), m, f->wst.p + f->wn,
+                               f->wkey.p + f->wn, f->wdead.p + f->wn, f->small.p, f->stream));
+    uint32_t bad = 0;
+    if ((st = read_u32(f, f->small.p, &bad))) return st;
+    if (bad != 0xFFFFFFFFu) {  // the write list is left as it was
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "object %u: non-finite record or location outside the bag matrix", bad);
+        return fail(KB_ERR_RANGE, buf);
+    }
+    f->wn += m;
+    if (!f->density_check) f->nagents += n;
+    f->w_from_compute = false;
+    return KB_OK;
+} catch (...) {
+    return kb::exception_status();
+}
+
+kb_status kb_flock_next_states_device(kb_field* f, const kb_flock_params* p, uint64_t step,
+                                      size_t n, const uint32_t* ids_dev, const float* states_dev,
+                                      float* out_dev) try {
+    if (!f || !p || (n && (!ids_dev || !states_dev || !out_dev))) return fail(KB_ERR_ARG, "null argument");
+    if (f->is_batch) return fail(KB_ERR_ARG, "a batch field: agents join a batch with kb_batch_add_replica");
+    std::string why;
+    if (!params_ok(p, &why)) return fail(KB_ERR_ARG, why);
+    if (n == 0) return KB_OK;
+    if (!aligned16(states_dev) || !aligned16(out_dev)) return fail(KB_ERR_ARG, "state buffers are not 16-byte aligned");
+    if (n > 0xFFFFFFF0ull) return fail(KB_ERR_ARG, "object count exceeds 2^32-16");
+    DeviceGuard g(f->device);
+    kb_status st = flush_pending(f);
+    if (st) return st;
+    if ((st = materialize(f))) return st;
+    const uint32_t m = (uint32_t)n;
+    if ((st = grow(f, std::max(f->rn, m)))) return st;
+    if (f->spare_hist.n < f->cells_cap) {
+        cudaError_t e = f->spare_hist.alloc(f->cells_cap);
+        if (e) return cuda_fail(e, "arrival counts");
+    }
+    set_rep_params(&f->rep, p);
+    if ((st = upload_rep(f))) return st;
+    KB_CUDA(launch_set_u64(f->dstep.p, step, f->stream));
+    f->dstep_host = step;
+    ForceArgs a{};
+    a.reps = f->d_rep.p;
+    a.nrep = 1;
+    a.rep0 = f->reps[0];
+    a.st = f->rst.p;
+    a.ids = f->rid.p;
+    a.start = f->start[f->cur].p;
+    a.n = f->rn;
+    a.step = f->dstep.p;
+    a.out_st = reinterpret_cast<float4*>(out_dev);
+    a.out_ids = f->tid.p;
+    a.out_key = f->tkey.p;
+    a.hist = f->spare_hist.p;
+    a.err = f->err.p;
+    KB_CUDA(launch_flock_agents(a, reinterpret_cast<const float4*>(states_dev), ids_dev, m,
+                                p->arith == KB_ARITH_STRICT, p->query_mode, f->stream));
+    KB_CUDA(cudaStreamSynchronize(f->stream));
+    return KB_OK;
+} catch (...) {
+    return kb::exception_status();
+}
+
 kb_status kb_field_get_locations(kb_field* f, int32_t buffered, size_t n, const uint32_t* ids,
                                  float* states, int32_t* found) try {
     if (!f || (n && (!ids || !states || !found))) return fail(KB_ERR_ARG, "null argument");

@@ -64,6 +64,8 @@ struct kb_field {
     uint32_t nblk_force = 0, nblk_seg = 0;
     uint32_t force_block = FORCE_THREADS;  // threads per force block over packed replicas
     DevBuf<float4> tst;
+    // arrival counts of kb_flock_next_states_device's agents (written, never read)
+    DevBuf<uint32_t> spare_hist;
     DevBuf<ScanCtl> scan_ctl, aux_ctl;
     DevBuf<unsigned long long> tstate, aux_tstate;
     uint32_t aux_tiles = 0;

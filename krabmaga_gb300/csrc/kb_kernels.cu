@@ -1317,6 +1317,23 @@ __global__ void k_pack_locations(Rep R, const float2* __restrict__ xy, const flo
     out_dead[i] = 0;
 }
 
+// The same for records already packed as {x, y, last_d} (device-resident input).
+__global__ void k_pack_states(Rep R, const float4* __restrict__ st, uint32_t n,
+                              float4* __restrict__ out_st, uint32_t* __restrict__ out_key,
+                              uint8_t* __restrict__ out_dead, uint32_t* bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = st[i];
+    const int64_t idx = bag_index(R, disc(v.x, R), disc(v.y, R));
+    if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w)) || idx < 0) {
+        atomicMin(bad, i);
+        return;
+    }
+    out_st[i] = v;
+    out_key[i] = R.cell_off + (uint32_t)idx;
+    out_dead[i] = 0;
+}
+
 __global__ void k_set_rep(Rep* dst, Rep v) { *dst = v; }
 __global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
 __global__ void k_add_u64(unsigned long long* dst, unsigned long long v) { *dst += v; }
@@ -1356,6 +1373,13 @@ cudaError_t launch_pack_locations(const Rep& rep, const float2* xy, const float2
                                   uint32_t* bad, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_pack_locations<<<grid_for(n, 256), 256, 0, s>>>(rep, xy, dxy, n, out_st, out_key, out_dead, bad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_states(const Rep& rep, const float4* st, uint32_t n, float4* out_st,
+                               uint32_t* out_key, uint8_t* out_dead, uint32_t* bad, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_pack_states<<<grid_for(n, 256), 256, 0, s>>>(rep, st, n, out_st, out_key, out_dead, bad);
     return cudaGetLastError();
 }
 

@@ -177,6 +177,9 @@ cudaError_t launch_moments(const Rep* reps, uint32_t nrep, const uint32_t* start
 cudaError_t launch_pack_locations(const Rep& rep, const float2* xy, const float2* dxy, uint32_t n,
                                   float4* out_st, uint32_t* out_key, uint8_t* out_dead,
                                   uint32_t* bad, cudaStream_t s);
+// The same for records already packed as float4 {x, y, last_d} on the device.
+cudaError_t launch_pack_states(const Rep& rep, const float4* st, uint32_t n, float4* out_st,
+                               uint32_t* out_key, uint8_t* out_dead, uint32_t* bad, cudaStream_t s);
 
 // General stable counting sort of the write list by key (insertion order
 // kept inside each bag): histogram, scatter, per-bag canonicalisation.

@@ -63,6 +63,7 @@ class Field2D:
         h_ = C.c_void_p()
         L.call("kb_field_create", C.byref(desc), C.byref(h_))
         self._h = h_
+        self.device = int(device)
         self.width = float(np.float32(w))
         self.height = float(np.float32(h))
         self.discretization = float(np.float32(d))
@@ -182,6 +183,52 @@ class Field2D:
         assert len(ids) == len(st)
         L.call("kb_flock_compute_agents", self._h, C.byref(params.to_c()), C.c_uint64(step),
                C.c_size_t(len(ids)), L.uptr(ids), L.fptr(st))
+
+    # ---- device-resident records: torch CUDA tensors on the field's GPU,
+    # ids as int32 holding the u32 bits, records float32 [n, 4] {x, y, dx, dy}
+    @staticmethod
+    def _dev_arg(t, dtype, what: str):
+        import torch
+
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+            raise TypeError(f"{what}: a contiguous CUDA tensor of {dtype} is expected")
+        # the library reads the tensor on its own stream: finish torch's work first
+        torch.cuda.current_stream(t.device).synchronize()
+        return C.c_void_p(t.data_ptr())
+
+    def read_buffer_device(self):
+        """(ids int32 [n], states float32 [n, 4]): a device copy of the read
+        buffer in its order (bags ascending, insertion order in a bag)."""
+        import torch
+
+        n = self.num_objects()
+        dev = torch.device("cuda", self.device)
+        ids = torch.empty(n, dtype=torch.int32, device=dev)
+        st = torch.empty((n, 4), dtype=torch.float32, device=dev)
+        got = C.c_size_t()
+        L.call("kb_field_copy_read_buffer", self._h, self._dev_arg(st, torch.float32, "states"),
+               self._dev_arg(ids, torch.int32, "ids"), C.c_size_t(n), C.byref(got))
+        return ids, st
+
+    def set_states_device(self, ids, states) -> None:
+        """set_locations for records held on the device (appended in order)."""
+        import torch
+
+        assert ids.shape[0] == states.shape[0] and states.shape[1:] == (4,)
+        L.call("kb_field_set_states_device", self._h, C.c_size_t(ids.shape[0]),
+               self._dev_arg(ids, torch.int32, "ids"), self._dev_arg(states, torch.float32, "states"))
+
+    def next_states_device(self, params, step: int, ids, states):
+        """Bird::step of device-held agents against the read buffer; returns
+        their next states (float32 [n, 4]); the write buffer is untouched."""
+        import torch
+
+        assert ids.shape[0] == states.shape[0] and states.shape[1:] == (4,)
+        out = torch.empty_like(states)
+        L.call("kb_flock_next_states_device", self._h, C.byref(params.to_c()), C.c_uint64(step),
+               C.c_size_t(ids.shape[0]), self._dev_arg(ids, torch.int32, "ids"),
+               self._dev_arg(states, torch.float32, "states"), self._dev_arg(out, torch.float32, "out"))
+        return out
 
     def lazy_update(self) -> None:
         """Field::lazy_update -- field_2d.rs:905-921"""

@@ -200,6 +200,15 @@ extern "C" {
     pub fn kb_flock_compute(f: *mut kb_field, p: *const kb_flock_params, step: u64) -> kb_status;
     pub fn kb_flock_compute_agents(f: *mut kb_field, p: *const kb_flock_params, step: u64,
                                    n: usize, ids: *const u32, states: *const f32) -> kb_status;
+
+    // ---- device-resident record exchange (device pointers; no reference counterpart)
+    pub fn kb_field_copy_read_buffer(f: *mut kb_field, states_dev: *mut f32, ids_dev: *mut u32,
+                                     cap: usize, n: *mut usize) -> kb_status;
+    pub fn kb_field_set_states_device(f: *mut kb_field, n: usize, ids_dev: *const u32,
+                                      states_dev: *const f32) -> kb_status;
+    pub fn kb_flock_next_states_device(f: *mut kb_field, p: *const kb_flock_params, step: u64,
+                                       n: usize, ids_dev: *const u32, states_dev: *const f32,
+                                       out_dev: *mut f32) -> kb_status;
     pub fn kb_flock_step(f: *mut kb_field, p: *const kb_flock_params, first_step: u64,
                          nsteps: u32) -> kb_status;
 

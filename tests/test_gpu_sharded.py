@@ -96,3 +96,89 @@ def test_two_gpu_strips_equal_the_oracle_strict(gpu):
     o.flock_run(oracle.params_from(kg.FlockParams(seed=seed, jump=jump)), 0, steps)
     oids, ost, _ = o.iter(1)
     assert np.array_equal(gids, oids) and _same(gst, ost)
+
+
+def _device_ranks(world, arith, case=CASE):
+    """Every rank's strip on this GPU with its records kept on the device
+    (GpuStripDevice), the ranks driven in this process: prepare on each,
+    then finish with the device tensors each rank was sent."""
+    from krabmaga_gb300.sharded import ShardedFlock
+
+    n, side, seed, steps, jump = case
+    ids, xy, dxy = kg.gen_uniform(n, side, side, seed, 1.0)
+    p = kg.FlockParams(seed=seed, jump=jump, arith=arith)
+    ranks = [ShardedFlock(side, D, p, ids, xy, dxy, device="cuda", gpu=0, rank=r, world=world)
+             for r in range(world)]
+    sent = 0
+    for k in range(steps):
+        parts = [sf.prepare(k) for sf in ranks]
+        assert all(t.is_cuda for pr in parts for t in pr)
+        sent += sum(int(parts[s][r].shape[0]) for s in range(world) for r in range(world) if r != s)
+        for r, sf in enumerate(ranks):
+            sf.finish([parts[s][r] for s in range(world)])
+    own = [sf.owned_state() for sf in ranks]
+    for sf in ranks:
+        sf.close()
+    return np.concatenate([o[0] for o in own]), np.concatenate([o[1] for o in own]), sent
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_device_resident_strips_equal_the_single_gpu_field(gpu, world):
+    n, side, seed, steps, jump = CASE
+    for arith in (kg.KB_ARITH_FAST, kg.KB_ARITH_STRICT):
+        gids, gst, sent = _device_ranks(world, arith)
+        assert sent > 0  # halo and migration records crossed ranks
+        ids, xy, dxy = kg.gen_uniform(n, side, side, seed, 1.0)
+        f = kg.Field2D(side, side, D, True, capacity_hint=n)
+        f.set_locations(ids, xy, dxy)
+        f.lazy_update()
+        p = kg.FlockParams(seed=seed, jump=jump, arith=arith)
+        L.call("kb_flock_step", f.handle, C.byref(p.to_c()), C.c_uint64(0), C.c_uint32(steps))
+        sids, sst = f.get_state()
+        f.close()
+        assert np.array_equal(gids, sids) and _same(gst, sst)
+
+
+def test_device_record_entry_points_match_the_host_ones(gpu):
+    """kb_field_copy_read_buffer / kb_flock_next_states_device /
+    kb_field_set_states_device against get_state / compute_agents /
+    set_locations on the same flock."""
+    import torch
+
+    n, side, seed = 3000, 346.41, 5
+    ids, xy, dxy = kg.gen_uniform(n, side, side, seed, 1.0)
+    p = kg.FlockParams(seed=seed, jump=2.0)
+    f = kg.Field2D(side, side, D, True, capacity_hint=n)
+    f.set_locations(ids, xy, dxy)
+    f.lazy_update()
+    hid, hst = f.get_state()
+    did, dst = f.read_buffer_device()
+    assert np.array_equal(did.cpu().numpy().view(np.uint32), hid)
+    assert _same(dst.cpu().numpy(), hst)
+    # next states of every other boid, on the device and through the write buffer
+    sel = np.arange(0, n, 2)
+    out = f.next_states_device(p, 3, did[sel].contiguous(), dst[sel].contiguous()).cpu().numpy()
+    g = kg.Field2D(side, side, D, True, capacity_hint=n)
+    g.set_locations(ids, xy, dxy)
+    g.lazy_update()
+    g.flock_compute_agents(p, 3, hid[sel], hst[sel])
+    found, want = g.get_locations(hid[sel], buffered=False)
+    assert found.all() and _same(out, want)
+    # records set from the device make the same read buffer as from the host
+    h = kg.Field2D(side, side, D, True, capacity_hint=n)
+    h.set_states_device(did.flip(0).contiguous(), dst.flip(0).contiguous())
+    h.lazy_update()
+    k = kg.Field2D(side, side, D, True, capacity_hint=n)
+    k.set_locations(hid[::-1], hst[::-1, :2], hst[::-1, 2:])
+    k.lazy_update()
+    a, b = h.get_state(), k.get_state()
+    assert np.array_equal(a[0], b[0]) and _same(a[1], b[1])
+    # a record outside the bag matrix is refused and the write buffer is left as it was
+    bad = dst[:4].clone()
+    bad[2, 0] = -5.0
+    with pytest.raises(L.KbError):
+        h.set_states_device(did[:4].contiguous(), bad)
+    h.lazy_update()
+    assert h.num_objects() == 0
+    for fld in (f, g, h, k):
+        fld.close()

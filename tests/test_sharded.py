@@ -147,3 +147,28 @@ def test_strip_geometry():
     s = strips(dw, 3)
     assert s[0][0] == 0 and s[-1][1] == dw and all(a[1] == b[0] for a, b in zip(s, s[1:]))
     assert query_reach(10.0, D) == 1 and query_reach(0.0, D) == -1
+
+
+def test_ranks_driven_in_one_process_equal_the_single_field():
+    """The two phases of a step (prepare on every rank, then finish with
+    what each rank was sent) driven in one process, no process group: the
+    same bits as the single field, over 2 and 3 strips."""
+    from krabmaga_gb300.model import FlockParams
+    from krabmaga_gb300.sharded import ShardedFlock
+
+    for world, case in ((2, (3000, 346.41, 7, 6, 3.0)), (3, (2500, 316.23, 11, 5, 2.0))):
+        n, side, seed, steps, jump = case
+        ids, xy, dxy = flock(n, side, seed)
+        p = FlockParams(seed=seed, jump=jump)
+        ranks = [ShardedFlock(side, D, p, ids, xy, dxy, make_local=OracleStrip, rank=r, world=world)
+                 for r in range(world)]
+        for k in range(steps):
+            parts = [sf.prepare(k) for sf in ranks]
+            for r, sf in enumerate(ranks):
+                sf.finish([parts[src][r] for src in range(world)])
+        own = [sf.owned_state() for sf in ranks]
+        gids = np.concatenate([o[0] for o in own])
+        gst = np.concatenate([o[1] for o in own])
+        oids, ost = _single(case)
+        assert np.array_equal(gids, oids)
+        assert np.array_equal(gst.view(np.uint32), ost.view(np.uint32))
