@@ -187,18 +187,21 @@ def allmax(ws, v):
     return float(t.item())
 
 
-def cpu_reference(wl, steps):
-    """The oracle's reference-equivalent run: returns (boid-updates/s, sample text)."""
+def cpu_reference(wl, steps, warmup=0):
+    """The oracle's reference-equivalent run, `steps` timed steps after
+    `warmup` untimed ones: returns (boid-updates/s, sample text)."""
     import oracle
 
     ids, xy, dxy = gen(wl, oracle)
     p = oracle.params(seed=wl["seed"], query_mode=0)
-    secs, _ = oracle.simulate_timed(wl["side"], wl["side"], D_C, p, ids, xy, dxy, steps)
-    return wl["n"] * steps / secs, (f"{wl['desc']}, {steps} steps through the priority-queue "
-                                    f"schedule (oracle restatement of the reference, 1 core)")
+    secs, _ = oracle.simulate_timed(wl["side"], wl["side"], D_C, p, ids, xy, dxy, steps,
+                                    warmup=warmup)
+    return wl["n"] * steps / secs, (f"{wl['desc']}, {steps} steps after {warmup} warm-up steps "
+                                    f"through the priority-queue schedule (oracle restatement "
+                                    f"of the reference, 1 core)")
 
 
-def cpu_reference_threads(wl, steps):
+def cpu_reference_threads(wl, steps, warmup=0):
     """The oracle's run with the agent pass on every host core (not what the
     reference can do: its schedule runs agents one at a time): returns
     (boid-updates/s, threads, sample text)."""
@@ -208,10 +211,11 @@ def cpu_reference_threads(wl, steps):
     ids, xy, dxy = gen(wl, oracle)
     p = oracle.params(seed=wl["seed"], query_mode=0)
     secs, _ = oracle.simulate_timed_threads(wl["side"], wl["side"], D_C, p, ids, xy, dxy, steps,
-                                            threads)
-    return wl["n"] * steps / secs, threads, (f"{wl['desc']}, {steps} steps, agent pass on "
-                                             f"{threads} host threads (oracle, not the reference's "
-                                             f"sequential schedule)")
+                                            threads, warmup=warmup)
+    return wl["n"] * steps / secs, threads, (f"{wl['desc']}, {steps} steps after {warmup} "
+                                             f"warm-up steps, agent pass on {threads} host "
+                                             f"threads (oracle, not the reference's sequential "
+                                             f"schedule)")
 
 
 def run_sweep(args, dev):
@@ -385,14 +389,17 @@ def run_reference(args, wl):
     ws, rank, _ = dist_setup()
     if rank != 0:
         return
+    # a bounded sample of the workload: at most ref_steps timed steps after
+    # at most ref_warmup warm-up steps, so that the run stays within minutes
     steps = max(1, min(args.steps, args.ref_steps))
-    value, sample = cpu_reference(wl, steps)
-    pv, threads, psample = cpu_reference_threads(wl, steps)
+    warm = max(0, min(args.warmup, args.ref_warmup))
+    value, sample = cpu_reference(wl, steps, warm)
+    pv, threads, psample = cpu_reference_threads(wl, steps, warm)
     # rank 0 alone runs the CPU arm (one core), whatever the number of ranks
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
         "ranks": ws,
-        "steps": steps, "warmup": 0, "ms_per_step": 1e3 * wl["n"] / value,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * wl["n"] / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox uniform flock)",
         "config": {"workload": wl["desc"], "global_batch": wl["n"], "parallelism": "cpu",
@@ -577,8 +584,9 @@ def run_ours(args, wl):
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
-        cval, sample = cpu_reference(wl, args.cpu_steps)
-        pv, threads, psample = cpu_reference_threads(wl, args.cpu_steps)
+        cwarm = max(0, min(args.warmup, args.ref_warmup))
+        cval, sample = cpu_reference(wl, args.cpu_steps, cwarm)
+        pv, threads, psample = cpu_reference_threads(wl, args.cpu_steps, cwarm)
         cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
                "all_cores": {"value": pv, "cores": threads, "sample": psample}}
 
@@ -631,6 +639,7 @@ def main():
     ap.add_argument("--arith", default="fast", choices=["fast", "strict"])
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--ref-steps", type=int, default=20)
+    ap.add_argument("--ref-warmup", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--e2e-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")

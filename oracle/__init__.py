@@ -67,6 +67,13 @@ _SIGS = {
                                          C.c_size_t]),
     "orc_simulate_timed": (C.c_double, [C.c_float, C.c_float, C.c_float, C.POINTER(Params),
                                         C.c_size_t, _U32, _F, _F, C.c_uint32, C.POINTER(_P)]),
+    "orc_simulate_timed_warm": (C.c_double, [C.c_float, C.c_float, C.c_float, C.POINTER(Params),
+                                             C.c_size_t, _U32, _F, _F, C.c_uint32, C.c_uint32,
+                                             C.POINTER(_P)]),
+    "orc_simulate_timed_threads_warm": (C.c_double, [C.c_float, C.c_float, C.c_float,
+                                                     C.POINTER(Params), C.c_size_t, _U32, _F, _F,
+                                                     C.c_uint32, C.c_uint32, C.c_uint32,
+                                                     C.POINTER(_P)]),
     "orc_gen_uniform": (C.c_int, [C.c_size_t, C.c_float, C.c_float, C.c_uint64, C.c_float, _U32,
                                   _F, _F]),
     "orc_gen_clustered": (C.c_int, [C.c_size_t, C.c_float, C.c_float, C.c_uint32, C.c_float,
@@ -248,15 +255,18 @@ class OracleField:
         return ids[:n], out[:n]
 
 
-def simulate_timed_threads(w, h, d, p: Params, ids, xy, dxy, nsteps, threads, keep_field=False):
+def simulate_timed_threads(w, h, d, p: Params, ids, xy, dxy, nsteps, threads, keep_field=False,
+                           warmup=0):
     """The same run with the agent pass on `threads` host threads (results
-    equal to the sequential run); returns (seconds, OracleField or None)."""
+    equal to the sequential run); returns (seconds, OracleField or None).
+    warmup: untimed steps before the nsteps timed ones."""
     ids = np.ascontiguousarray(ids, np.uint32)
     xy = np.ascontiguousarray(xy, np.float32)
     dxy = np.ascontiguousarray(dxy, np.float32)
     out = C.c_void_p()
-    secs = lib.orc_simulate_timed_threads(w, h, d, C.byref(p), len(ids), _u(ids), _f(xy), _f(dxy),
-                                          nsteps, threads, C.byref(out) if keep_field else None)
+    secs = lib.orc_simulate_timed_threads_warm(w, h, d, C.byref(p), len(ids), _u(ids), _f(xy),
+                                               _f(dxy), warmup, nsteps, threads,
+                                               C.byref(out) if keep_field else None)
     f = None
     if keep_field:
         f = OracleField.__new__(OracleField)
@@ -267,15 +277,16 @@ def simulate_timed_threads(w, h, d, p: Params, ids, xy, dxy, nsteps, threads, ke
     return secs, f
 
 
-def simulate_timed(w, h, d, p: Params, ids, xy, dxy, nsteps, keep_field=False):
+def simulate_timed(w, h, d, p: Params, ids, xy, dxy, nsteps, keep_field=False, warmup=0):
     """Reference-equivalent timed run (priority-queue schedule); returns
-    (seconds in the step loop, OracleField or None)."""
+    (seconds in the step loop, OracleField or None).  warmup: untimed steps
+    (0 .. warmup-1) before the nsteps timed ones."""
     ids = np.ascontiguousarray(ids, np.uint32)
     xy = np.ascontiguousarray(xy, np.float32)
     dxy = np.ascontiguousarray(dxy, np.float32)
     out = C.c_void_p()
-    secs = lib.orc_simulate_timed(w, h, d, C.byref(p), len(ids), _u(ids), _f(xy), _f(dxy),
-                                  nsteps, C.byref(out) if keep_field else None)
+    secs = lib.orc_simulate_timed_warm(w, h, d, C.byref(p), len(ids), _u(ids), _f(xy), _f(dxy),
+                                       warmup, nsteps, C.byref(out) if keep_field else None)
     f = None
     if keep_field:
         f = OracleField.__new__(OracleField)

@@ -732,9 +732,25 @@ size_t orc_flock_step_fp64(void* fp, const orc_params* pp, uint64_t step, uint32
 // Schedule::steps through a binary-heap schedule.  Returns the seconds spent
 // in the step loop (init excluded, lib.rs:1515-1526); the final read buffer
 // is left in *out_field if non-NULL (caller frees).
+double orc_simulate_timed_warm(float w, float h, float d, const orc_params* pp, size_t n,
+                               const uint32_t* ids, const float* xy, const float* dxy,
+                               uint32_t nwarm, uint32_t nsteps, void** out_field);
+double orc_simulate_timed_threads_warm(float w, float h, float d, const orc_params* pp, size_t n,
+                                       const uint32_t* ids, const float* xy, const float* dxy,
+                                       uint32_t nwarm, uint32_t nsteps, uint32_t threads,
+                                       void** out_field);
+
 double orc_simulate_timed(float w, float h, float d, const orc_params* pp, size_t n,
                           const uint32_t* ids, const float* xy, const float* dxy,
                           uint32_t nsteps, void** out_field) {
+    return orc_simulate_timed_warm(w, h, d, pp, n, ids, xy, dxy, 0, nsteps, out_field);
+}
+
+// The same after nwarm untimed steps (steps 0 .. nwarm-1): the seconds of
+// steps nwarm .. nwarm+nsteps-1 alone.
+double orc_simulate_timed_warm(float w, float h, float d, const orc_params* pp, size_t n,
+                               const uint32_t* ids, const float* xy, const float* dxy,
+                               uint32_t nwarm, uint32_t nsteps, void** out_field) {
     FlockParams p = to_params(pp);
     Field2D* f = new Field2D(w, h, d, true);
     typedef std::priority_queue<Event, std::vector<Event>, EventLess> PQ;
@@ -748,7 +764,8 @@ double orc_simulate_timed(float w, float h, float d, const orc_params* pp, size_
     auto t0 = std::chrono::steady_clock::now();
     std::vector<Event> cevents;
     std::vector<Bird> vec;
-    for (uint32_t s = 0; s < nsteps; ++s) {
+    for (uint32_t s = 0; s < nwarm + nsteps; ++s) {
+        if (s == nwarm) t0 = std::chrono::steady_clock::now();
         if (s == 0) f->lazy_update();  // schedule.rs:349-351
         if (pq.empty()) break;
         float now = pq.top().time;
@@ -782,6 +799,13 @@ double orc_simulate_timed(float w, float h, float d, const orc_params* pp, size_
 double orc_simulate_timed_threads(float w, float h, float d, const orc_params* pp, size_t n,
                                   const uint32_t* ids, const float* xy, const float* dxy,
                                   uint32_t nsteps, uint32_t threads, void** out_field) {
+    return orc_simulate_timed_threads_warm(w, h, d, pp, n, ids, xy, dxy, 0, nsteps, threads, out_field);
+}
+
+double orc_simulate_timed_threads_warm(float w, float h, float d, const orc_params* pp, size_t n,
+                                       const uint32_t* ids, const float* xy, const float* dxy,
+                                       uint32_t nwarm, uint32_t nsteps, uint32_t threads,
+                                       void** out_field) {
     FlockParams p = to_params(pp);
     Field2D* f = new Field2D(w, h, d, true);
     for (size_t i = 0; i < n; ++i) {
@@ -792,7 +816,8 @@ double orc_simulate_timed_threads(float w, float h, float d, const orc_params* p
     auto t0 = std::chrono::steady_clock::now();
     f->lazy_update();
     std::vector<Bird> agents, next;
-    for (uint32_t s = 0; s < nsteps; ++s) {
+    for (uint32_t s = 0; s < nwarm + nsteps; ++s) {
+        if (nwarm && s == nwarm) t0 = std::chrono::steady_clock::now();
         read_order(*f, agents);
         next.resize(agents.size());
         const size_t m = agents.size();

@@ -146,3 +146,18 @@ def test_threaded_timing_run_equals_the_sequential_steps():
     a_ids, a_st, _ = f.iter(1)
     b_ids, b_st, _ = o.iter(1)
     assert np.array_equal(a_ids, b_ids) and np.array_equal(a_st.view(np.uint32), b_st.view(np.uint32))
+
+
+def test_warm_up_steps_are_steps_of_the_same_run():
+    # the timed runs' warm-up steps are the run's first steps (untimed): a
+    # 2 + 4 step run ends where a 6-step run does, in both timing runs
+    ids, xy, dxy = _random_flock(1500, 260.0, seed=9)
+    p = oracle.params(seed=3, query_mode=0)
+    _, a = oracle.simulate_timed(260.0, 260.0, FLOCK_D, p, ids, xy, dxy, 4, keep_field=True,
+                                 warmup=2)
+    _, b = oracle.simulate_timed(260.0, 260.0, FLOCK_D, p, ids, xy, dxy, 6, keep_field=True)
+    _, c = oracle.simulate_timed_threads(260.0, 260.0, FLOCK_D, p, ids, xy, dxy, 4, 3,
+                                         keep_field=True, warmup=2)
+    sa, sb, sc = a.iter(1), b.iter(1), c.iter(1)
+    for s in (sa, sc):
+        assert np.array_equal(s[0], sb[0]) and np.array_equal(s[1].view(np.uint32), sb[1].view(np.uint32))
