@@ -158,6 +158,8 @@ def test_warm_up_steps_are_steps_of_the_same_run():
     _, b = oracle.simulate_timed(260.0, 260.0, FLOCK_D, p, ids, xy, dxy, 6, keep_field=True)
     _, c = oracle.simulate_timed_threads(260.0, 260.0, FLOCK_D, p, ids, xy, dxy, 4, 3,
                                          keep_field=True, warmup=2)
-    sa, sb, sc = a.iter(1), b.iter(1), c.iter(1)
-    for s in (sa, sc):
-        assert np.array_equal(s[0], sb[0]) and np.array_equal(s[1].view(np.uint32), sb[1].view(np.uint32))
+    _, e = oracle.simulate_timed_threads(260.0, 260.0, FLOCK_D, p, ids, xy, dxy, 6, 3,
+                                         keep_field=True)
+    for x, y in ((a, b), (c, e)):
+        sx, sy = x.iter(1), y.iter(1)
+        assert np.array_equal(sx[0], sy[0]) and np.array_equal(sx[1].view(np.uint32), sy[1].view(np.uint32))
