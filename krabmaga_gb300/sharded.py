@@ -170,6 +170,9 @@ class ShardedFlock:
         self.on_device = device == "cuda"
         # the exchange buffers: host memory for gloo, this rank's GPU for NCCL
         self.device = torch.device("cuda", gpu) if self.on_device else torch.device(device)
+        if self.on_device and self.dist is not None:
+            # NCCL's object collectives (gather_state) use the current device
+            torch.cuda.set_device(self.device)
         self.max_x, self.dw, self.dh = geometry(w, d)
         self.dd = max(query_reach(params.neighbor_radius, d), 0)
         self.strips = strips(self.dw, self.world)
