@@ -180,5 +180,18 @@ def test_device_record_entry_points_match_the_host_ones(gpu):
         h.set_states_device(did[:4].contiguous(), bad)
     h.lazy_update()
     assert h.num_objects() == 0
+    # an output shorter than the read buffer is refused with the length reported
+    n_out = C.c_size_t()
+    small_st = torch.empty((10, 4), dtype=torch.float32, device=dst.device)
+    small_id = torch.empty(10, dtype=torch.int32, device=dst.device)
+    with pytest.raises(L.KbError):
+        L.call("kb_field_copy_read_buffer", f.handle, C.c_void_p(small_st.data_ptr()),
+               C.c_void_p(small_id.data_ptr()), C.c_size_t(10), C.byref(n_out))
+    assert n_out.value == n
+    # empty calls are no-ops
+    L.call("kb_field_set_states_device", f.handle, C.c_size_t(0), None, None)
+    L.call("kb_flock_next_states_device", f.handle, C.byref(p.to_c()), C.c_uint64(0),
+           C.c_size_t(0), None, None, None)
+    assert f.num_objects() == n
     for fld in (f, g, h, k):
         fld.close()
