@@ -226,6 +226,8 @@ kb_status build_rep_blocks(kb_field* f) {
         const uint32_t ns = rep_segments(R);
         for (uint32_t g = 0; g < ns; g += REBIN_SEG_WARPS) bs.push_back(make_uint2(r, R.seg_off + g));
     }
+    if (bf.size() > f->blk_force.n || bs.size() > f->blk_seg.n)
+        f->drop_graphs();  // captured over the tables about to be replaced
     if (bf.size() > f->blk_force.n) {
         cudaError_t e = f->blk_force.alloc(std::max<size_t>(bf.size(), 2 * f->blk_force.n));
         if (e) return cuda_fail(e, "replica block table");

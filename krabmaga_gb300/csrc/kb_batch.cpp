@@ -17,14 +17,16 @@ struct kb_batch {
     kb_flock_params common{};  // query mode and arithmetic shared by the replicas
     std::vector<uint8_t> have;  // replica initialised
     struct GKey {
-        uint32_t launches, spl;
+        uint32_t launches, spl;  // spl 0: separate-kernel steps (launches = steps)
         int cur, a_last, virt;
+        uint64_t sig;  // separate kernels: the launch shapes the capture baked in
         bool operator<(const GKey& o) const {
             if (launches != o.launches) return launches < o.launches;
             if (spl != o.spl) return spl < o.spl;
             if (cur != o.cur) return cur < o.cur;
             if (a_last != o.a_last) return a_last < o.a_last;
-            return virt < o.virt;
+            if (virt != o.virt) return virt < o.virt;
+            return sig < o.sig;
         }
     };
     struct GVal {
@@ -158,7 +160,52 @@ kb_status kb_batch_step(kb_batch* b, uint64_t first_step, uint32_t nsteps, uint3
     if (!fused_eligible(f, p)) {
         if ((st = materialize(f))) return st;
         if ((st = grow(f, f->rn))) return st;
-        return enqueue_steps(f, p, nsteps, all_fast_rebin_ok(f) && f->layout_is_positions);
+        const bool fast = all_fast_rebin_ok(f) && f->layout_is_positions;
+        if (graph_launches <= 1 || !fast) return enqueue_steps(f, p, nsteps, fast);
+        // separate-kernel steps replayed from CUDA graphs of up to graph_launches
+        // steps (the kernels read the step number from device memory, so one
+        // capture serves every step range)
+        if (b->graph_epoch != f->graph_epoch) {
+            b->drop_graphs();
+            b->graph_epoch = f->graph_epoch;
+        }
+        uint32_t done = 0;
+        while (done < nsteps) {
+            const uint32_t k = std::min(graph_launches, nsteps - done);
+            if (k < 4) {
+                if ((st = enqueue_steps(f, p, k, fast))) return st;
+                done += k;
+                continue;
+            }
+            const uint64_t sig = ((uint64_t)f->force_block << 48) ^ ((uint64_t)f->nblk_force << 24) ^
+                                 (uint64_t)f->nblk_seg ^ ((uint64_t)f->rn << 8) ^
+                                 (f->ids_unique ? (1ull << 63) : 0ull);
+            kb_batch::GKey key{k, 0u, f->cur, 0, 0, sig};
+            auto it = b->graphs.find(key);
+            const int cur0 = f->cur;
+            if (it == b->graphs.end()) {
+                cudaGraph_t graph = nullptr;
+                KB_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
+                st = enqueue_steps(f, p, k, fast);
+                cudaError_t ce = cudaStreamEndCapture(f->stream, &graph);
+                f->cur = cur0;  // the capture recorded the swaps; the replay performs them
+                if (st) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return st;
+                }
+                if (ce) return cuda_fail(ce, "cudaStreamEndCapture");
+                cudaGraphExec_t exec = nullptr;
+                ce = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ce) return cuda_fail(ce, "cudaGraphInstantiate");
+                if (b->graphs.size() > 16) b->drop_graphs();
+                it = b->graphs.emplace(key, kb_batch::GVal{exec, (k & 1u) ? 1 - cur0 : cur0, 0}).first;
+            }
+            KB_CUDA(cudaGraphLaunch(it->second.exec, f->stream));
+            f->cur = it->second.cur;
+            done += k;
+        }
+        return KB_OK;
     }
     if ((st = grow(f, f->rn))) return st;
     if ((st = fused_prepare(f, p))) return st;

@@ -246,3 +246,24 @@ def test_mode0_autotune_picks_a_block_size_and_refuses_others(gpu):
         with pytest.raises(kg.KbError) as e:
             b.autotune(used, 2, candidates=bad)
         assert e.value.status == L.KB_ERR_ARG
+
+
+def test_mode0_graphs_follow_a_block_size_change(gpu):
+    # separate-kernel steps replayed from graphs, then a force block size set
+    # by the autotuner, then graphs again: the graphs captured before the
+    # change are not replayed after it, every replica still equals the oracle
+    reps = small_sweep(kg.KB_ARITH_STRICT)
+    b = kg.Batch(reps)
+    b.set_step_options(0)
+    b.step(0, 8, 1, 4)
+    done = 8
+    for threads in (512, 128):
+        t, _, used, _ = b.autotune(done, 1, candidates=[(threads, 1)])
+        assert t == threads
+        done += used
+        b.step(done, 9, 1, 4)
+        done += 9
+    for i, rep in enumerate(reps):
+        ids, st = b.get_replica(i)
+        oids, ost = oracle_run(rep, done)
+        assert np.array_equal(ids, oids) and same_bits(st, ost), f"replica {i}"
