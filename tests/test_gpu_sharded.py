@@ -195,3 +195,24 @@ def test_device_record_entry_points_match_the_host_ones(gpu):
     assert f.num_objects() == n
     for fld in (f, g, h, k):
         fld.close()
+
+
+def test_device_discretize_matches_the_reference_rounding(gpu):
+    """discretize_device on the GPU is floor(fl(v / d)) bit for bit at bag
+    edges (k * d and its neighbouring floats), where a product with the
+    reciprocal of d can land on the other side."""
+    import torch
+
+    from krabmaga_gb300.sharded import discretize, discretize_device
+
+    d = np.float32(D)
+    k = np.arange(1, 2000, dtype=np.float32)
+    edge = (k * d).astype(np.float32)
+    vals = np.concatenate([edge, np.nextafter(edge, np.float32(0)), np.nextafter(edge, np.float32(1e9)),
+                           np.random.default_rng(1).random(5000).astype(np.float32) * 6000])
+    got = discretize_device(torch.from_numpy(vals).cuda(), float(d)).cpu().numpy()
+    want = discretize(vals, float(d))
+    assert np.array_equal(got, want)
+    # the reciprocal product disagrees somewhere on these edges, so the test can tell them apart
+    rec = np.floor(vals * (np.float32(1) / d)).astype(np.int64)
+    assert (rec != want).any()
