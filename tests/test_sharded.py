@@ -172,3 +172,34 @@ def test_ranks_driven_in_one_process_equal_the_single_field():
         oids, ost = _single(case)
         assert np.array_equal(gids, oids)
         assert np.array_equal(gst.view(np.uint32), ost.view(np.uint32))
+
+
+def test_strips_in_the_exact_query_mode_and_a_wider_ring():
+    """The in-tree Bird's exact query (four-corner rule) and a radius of two
+    bags (dd = 2, two halo columns each side): still the single field's bits."""
+    import oracle
+
+    from krabmaga_gb300 import _lib as L
+    from krabmaga_gb300.model import FlockParams
+    from krabmaga_gb300.sharded import ShardedFlock
+
+    for qmode, radius in ((L.KB_QUERY_EXACT, 10.0), (L.KB_QUERY_RELAX, 14.0)):
+        n, side, seed, steps = 2500, 316.23, 21, 5
+        ids, xy, dxy = flock(n, side, seed)
+        p = FlockParams(seed=seed, jump=2.0, neighbor_radius=radius, query_mode=qmode)
+        world = 3
+        ranks = [ShardedFlock(side, D, p, ids, xy, dxy, make_local=OracleStrip, rank=r, world=world)
+                 for r in range(world)]
+        assert ranks[0].dd == (1 if radius == 10.0 else 2)
+        for k in range(steps):
+            parts = [sf.prepare(k) for sf in ranks]
+            for r, sf in enumerate(ranks):
+                sf.finish([parts[s][r] for s in range(world)])
+        own = [sf.owned_state() for sf in ranks]
+        o = oracle.OracleField(side, side, D, True)
+        o.set_many(ids, xy, dxy)
+        o.lazy_update()
+        o.flock_run(oracle.params_from(p), 0, steps)
+        oids, ost, _ = o.iter(1)
+        assert np.array_equal(np.concatenate([x[0] for x in own]), oids)
+        assert np.array_equal(np.concatenate([x[1] for x in own]).view(np.uint32), ost.view(np.uint32))
