@@ -204,9 +204,12 @@ kb_status grow(kb_field* f, uint32_t need) {
 }
 
 // First segment of each replica (Rep::seg_off), before any table upload.
+// Packed replicas take the packed segment height (Rep::seg_rows); a plain
+// field keeps the default (or the dense one, chosen per step).
 void assign_segments(std::vector<Rep>& reps) {
     uint32_t g = 0;
     for (Rep& R : reps) {
+        R.seg_rows = reps.size() > 1 ? PACKED_SEG_ROWS : 0;
         R.seg_off = g;
         g += rep_segments(R);
     }

@@ -52,7 +52,7 @@ struct Rep {
     uint32_t seg_off;       // first 32-bag column segment of this replica (segment rebin)
     unsigned long long dh_magic;  // ceil(2^64 / dh): n / dh == umul64hi(n, dh_magic) for n < 2^32
     int32_t cell_wrap;      // toroidal fields: 0 clamp the query's cell range (the reference), 1 wrap it
-    uint32_t _pad3;
+    int32_t seg_rows;       // bags per segment of the packed segment rebin (0: the default)
 };
 
 // ------------------------------------------------------------------ Philox

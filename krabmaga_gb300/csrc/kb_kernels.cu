@@ -799,7 +799,8 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 constexpr uint32_t FULL_MASK = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint32_t rep_segments_dev(const Rep& R) {
-    return (uint32_t)R.dw * (((uint32_t)R.dh + SEG_ROWS - 1) / SEG_ROWS);
+    const uint32_t rows = R.seg_rows > 0 ? (uint32_t)R.seg_rows : (uint32_t)SEG_ROWS;
+    return (uint32_t)R.dw * (((uint32_t)R.dh + rows - 1) / rows);
 }
 
 __device__ __forceinline__ int rep_of_seg(const Rep* reps, int nrep, uint32_t g) {
@@ -815,18 +816,34 @@ __device__ __forceinline__ int rep_of_seg(const Rep* reps, int nrep, uint32_t g)
 // Slot of one write-list entry of a batch of 32 (key k per lane, ~0u for
 // none) in its bag of the segment, or ~0u when the key is outside the
 // segment.  Every lane of the warp calls it.
-__device__ __forceinline__ uint32_t seg_rank(uint32_t k, uint32_t c0, int nb, uint32_t lo,
-                                             uint32_t hi, uint32_t* cnt, uint32_t lane_lt,
-                                             bool& bad) {
+// Bag offsets of a segment: lane l holds bag l (lo[0], hi[0]) and, with two
+// bags per lane (64-bag segments), bag l + 32 (lo[1], hi[1]).
+template <int BPL>
+struct SegBags {
+    uint32_t lo[BPL], hi[BPL];
+};
+
+template <int BPL>
+__device__ __forceinline__ uint32_t seg_rank(uint32_t k, uint32_t c0, int nb, const SegBags<BPL>& sb,
+                                             uint32_t* cnt, uint32_t lane_lt, bool& bad) {
     const uint32_t local = k - c0;
     const bool in = local < (uint32_t)nb;
     if (__ballot_sync(FULL_MASK, in) == 0u) return 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(FULL_MASK, in ? local : 0xFFFFFFFFu);
     const uint32_t rank = __popc(peers & lane_lt);
     const uint32_t src = local & 31u;
-    const uint32_t blo = __shfl_sync(FULL_MASK, lo, src);
-    const uint32_t bhi = __shfl_sync(FULL_MASK, hi, src);
-    const uint32_t base = in ? cnt[src] : 0u;
+    uint32_t blo = __shfl_sync(FULL_MASK, sb.lo[0], src);
+    uint32_t bhi = __shfl_sync(FULL_MASK, sb.hi[0], src);
+    if (BPL == 2) {
+        const uint32_t blo1 = __shfl_sync(FULL_MASK, sb.lo[BPL - 1], src);
+        const uint32_t bhi1 = __shfl_sync(FULL_MASK, sb.hi[BPL - 1], src);
+        if (local >= 32u) {
+            blo = blo1;
+            bhi = bhi1;
+        }
+    }
+    const uint32_t slot = BPL == 2 ? local : src;
+    const uint32_t base = in ? cnt[slot] : 0u;
     __syncwarp();
     uint32_t dst = 0xFFFFFFFFu;
     if (in) {
@@ -835,7 +852,7 @@ __device__ __forceinline__ uint32_t seg_rank(uint32_t k, uint32_t c0, int nb, ui
             bad = true;
             dst = 0xFFFFFFFFu;
         }
-        if (rank + 1u == (uint32_t)__popc(peers)) cnt[src] = base + rank + 1u;
+        if (rank + 1u == (uint32_t)__popc(peers)) cnt[slot] = base + rank + 1u;
     }
     __syncwarp();
     return dst;
@@ -846,22 +863,24 @@ __device__ __forceinline__ uint32_t seg_rank(uint32_t k, uint32_t c0, int nb, ui
 #define KB_REBIN_BATCHES 2
 #endif
 
+template <int BPL>
 __device__ __forceinline__ void seg_batch(const RebinArgs& a, bool valid, uint32_t p, uint32_t c0,
-                                          int nb, uint32_t lo, uint32_t hi, uint32_t* cnt,
+                                          int nb, const SegBags<BPL>& sb, uint32_t* cnt,
                                           uint32_t lane_lt, bool& bad) {
     const uint32_t k = valid ? __ldg(a.key + p) : 0xFFFFFFFFu;
-    const uint32_t dst = seg_rank(k, c0, nb, lo, hi, cnt, lane_lt, bad);
+    const uint32_t dst = seg_rank<BPL>(k, c0, nb, sb, cnt, lane_lt, bad);
     if (dst != 0xFFFFFFFFu) {
         a.s_st[dst] = __ldg(a.a_st + p);
         a.s_ids[dst] = __ldg(a.a_ids + p);
     }
 }
 
-// ROWS (<= 32) consecutive bags of one column per warp.
+// ROWS (<= 64) consecutive bags of one column per warp (one or two per lane).
 template <int ROWS>
 __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, uint32_t g,
                                               uint32_t* cnt) {
-    static_assert(ROWS >= 1 && ROWS <= 32, "a segment's bags map to the lanes of one warp");
+    static_assert(ROWS >= 1 && ROWS <= 64, "a segment's bags map to one or two per lane");
+    constexpr int BPL = ROWS > 32 ? 2 : 1;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t nsy = ((uint32_t)R.dh + ROWS - 1) / ROWS;
     const uint32_t local = g - R.seg_off;
@@ -874,17 +893,32 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
     const bool interior = X > 0 && X < R.seam && Y0 > 0 && Y1 < R.seam;
     // this segment's bag offsets and (interior) the bounds of its three
     // source runs, in one round trip
-    uint32_t lo = 0, hi = 0, b = 0;
-    if ((int)lane < nb) {
-        hi = min(__ldg(a.start_next + c0 + lane + 1), a.n);
-        lo = min(__ldg(a.start_next + c0 + lane), hi);
+    SegBags<BPL> sb;
+    uint32_t b = 0;
+#pragma unroll
+    for (int h = 0; h < BPL; ++h) {
+        sb.lo[h] = sb.hi[h] = 0u;
+        const int bag = (int)lane + 32 * h;
+        if (bag < nb) {
+            sb.hi[h] = min(__ldg(a.start_next + c0 + bag + 1), a.n);
+            sb.lo[h] = min(__ldg(a.start_next + c0 + bag), sb.hi[h]);
+        }
     }
     if (interior && lane < 6u) {
         const uint32_t cb = R.cell_off + (uint32_t)(X - 1 + (int)(lane % 3u)) * (uint32_t)R.dh;
         b = min(__ldg(a.start_cur + cb + (lane < 3u ? (uint32_t)(Y0 - 1) : (uint32_t)(Y1 + 2))), a.n);
     }
-    if (__shfl_sync(FULL_MASK, lo, 0) == __shfl_sync(FULL_MASK, hi, nb - 1)) return;  // no arrivals
-    cnt[lane] = 0u;
+    {
+        const uint32_t first = __shfl_sync(FULL_MASK, sb.lo[0], 0);
+        uint32_t last = __shfl_sync(FULL_MASK, sb.hi[0], (nb - 1) & 31);
+        if (BPL == 2) {
+            const uint32_t last1 = __shfl_sync(FULL_MASK, sb.hi[BPL - 1], (nb - 1) & 31);
+            if (nb > 32) last = last1;
+        }
+        if (first == last) return;  // no arrivals
+    }
+#pragma unroll
+    for (int h = 0; h < BPL; ++h) cnt[lane + 32 * h] = 0u;
     __syncwarp();
     const uint32_t lane_lt = (1u << lane) - 1u;
     bool bad = false;
@@ -908,7 +942,7 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
             }
 #pragma unroll
             for (int b = 0; b < KB_REBIN_BATCHES; ++b)
-                dst[b] = seg_rank(dst[b], c0, nb, lo, hi, cnt, lane_lt, bad);
+                dst[b] = seg_rank<BPL>(dst[b], c0, nb, sb, cnt, lane_lt, bad);
             float4 rec[KB_REBIN_BATCHES];
             uint32_t rid[KB_REBIN_BATCHES];
 #pragma unroll
@@ -950,11 +984,15 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
                 const uint32_t s = min(__ldg(a.start_cur + cb + (uint32_t)ra[r]), e);
 #pragma unroll 1
                 for (uint32_t f = s; f < e; f += 32u)
-                    seg_batch(a, f + lane < e, f + lane, c0, nb, lo, hi, cnt, lane_lt, bad);
+                    seg_batch<BPL>(a, f + lane < e, f + lane, c0, nb, sb, cnt, lane_lt, bad);
             }
         }
     }
-    if ((int)lane < nb && cnt[lane] != hi - lo) bad = true;
+#pragma unroll
+    for (int h = 0; h < BPL; ++h) {
+        const int bag = (int)lane + 32 * h;
+        if (bag < nb && cnt[bag] != sb.hi[h] - sb.lo[h]) bad = true;
+    }
     if (__any_sync(FULL_MASK, bad) && lane == 0u) atomicOr(a.err, ERR_REBIN_MISS | ERR_MISS_MATERIALIZE);
 }
 
@@ -962,10 +1000,15 @@ __device__ __forceinline__ void rebin_segment(const RebinArgs& a, const Rep& R, 
 #define KB_REBIN_MINB 6
 #endif
 
+#ifndef KB_REBIN_MINB_MULTI
+#define KB_REBIN_MINB_MULTI 6
+#endif
+
 template <bool MULTI, int ROWS = SEG_ROWS>
-__global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_seg(RebinArgs a) {
+__global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, MULTI ? KB_REBIN_MINB_MULTI : KB_REBIN_MINB)
+    k_rebin_seg(RebinArgs a) {
     pdl_enter();
-    __shared__ uint32_t s_cnt[REBIN_SEG_WARPS][32];
+    __shared__ uint32_t s_cnt[REBIN_SEG_WARPS][MULTI ? PACKED_SEG_ROWS : 32];
     const uint32_t w = threadIdx.x >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && a.step != nullptr) *a.step += 1ull;
     if (MULTI) {
@@ -975,8 +1018,9 @@ __global__ void __launch_bounds__(32 * REBIN_SEG_WARPS, KB_REBIN_MINB) k_rebin_s
         load_rep_shared(&sR, a.reps + e.x);
         __syncthreads();
         const uint32_t g = e.y + w;
+        // packed replicas always carry seg_rows == PACKED_SEG_ROWS (assign_segments)
         if (g >= sR.seg_off + rep_segments_dev(sR)) return;  // whole warps
-        rebin_segment<SEG_ROWS>(a, sR, g, s_cnt[w]);
+        rebin_segment<PACKED_SEG_ROWS>(a, sR, g, s_cnt[w]);
         return;
     }
     const uint32_t g = blockIdx.x * REBIN_SEG_WARPS + w;

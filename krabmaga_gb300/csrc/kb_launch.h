@@ -153,7 +153,13 @@ constexpr int SEG_ROWS = 32;
 // and the warp walks them in order, so fewer rows per warp shorten the tail.
 constexpr int DENSE_SEG_ROWS = 8;
 constexpr int REBIN_SEG_WARPS = 8;  // segments (warps) per block
-inline uint32_t rep_segments(const Rep& R, int rows = SEG_ROWS) {
+// Segments of the replicas of a packed batch: 64 bags (two per lane), half
+// as many segments as 32-bag ones (the packed rebin's time follows the
+// number of segments; measured on the 512-replica sweep).
+constexpr int PACKED_SEG_ROWS = 64;
+// rows 0: the replica's own segment height (Rep::seg_rows, else SEG_ROWS).
+inline uint32_t rep_segments(const Rep& R, int rows = 0) {
+    if (rows == 0) rows = R.seg_rows > 0 ? R.seg_rows : SEG_ROWS;
     return (uint32_t)R.dw * (((uint32_t)R.dh + (uint32_t)rows - 1) / (uint32_t)rows);
 }
 cudaError_t launch_rebin(const RebinArgs& a, cudaStream_t s);
