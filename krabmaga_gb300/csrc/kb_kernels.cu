@@ -733,6 +733,58 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     }
 }
 
+// The exclusive scan, in place, of ntiles tile sums (one block; large bag
+// matrices: the tiles then take their prefix with one load).
+constexpr int SUMS_THREADS = 1024;
+constexpr int SUMS_ITEMS = 8;
+__global__ void __launch_bounds__(SUMS_THREADS) k_scan_sums(unsigned long long* sums, uint32_t ntiles) {
+    pdl_enter();
+    __shared__ uint32_t s_warp[SUMS_THREADS / 32];
+    __shared__ uint32_t s_carry;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_carry = 0u;
+    __syncthreads();
+    for (uint64_t chunk = 0; chunk < ntiles; chunk += (uint64_t)SUMS_THREADS * SUMS_ITEMS) {
+        const uint64_t base = chunk + (uint64_t)tid * SUMS_ITEMS;
+        uint32_t v[SUMS_ITEMS], t = 0;
+#pragma unroll
+        for (int k = 0; k < SUMS_ITEMS; ++k) {
+            v[k] = base + k < ntiles ? (uint32_t)sums[base + k] : 0u;
+            t += v[k];
+        }
+        uint32_t x = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31u) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= (uint32_t)o) w += y;
+            }
+            s_warp[lane] = w;  // inclusive warp prefixes
+        }
+        __syncthreads();
+        uint32_t run = s_carry + (warp > 0 ? s_warp[warp - 1] : 0u) + x - t;
+#pragma unroll
+        for (int k = 0; k < SUMS_ITEMS; ++k) {
+            if (base + k < ntiles) sums[base + k] = (unsigned long long)run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (tid == 0) s_carry += s_warp[SUMS_THREADS / 32 - 1];
+        __syncthreads();
+    }
+}
+
+// PREFIX: sums[] already holds each tile's exclusive prefix (k_scan_sums);
+// otherwise the tile adds up the sums of the tiles before it.
+template <bool PREFIX>
 __global__ void __launch_bounds__(SCAN_THREADS)
     k_scan_tiles(uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n,
                  const unsigned long long* __restrict__ sums, int zero_in, uint32_t ntiles) {
@@ -741,7 +793,11 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     const uint32_t tile = blockIdx.x, tid = threadIdx.x;
     // this tile's prefix: the sums of the tiles before it
     uint32_t part = 0;
-    for (uint32_t k = tid; k < tile; k += SCAN_THREADS) part += (uint32_t)sums[k];
+    if (PREFIX) {
+        if (tid == 0) part = (uint32_t)sums[tile];
+    } else {
+        for (uint32_t k = tid; k < tile; k += SCAN_THREADS) part += (uint32_t)sums[k];
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) s_red[tid >> 5] = part;
@@ -1449,11 +1505,22 @@ cudaError_t launch_scan(const uint32_t* in, uint32_t* out, uint32_t n, ScanCtl* 
         return cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
     }
     const uint32_t nt2 = (n + SCAN2_TILE - 1) / SCAN2_TILE;
+    // tile_state holds scan_state_words(n) >= nt2 + 1 words: one sum per tile
     if (nt2 <= SCAN2_MAX_TILES) {
-        // tile_state holds scan_state_words(n) >= nt2 + 1 words: one sum per tile
         cudaError_t e = launch_pdl(k_tile_sums, nt2, SCAN_THREADS, s, in, n, tile_state);
         if (e != cudaSuccess) return e;
-        return launch_pdl(k_scan_tiles, nt2, SCAN_THREADS, s, const_cast<uint32_t*>(in), out, n,
+        return launch_pdl(k_scan_tiles<false>, nt2, SCAN_THREADS, s, const_cast<uint32_t*>(in), out, n,
+                          tile_state, zero_in ? 1 : 0, nt2);
+    }
+    // larger matrices: the tile sums scanned by one block in between (no
+    // waits); the single-pass look-back scan below serves the largest ones
+    // and the bounded-wait test of its look-back (wait.withhold)
+    if (nt2 <= SCAN3_MAX_TILES && wait.withhold == ~0u) {
+        cudaError_t e = launch_pdl(k_tile_sums, nt2, SCAN_THREADS, s, in, n, tile_state);
+        if (e != cudaSuccess) return e;
+        e = launch_pdl(k_scan_sums, 1u, (unsigned)SUMS_THREADS, s, tile_state, nt2);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(k_scan_tiles<true>, nt2, SCAN_THREADS, s, const_cast<uint32_t*>(in), out, n,
                           tile_state, zero_in ? 1 : 0, nt2);
     }
     return launch_pdl(k_scan, nt, SCAN_THREADS, s, in, out, n, ctl, tile_state, err, zero_in ? 1 : 0, nt,

@@ -29,6 +29,12 @@ constexpr uint32_t SCAN2_TILE = 256u * KB_SCAN2_ITEMS;
 #define KB_SCAN2_MAX 4096
 #endif
 constexpr uint32_t SCAN2_MAX_TILES = KB_SCAN2_MAX;
+// Above SCAN2_MAX_TILES tiles a third launch scans the tile sums (up to
+// SCAN3_MAX_TILES tiles, about 268 M bags); beyond it the look-back scan.
+#ifndef KB_SCAN3_MAX
+#define KB_SCAN3_MAX 262144
+#endif
+constexpr uint32_t SCAN3_MAX_TILES = KB_SCAN3_MAX;
 // 64-bit state words a scan of n items needs (either form).
 inline uint32_t scan_state_words(uint32_t n) {
     const uint32_t a = scan_tiles(n), b = (n + SCAN2_TILE - 1) / SCAN2_TILE;

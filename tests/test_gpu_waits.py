@@ -113,3 +113,21 @@ def test_wait_test_rejects_unknown_hooks(gpu):
         assert e.value.status == L.KB_ERR_ARG
     finally:
         f.close()
+
+
+def test_large_bag_matrices_scan_without_waits(gpu):
+    # over 4096 scan tiles the bag offsets take three launches (tile sums, one
+    # block scanning them, the tiles): 9 M bags need two rounds of that block
+    side, d, n = 1500.0, 0.5, 4000
+    ids, xy, dxy = kg.gen_uniform(n, side, side, 8, 1.0)
+    f = kg.Field2D(side, side, d, True, capacity_hint=n)
+    try:
+        f.set_locations(ids, xy, dxy)
+        f.lazy_update()
+        p = kg.FlockParams(seed=4, jump=0.3, neighbor_radius=1.0, arith=kg.KB_ARITH_STRICT)
+        step(f, p, 0, 3)
+        gids, gst = f.get_state()
+        oids, ost = oracle_state(side, d, ids, xy, dxy, p, 3)
+        assert np.array_equal(gids, oids) and same_bits(gst, ost)
+    finally:
+        f.close()
