@@ -296,7 +296,9 @@ kb_status kb_field_device_flags(kb_field* f, uint32_t* flags, int32_t clear);
  * used again once its state is set anew.  withhold (KB_WITHHOLD_*) is the test
  * hook that makes a wait run out on purpose, without any fault: the
  * look-back scan tile, or the block of the persistent step, numbered `index`
- * does not publish its signal. */
+ * does not publish its signal (KB_WITHHOLD_SCAN_PUBLISH also makes the bag
+ * offsets of any size go through the look-back scan, which otherwise serves
+ * the largest matrices only). */
 #define KB_WITHHOLD_NONE 0
 #define KB_WITHHOLD_SCAN_PUBLISH 1
 #define KB_WITHHOLD_GRID_ARRIVAL 2

@@ -1,8 +1,9 @@
 """Bounded device waits run out without a fault, and the field recovers.
 
 The library's kernels wait on one another in two places: the single-pass
-look-back scan of large bag matrices (a tile waits for its predecessors'
-published sums) and the persistent tiled step (blocks meet at grid barriers).
+look-back scan of the largest bag matrices (a tile waits for its
+predecessors' published sums; the scan test hook selects it for any size)
+and the persistent tiled step (blocks meet at grid barriers).
 Every such wait is bounded.  Here the test hook makes one publisher withhold
 its signal, with a short iteration limit, so that the waits give up on
 purpose: the kernel returns, the error word carries KB_FLAG_SPIN_TIMEOUT,
