@@ -111,3 +111,43 @@ def test_rank_zero_gathers_every_row_in_rank_order(world, case):
     for a, b in zip(got[0], expect):
         assert {k: v for k, v in a.items() if k not in TIMING} == \
             {k: v for k, v in b.items() if k not in TIMING}
+
+
+def _rank_edge(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world),
+                      RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import torch.distributed as dist
+
+    import krabmaga_gb300 as kg
+    from test_explore_distributed import oracle_runner
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        base = kg.FlockerConfig(initial_flockers=80, dim=60.0, init_seed=5)
+        # two configurations over three ranks (rank 2 gets none), rep_conf 0 counts as 1
+        rows = kg.explore_distributed(3, 0, {"jump": [0.4, 0.8]}, ["boids"],
+                                      kg.ExploreMode.Matched, base, device=0, runner=oracle_runner)
+        q.put((rank, rows))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_fewer_configurations_than_ranks_and_zero_repetitions():
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_edge, args=(r, 3, port, q)) for r in range(3)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=300) for _ in range(3))
+    for p in procs:
+        p.join(60)
+    assert all(p.exitcode == 0 for p in procs)
+    assert got[1] == [] and got[2] == []
+    rows = got[0]
+    assert [(r["Simulation"], r["Run"], r["jump"], r["boids"]) for r in rows] == \
+        [(0, 0, 0.4, 80), (0, 0, 0.8, 80)]
