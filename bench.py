@@ -294,8 +294,9 @@ def run_sweep(args, dev):
         "unit": UNIT, "batched_ms_per_step": best["ms_per_step"], "best_mode": best["mode"],
         "modes": runs,
         "launch": "mode 2: tile step + scan per step, CUDA graphs of 100 steps; mode 0: force + "
-                  "offsets scan (two launches) + rebin per step over all replicas, CUDA graphs "
-                  "of 100 steps, programmatic dependent launch between the kernels",
+                  "offsets scan (three launches at this bag count) + rebin (64-bag segments) per "
+                  "step over all replicas, CUDA graphs of 100 steps, programmatic dependent "
+                  "launch between the kernels",
         "data": "synthetic (seeded)", "l2": "working set larger than L2 (no flush)",
     }
 
